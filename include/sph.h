@@ -1,0 +1,186 @@
+/*
+ * sph.h -- C ABI of libsph, the sm_103a (GB300) engine for pyticles' SPH step:
+ * cell-list neighbour search -> summation density (short and long smoothing
+ * lengths) -> van der Waals pressure forces, artificial viscosity, heat flux
+ * and energy rates -> improved-Euler (or Euler / RK4) update -> periodic box.
+ *
+ * Plain C types only: no torch, no CUDA types in the signatures.  Pointers
+ * tagged `mem` are device pointers when mem == SPH_DEVICE (e.g. from
+ * torch.Tensor.data_ptr()) and host pointers when mem == SPH_HOST; the
+ * library copies host data on its own stream.  Every call returns an
+ * int status (SPH_OK == 0).  The library never keeps a pointer the caller
+ * passed in: state is copied into engine-owned, cell-sorted device arrays.
+ *
+ * Reference interfaces replaced (andrewcharles/pyticles, file:line):
+ *   sph_engine_create / sph_sim_add     SmoothParticleSystem.__init__   particles.py:271-359
+ *                                       SpamComplete.__init__            spam_complete_force.py:36-60
+ *   sph_advance                         SmoothParticleSystem.update      particles.py:459-494
+ *                                       integrator.imp_euler/euler/rk4   integrator.py:14-103
+ *                                       PeriodicBox.apply                box.py:33-47
+ *                                       apply_thermostat                 particles.py:450-457
+ *   sph_sim_derivatives                 SpamComplete.apply               spam_complete_force.py:63-183
+ *                                       (calc_sphforce3d call            spam_complete_force.py:158-165)
+ *                                       properties.spam_properties       properties.py:63-120
+ *                                       forces.SpamForce/CohesiveSpamForce forces.py:321-405
+ *   sph_sim_pair_count / export_pairs   VerletList.build + separations   neighbour_list.py:160-189, 63-83
+ */
+#ifndef PYTICLES_GB300_SPH_H
+#define PYTICLES_GB300_SPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+enum sph_status {
+    SPH_OK = 0,
+    SPH_EINVAL = 1,          /* bad argument (size, dim, kernel, box ...)       */
+    SPH_ENOMEM = 2,          /* device allocation failed or HBM budget exceeded */
+    SPH_ECELL_OVERFLOW = 3,  /* a cell holds more particles than a kernel can stage */
+    SPH_ETIMEOUT = 4,        /* a bounded device wait gave up                    */
+    SPH_ENAN = 5,            /* a non-finite density, pressure or rate appeared  */
+    SPH_ECUDA = 6,           /* a CUDA runtime call failed                       */
+    SPH_ESKIN = 7,           /* a particle moved further within one step than the
+                                cell slack allows (cell list would miss pairs)   */
+    SPH_ECAPACITY = 8,       /* engine particle / simulation capacity exceeded  */
+    SPH_ENOTFOUND = 9        /* unknown simulation id                           */
+};
+
+/* Kernel ids follow spkernel.ktable (spkernel.py:20): 1 gaussian, 2 lucy,
+ * 3 debrun; 4 is the M4 cubic spline (support 2h), which pyticles lacks. */
+enum sph_kernel {
+    SPH_KERNEL_GAUSSIAN = 1,
+    SPH_KERNEL_LUCY = 2,
+    SPH_KERNEL_DEBRUN = 3,
+    SPH_KERNEL_CUBIC = 4
+};
+
+/* Arithmetic of the pair passes.  SPH_FP64: everything in FP64.
+ * SPH_MIXED: FP32 pair arithmetic on cell-local coordinates with
+ * compensated FP32 per-particle sums; FP64 pair-set test (exact fallback
+ * for borderline pairs), FP64 integrator and FP64 global reductions. */
+enum sph_precision { SPH_FP64 = 0, SPH_MIXED = 1 };
+
+/* integrator names follow particles.py:119-121 */
+enum sph_integrator { SPH_EULER = 0, SPH_IEULER = 1, SPH_RK4 = 2 };
+
+enum sph_memory { SPH_DEVICE = 0, SPH_HOST = 1 };
+
+/* Per-simulation parameters (POD).  dim, kernel, viscosity, heat_flux and
+ * integrator must agree across all simulations of one engine; the rest may
+ * differ per simulation. */
+typedef struct sph_params {
+    int32_t dim;            /* 2 or 3                                                */
+    int32_t kernel;         /* enum sph_kernel                                       */
+    int32_t viscosity;      /* 1: Monaghan (1992) artificial viscosity, short h     */
+    int32_t heat_flux;      /* 1: Fourier heat flux q and conduction energy rate    */
+    int32_t thermostat;     /* 1: scaling thermostat after every step               */
+    int32_t integrator;     /* enum sph_integrator                                   */
+    double box[3];          /* periodic extents xmax, ymax, zmax (box.py:18-22)     */
+    double h_short;         /* repulsive smoothing length  (particles.py:286, p.h)  */
+    double h_long;          /* cohesive smoothing length   (particles.py:287, p.hlr)*/
+    double cutoff;          /* pair set: rsq < cutoff^2 + tolerance^2               */
+    double tolerance;       /*   (neighbour_list.py:153-157, 178)                   */
+    double adash, bdash, kbdash;   /* van der Waals a, b, k_B (properties.py:18-20) */
+    double visc_alpha;      /* Monaghan alpha (SpamComplete eta)                    */
+    double visc_beta;       /* Monaghan beta  (SpamComplete zeta)                   */
+    double visc_eps;        /* epsilon in mu = h v.r / (r^2 + eps h^2)              */
+    double sound_speed;     /* c in the viscosity (spam_complete_force.py:142: 1)   */
+    double thermalk;        /* conductivity kappa (f_properties.py:14)              */
+    double dt;              /* time step                                             */
+    double thermostat_temp;      /* target temperature at step 0                    */
+    double thermostat_temp_end;  /* target after thermostat_ramp_steps (linear)     */
+    int64_t thermostat_ramp_steps;
+} sph_params;
+
+typedef struct sph_engine sph_engine;
+
+/* Creates an engine for up to max_particles particles in up to max_sims
+ * simulations of the same dim/kernel/flags as `group`.  stream is a
+ * cudaStream_t (NULL: the engine creates its own non-blocking stream).
+ * Device scratch is allocated here and grown by sph_sim_add if needed. */
+int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precision,
+                      int64_t max_particles, int32_t max_sims, void *stream);
+int sph_engine_destroy(sph_engine *e);
+
+/* Adds a simulation of n particles.  r and v are n x dim row-major
+ * (the layout of ParticleSystem.r / .v), m and u have length n.
+ * Positions must lie within [-box/4, 5 box/4] per axis (the teleport wrap
+ * keeps them in [0, box] once stepping).  Writes its id to *sim_id. */
+int sph_sim_add(sph_engine *e, const sph_params *p, int64_t n, const double *r,
+                const double *v, const double *m, const double *u, int32_t mem,
+                int32_t *sim_id);
+int sph_sim_remove(sph_engine *e, int32_t sim_id);
+/* Replaces the state of an existing simulation (same n). */
+int sph_sim_set_state(sph_engine *e, int32_t sim_id, const double *r, const double *v,
+                      const double *m, const double *u, int32_t mem);
+/* Reads the state back in the caller's original particle order.
+ * Any pointer may be NULL to skip it. */
+int sph_sim_get_state(sph_engine *e, int32_t sim_id, double *r, double *v, double *u,
+                      int32_t mem);
+/* Reads the per-particle properties left by the last step, with the
+ * reference's semantics: rho, p, pco of the step's first evaluation
+ * (scatter_state restores them, particles.py:513-526) and t, rho_lr,
+ * vdot, udot, jq of the last evaluation.  Any pointer may be NULL. */
+int sph_sim_get_properties(sph_engine *e, int32_t sim_id, double *rho, double *rho_lr,
+                           double *t, double *p, double *pco, double *vdot, double *udot,
+                           double *jq, int32_t mem);
+int sph_sim_count(sph_engine *e, int32_t sim_id, int64_t *n);
+
+/* Advances every simulation by nsteps steps of its integrator, applying
+ * the periodic box after each step and the thermostat when enabled. */
+int sph_advance(sph_engine *e, int32_t nsteps);
+
+/* One derivative evaluation f(x) of every simulation at its current state
+ * (no state change), then copies simulation sim_id's results out in the
+ * caller's order.  vdot and jq are n x dim.  Any pointer may be NULL. */
+int sph_sim_derivatives(sph_engine *e, int32_t sim_id, double *rho, double *rho_lr,
+                        double *t, double *p, double *pco, double *vdot, double *udot,
+                        double *jq, int32_t mem);
+
+/* Number of unordered pairs (i<j) in the pair set at the current state. */
+int sph_sim_pair_count(sph_engine *e, int32_t sim_id, int64_t *nip);
+/* Exports the pair set with NeighbourList attributes: iap (nip x 2, int64,
+ * i<j, original indices), drij (nip x dim, r_j - r_i minimum-imaged), rsq
+ * (nip), dv (nip x dim, v_j - v_i).  Pairs are ordered by (i, j).  cap is
+ * the capacity in pairs; *nip receives the count (SPH_ECAPACITY if larger
+ * than cap).  Any array pointer may be NULL. */
+int sph_sim_export_pairs(sph_engine *e, int32_t sim_id, int64_t cap, int64_t *iap,
+                         double *drij, double *rsq, double *dv, int64_t *nip, int32_t mem);
+
+/* Sum over all simulations of the pair-set size seen by the last
+ * evaluation pass (the metric's unit of work). */
+int sph_last_pair_total(sph_engine *e, int64_t *pairs);
+
+/* Per-simulation diagnostics of the current state, FP64 reductions:
+ * out[0] kinetic energy, out[1] internal energy, out[2..4] momentum,
+ * out[5] mean temperature of the last evaluation. */
+int sph_sim_diagnostics(sph_engine *e, int32_t sim_id, double out[6]);
+
+/* Tuning knobs of the pair passes (chosen by the autotuner). */
+typedef struct sph_tuning {
+    int32_t block_size;       /* threads per block of the pair passes        */
+    int32_t cells_per_warp;   /* reserved for the staged sweep; 0 = auto     */
+    double cell_ratio;        /* cell edge / pair cutoff lower bound (>=1)    */
+    int32_t use_graph;        /* capture each advance chunk as a CUDA graph   */
+    int32_t steps_per_graph;  /* steps unrolled into one graph                */
+} sph_tuning;
+int sph_get_tuning(sph_engine *e, sph_tuning *t);
+int sph_set_tuning(sph_engine *e, const sph_tuning *t);
+
+/* Waits for the engine's stream; returns the first device-side error
+ * (SPH_ENAN, SPH_ESKIN, ...) raised since the last call, then clears it. */
+int sph_sync(sph_engine *e);
+/* Per-simulation device error word (0 = ok). */
+int sph_sim_status(sph_engine *e, int32_t sim_id, int32_t *status);
+
+const char *sph_status_string(int status);
+int sph_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYTICLES_GB300_SPH_H */

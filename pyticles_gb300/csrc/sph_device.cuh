@@ -1,0 +1,167 @@
+// sph_device.cuh -- device helpers shared by the binning and pair kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sph_internal.h"
+
+namespace sph {
+
+template <typename R> struct V4;
+template <> struct V4<float> { using T = float4; };
+template <> struct V4<double> { using T = double4_32a; };
+
+template <typename R>
+__device__ __forceinline__ typename V4<R>::T make_v4(R x, R y, R z, R w) {
+    typename V4<R>::T o;
+    o.x = x; o.y = y; o.z = z; o.w = w;
+    return o;
+}
+
+// Cell coordinate of position x on axis a: the position is first wrapped
+// into [0, L) (shift = L floor(x/L)), then binned with the cell edge.  The
+// binning kernel and every pass that needs a particle's cell centre call
+// this same function so the results agree bit for bit.
+__device__ __forceinline__ int cell_coord(double x, const SimDev &S, int a, double *shift) {
+    double k = floor(x * (1.0 / S.L[a]));
+    double sh = k * S.L[a];
+    double xw = x - sh;
+    int ci = (int)(xw * S.inv_edge[a]);
+    if (ci < 0) ci = 0;
+    if (ci >= S.nc[a]) ci = S.nc[a] - 1;
+    *shift = sh;
+    return ci;
+}
+
+__device__ __forceinline__ double cell_centre(int ci, const SimDev &S, int a) {
+    return ((double)ci + 0.5) * S.edge[a];
+}
+
+// The reference's FP64 pair test (neighbour_list.py:168-178): dr = r_j - r_i,
+// one minimum-image shift per axis with strict comparisons against L/2,
+// rsq = dx*dx + dy*dy (+ dz*dz) summed left to right, no FMA contraction.
+template <int D>
+__device__ __forceinline__ double exact_rsq(double *const xe[3], const SimDev &S, int i, int j) {
+    double rsq = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double d = __dsub_rn(xe[a][j], xe[a][i]);
+        if (d > S.half_L[a]) d = __dsub_rn(d, S.L[a]);
+        if (d < -S.half_L[a]) d = __dadd_rn(d, S.L[a]);
+        double sq = __dmul_rn(d, d);
+        rsq = (a == 0) ? sq : __dadd_rn(rsq, sq);
+    }
+    return rsq;
+}
+
+// Compensated (Kahan) accumulation for FP32 sums; FP64 sums are plain.
+template <typename R> struct Acc;
+template <> struct Acc<float> {
+    float s, c;
+    __device__ __forceinline__ void init(float x) { s = x; c = 0.0f; }
+    __device__ __forceinline__ void add(float x) {
+        float y = __fsub_rn(x, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ float get() const { return s; }
+};
+template <> struct Acc<double> {
+    double s;
+    __device__ __forceinline__ void init(double x) { s = x; }
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double get() const { return s; }
+};
+
+// Fast-test bounds around the pair threshold.  In mixed mode the squared
+// distance comes from FP32 cell-local coordinates whose error is below
+// 5e-6 relative for cell edges up to twice the cutoff; pairs whose FP32
+// rsq lies within 2^-12 of the threshold are re-tested exactly in FP64.
+template <typename R> struct Margin;
+template <> struct Margin<float> { static constexpr double rel = 1.0 / 4096.0; };
+template <> struct Margin<double> { static constexpr double rel = 1e-9; };
+
+// ---- smoothing kernels: W(r) and g = (dW/dr)/r, so dwdx = g (r_j - r_i) ----
+// Lucy (spkernel.py:86-118), Gaussian (spkernel.py:39-52, Lucy's gradient
+// sign), Debrun (spkernel.py:120-153), M4 cubic spline (support 2h).
+template <typename R> struct KConst {
+    R h, inv_h, sig, g0;  // g0: Lucy -12 sig/h^2, Gaussian -2/h^2, cubic sig/h^2
+};
+
+template <typename R>
+__device__ __forceinline__ KConst<R> make_kconst(int K, double h, double sig) {
+    KConst<R> k;
+    k.h = (R)h;
+    k.inv_h = (R)(1.0 / h);
+    k.sig = (R)sig;
+    if (K == SPH_KERNEL_LUCY) k.g0 = (R)(-12.0 * sig / (h * h));
+    else if (K == SPH_KERNEL_GAUSSIAN) k.g0 = (R)(-2.0 / (h * h));
+    else if (K == SPH_KERNEL_CUBIC) k.g0 = (R)(sig / (h * h));
+    else k.g0 = (R)(-3.0 * sig);
+    return k;
+}
+
+template <typename R> __device__ __forceinline__ R rexp(R x);
+template <> __device__ __forceinline__ float rexp<float>(float x) { return expf(x); }
+template <> __device__ __forceinline__ double rexp<double>(double x) { return exp(x); }
+template <typename R> __device__ __forceinline__ R rsqrt_(R x);
+template <> __device__ __forceinline__ float rsqrt_<float>(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double rsqrt_<double>(double x) { return sqrt(x); }
+
+template <int K, typename R>
+__device__ __forceinline__ void kernel_wg(const KConst<R> &k, R r, R *w, R *g) {
+    if (K == SPH_KERNEL_LUCY) {
+        R q = r * k.inv_h;
+        if (q < (R)1) {
+            R s = (R)1 - q;
+            R s2 = s * s;
+            *w = k.sig * ((R)1 + (R)3 * q) * (s2 * s);
+            *g = k.g0 * s2;
+        } else {
+            *w = (R)0;
+            *g = (R)0;
+        }
+    } else if (K == SPH_KERNEL_GAUSSIAN) {
+        R q = r * k.inv_h;
+        R e = k.sig * rexp<R>(-q * q);
+        *w = e;
+        *g = k.g0 * e;
+    } else if (K == SPH_KERNEL_DEBRUN) {
+        if (r < k.h) {
+            R s = k.h - r;
+            *w = k.sig * s * s * s;
+            *g = (r > (R)0) ? k.g0 * s * s / r : (R)0;
+        } else {
+            *w = (R)0;
+            *g = (R)0;
+        }
+    } else {  // cubic spline
+        R q = r * k.inv_h;
+        if (q < (R)1) {
+            *w = k.sig * ((R)1 - (R)1.5 * q * q + (R)0.75 * q * q * q);
+            *g = k.g0 * ((R)-3 + (R)2.25 * q);
+        } else if (q < (R)2) {
+            R s = (R)2 - q;
+            *w = (R)0.25 * k.sig * s * s * s;
+            *g = (R)-0.75 * k.sig * s * s * k.inv_h / r;
+        } else {
+            *w = (R)0;
+            *g = (R)0;
+        }
+    }
+}
+
+template <int K, typename R>
+__device__ __forceinline__ R kernel_g(const KConst<R> &k, R r) {
+    R w, g;
+    kernel_wg<K, R>(k, r, &w, &g);
+    return g;
+}
+
+__device__ __forceinline__ void set_err(int *err, int *err_any, int s, int code) {
+    atomicCAS(&err[s], 0, code);
+    atomicCAS(err_any, 0, code);
+}
+
+}  // namespace sph

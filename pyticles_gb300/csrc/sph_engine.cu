@@ -1,0 +1,1125 @@
+// sph_engine.cu -- host side of libsph: the engine object behind the C ABI
+// declared in include/sph.h.
+//
+// One engine holds many simulations of the same dim / kernel / flags in
+// flattened device arrays.  A step is: counting-sort binning of every
+// simulation's particles into its own Morton-ordered cell range (one global
+// cell table), then per integrator stage a density pass, an optional heat
+// pass and a force pass whose epilogue writes the next stage's state (or the
+// final state with the periodic wrap and thermostat).  The step is captured
+// once as a CUDA graph and replayed; the graph is rebuilt when simulations
+// join or leave.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "sph_internal.h"
+
+using namespace sph;
+
+namespace {
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) {                                   \
+            fprintf(stderr, "libsph: %s failed: %s (%s:%d)\n", #call, \
+                    cudaGetErrorString(_e), __FILE__, __LINE__);   \
+            return SPH_ECUDA;                                      \
+        }                                                          \
+    } while (0)
+
+#define TRY(call)                 \
+    do {                          \
+        int _st = (call);         \
+        if (_st != SPH_OK) return _st; \
+    } while (0)
+
+struct Sim {
+    sph_params prm;
+    int64_t n = 0;
+    bool active = false;
+    int nc[3] = {1, 1, 1};
+    double edge[3] = {1, 1, 1};
+    int ncells = 0;
+    std::vector<int> morton;   // linear cell -> Morton rank
+    std::vector<int> rank_lin; // Morton rank -> linear cell
+    int cell_off = 0;
+    int part_off = 0;          // B layout
+    int a_off = 0;             // contiguous range in A
+    int64_t steps = 0;
+    double vmax = 0.0;
+};
+
+template <typename T>
+int dalloc(T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return SPH_ENOMEM;
+    }
+    return SPH_OK;
+}
+
+}  // namespace
+
+struct sph_engine {
+    sph_params group;
+    int precision = SPH_MIXED;
+    int dim = 2, nb = 9, nstage = 2;
+    size_t rsize = 4, v4size = 16;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t cap_p = 0;
+    int cap_s = 0;
+    int64_t cap_c = 0;
+    int64_t cap_chunks = 0;
+    sph_tuning tune;
+
+    std::vector<Sim> sims;        // indexed by id (device slot)
+    bool layout_dirty = true;
+    int np_b = 0;                 // particles in the current B layout
+    int a_extent = 0;             // used extent of A
+    int ncells_total = 0;
+    int nchunks = 0;
+    bool any_thermostat = false;
+
+    // device buffers
+    double *a_pos[3] = {}, *a_vel[3] = {}, *a_u = nullptr, *a_m = nullptr;
+    int *a_id = nullptr, *a_sim = nullptr;
+    double *b_pos[3] = {}, *b_vel[3] = {}, *b_u = nullptr, *b_m = nullptr;
+    int *b_id = nullptr, *b_sim = nullptr;
+    int *cell_of = nullptr, *rank = nullptr, *order_tmp = nullptr, *order = nullptr;
+    int *cell_b = nullptr;
+    int *cell_count = nullptr, *cell_start = nullptr, *nbr = nullptr, *morton = nullptr;
+    int *scan_tmp = nullptr;
+    void *pk_pos[2] = {}, *pk_vel[2] = {}, *pk_f = nullptr, *pk_q = nullptr;
+    double *xe[2][3] = {}, *ve[3] = {}, *ue = nullptr;
+    void *rho = nullptr, *rho_l = nullptr, *temp = nullptr, *pres = nullptr, *pco = nullptr;
+    void *rho0 = nullptr, *pres0 = nullptr, *pco0 = nullptr;
+    void *q[3] = {}, *vdot[3] = {}, *udot = nullptr, *f0v[3] = {}, *f0u = nullptr;
+    double *acc_r[3] = {}, *acc_v[3] = {}, *acc_u = nullptr;
+    double *stage_buf = nullptr;  // AoS staging (cap_p * 3 doubles)
+    SimDev *sims_d = nullptr;
+    double *t_scale = nullptr, *tsum_part = nullptr;
+    long long *steps_d = nullptr;
+    unsigned long long *pair_count = nullptr;
+    int *err = nullptr, *err_any = nullptr;
+    int *chunk_sim = nullptr, *chunk_start = nullptr, *chunk_len = nullptr;
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_steps = 0;
+    bool props_valid = false;
+};
+
+namespace {
+
+int nstage_of(int integ) { return integ == SPH_EULER ? 1 : (integ == SPH_RK4 ? 4 : 2); }
+
+double kernel_sigma(int kernel, int dim, double h) {
+    const double pi = 3.14159265358979323846;
+    switch (kernel) {
+        case SPH_KERNEL_LUCY:
+            return dim == 2 ? 5.0 / (pi * h * h) : 105.0 / (pi * 16.0 * (h * h * h));
+        case SPH_KERNEL_GAUSSIAN:
+            return 1.0 / (std::pow(h, dim) * std::pow(pi, dim / 2.0));
+        case SPH_KERNEL_DEBRUN: {
+            double h2 = h * h, h6 = h2 * h2 * h2;
+            return dim == 2 ? 10.0 / (pi * h6) : 15.0 / (pi * h6);
+        }
+        default:
+            return dim == 2 ? 10.0 / (7.0 * pi * h * h) : 1.0 / (pi * h * h * h);
+    }
+}
+
+double kernel_w0(int kernel, int dim, double h) {
+    double sig = kernel_sigma(kernel, dim, h);
+    switch (kernel) {
+        case SPH_KERNEL_DEBRUN: return sig * h * h * h;
+        default: return sig;  // Lucy, Gaussian, cubic spline: W(0) = sigma
+    }
+}
+
+uint64_t part1by1(uint64_t x) {
+    x &= 0xffffffffull;
+    x = (x | (x << 16)) & 0x0000ffff0000ffffull;
+    x = (x | (x << 8)) & 0x00ff00ff00ff00ffull;
+    x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0full;
+    x = (x | (x << 2)) & 0x3333333333333333ull;
+    x = (x | (x << 1)) & 0x5555555555555555ull;
+    return x;
+}
+
+uint64_t part1by2(uint64_t x) {
+    x &= 0x1fffffull;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+int validate_params(const sph_engine *e, const sph_params *p) {
+    if (p->dim != e->dim || p->kernel != e->group.kernel || p->viscosity != e->group.viscosity ||
+        p->heat_flux != e->group.heat_flux || p->integrator != e->group.integrator)
+        return SPH_EINVAL;
+    for (int a = 0; a < p->dim; ++a)
+        if (!(p->box[a] > 0.0) || !std::isfinite(p->box[a])) return SPH_EINVAL;
+    if (!(p->h_short > 0) || !(p->h_long > 0) || !(p->cutoff > 0) || p->tolerance < 0)
+        return SPH_EINVAL;
+    if (!(p->kbdash > 0) || !(p->dt > 0)) return SPH_EINVAL;
+    return SPH_OK;
+}
+
+// Cell grid of one simulation: edge >= cutoff * ratio plus room for the
+// largest displacement of one step (8 dt vmax), at least 3 cells per axis or
+// else a single cell on that axis (the pass then applies the minimum image).
+void make_grid(Sim &S, int dim, double ratio) {
+    double rc = std::sqrt(S.prm.cutoff * S.prm.cutoff + S.prm.tolerance * S.prm.tolerance);
+    double need = rc * std::max(1.0, ratio) + 8.0 * S.prm.dt * S.vmax;
+    need *= (1.0 + 1e-9);
+    S.ncells = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (a >= dim) {
+            S.nc[a] = 1;
+            S.edge[a] = 1.0;
+            continue;
+        }
+        int nc = (int)std::floor(S.prm.box[a] / need);
+        if (nc < 3) nc = 1;
+        S.nc[a] = nc;
+        S.edge[a] = S.prm.box[a] / nc;
+        S.ncells *= nc;
+    }
+    // Morton order of the grid cells
+    std::vector<std::pair<uint64_t, int>> codes(S.ncells);
+    for (int c = 0; c < S.ncells; ++c) {
+        int cx = c % S.nc[0], cy = (c / S.nc[0]) % S.nc[1], cz = c / (S.nc[0] * S.nc[1]);
+        uint64_t code = dim == 2 ? (part1by1(cx) | (part1by1(cy) << 1))
+                                 : (part1by2(cx) | (part1by2(cy) << 1) | (part1by2(cz) << 2));
+        codes[c] = {code, c};
+    }
+    std::sort(codes.begin(), codes.end());
+    S.morton.assign(S.ncells, 0);
+    S.rank_lin.assign(S.ncells, 0);
+    for (int r = 0; r < S.ncells; ++r) {
+        S.morton[codes[r].second] = r;
+        S.rank_lin[r] = codes[r].second;
+    }
+}
+
+SimDev make_simdev(const sph_engine *e, const Sim &S) {
+    SimDev d;
+    memset(&d, 0, sizeof(d));
+    const sph_params &p = S.prm;
+    double rc = std::sqrt(p.cutoff * p.cutoff + p.tolerance * p.tolerance);
+    for (int a = 0; a < 3; ++a) {
+        d.L[a] = p.box[a];
+        d.half_L[a] = p.box[a] / 2.;
+        d.edge[a] = S.edge[a];
+        d.inv_edge[a] = 1.0 / S.edge[a];
+        d.nc[a] = S.nc[a];
+        d.slack_half[a] = (a < e->dim) ? (S.nc[a] >= 3 ? 0.5 * (S.edge[a] - rc) : 1e300) : 1e300;
+        if (a < e->dim && S.nc[a] == 1) d.small_mask |= (1 << a);
+    }
+    d.active = S.active ? 1 : 0;
+    d.cell_off = S.cell_off;
+    d.ncells = S.ncells;
+    d.part_off = S.part_off;
+    d.n = (int)S.n;
+    d.nbr_count = e->nb;
+    d.thermostat = p.thermostat;
+    d.thr = p.cutoff * p.cutoff + p.tolerance * p.tolerance;
+    d.hs = p.h_short;
+    d.hl = p.h_long;
+    d.sig_s = kernel_sigma(p.kernel, e->dim, p.h_short);
+    d.sig_l = kernel_sigma(p.kernel, e->dim, p.h_long);
+    d.ws0 = kernel_w0(p.kernel, e->dim, p.h_short);
+    d.wl0 = kernel_w0(p.kernel, e->dim, p.h_long);
+    d.a = p.adash;
+    d.b = p.bdash;
+    d.kb = p.kbdash;
+    d.alpha = p.visc_alpha;
+    d.beta = p.visc_beta;
+    d.eps = p.visc_eps;
+    d.c = p.sound_speed;
+    d.kappa = p.thermalk;
+    d.dt = p.dt;
+    d.T0 = p.thermostat_temp;
+    d.T1 = p.thermostat_temp_end;
+    d.ramp = p.thermostat_ramp_steps;
+    return d;
+}
+
+void free_graph(sph_engine *e) {
+    if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    e->graph_exec = nullptr;
+    e->graph = nullptr;
+    e->graph_steps = 0;
+}
+
+int alloc_cells(sph_engine *e, int64_t cells) {
+    if (cells <= e->cap_c) return SPH_OK;
+    int64_t c = std::max<int64_t>(cells, e->cap_c * 2);
+    cudaFree(e->cell_count);
+    cudaFree(e->cell_start);
+    cudaFree(e->nbr);
+    cudaFree(e->morton);
+    cudaFree(e->scan_tmp);
+    e->cap_c = 0;
+    TRY(dalloc(&e->cell_count, c));
+    TRY(dalloc(&e->cell_start, c + 1));
+    TRY(dalloc(&e->nbr, c * e->nb));
+    TRY(dalloc(&e->morton, c));
+    TRY(dalloc(&e->scan_tmp, c / 4096 + 2));
+    e->cap_c = c;
+    free_graph(e);
+    return SPH_OK;
+}
+
+View make_view(const sph_engine *e) {
+    View v;
+    memset(&v, 0, sizeof(v));
+    v.np = e->np_b;
+    v.dim = e->dim;
+    v.sims = e->sims_d;
+    for (int a = 0; a < 3; ++a) {
+        v.a_pos[a] = e->a_pos[a];
+        v.a_vel[a] = e->a_vel[a];
+        v.b_pos[a] = e->b_pos[a];
+        v.b_vel[a] = e->b_vel[a];
+        v.q[a] = e->q[a];
+        v.vdot[a] = e->vdot[a];
+        v.f0v[a] = e->f0v[a];
+        v.acc_r[a] = e->acc_r[a];
+        v.acc_v[a] = e->acc_v[a];
+    }
+    v.a_u = e->a_u;
+    v.a_m = e->a_m;
+    v.a_id = e->a_id;
+    v.a_sim = e->a_sim;
+    v.b_u = e->b_u;
+    v.b_m = e->b_m;
+    v.b_id = e->b_id;
+    v.b_sim = e->b_sim;
+    v.cell_of = e->cell_of;
+    v.rank = e->rank;
+    v.order_tmp = e->order_tmp;
+    v.order = e->order;
+    v.cell_count = e->cell_count;
+    v.cell_start = e->cell_start;
+    v.cell_b = e->cell_b;
+    v.nbr = e->nbr;
+    v.morton = e->morton;
+    v.pk_f = e->pk_f;
+    v.pk_q = e->pk_q;
+    v.rho = e->rho;
+    v.rho_l = e->rho_l;
+    v.temp = e->temp;
+    v.pres = e->pres;
+    v.pco = e->pco;
+    v.rho0 = e->rho0;
+    v.pres0 = e->pres0;
+    v.pco0 = e->pco0;
+    v.udot = e->udot;
+    v.f0u = e->f0u;
+    v.acc_u = e->acc_u;
+    v.tsum_part = e->tsum_part;
+    v.chunk_sim = e->chunk_sim;
+    v.chunk_start = e->chunk_start;
+    v.chunk_len = e->chunk_len;
+    v.nchunks = e->nchunks;
+    v.t_scale = e->t_scale;
+    v.steps = e->steps_d;
+    v.pair_count = e->pair_count;
+    v.err = e->err;
+    v.err_any = e->err_any;
+    return v;
+}
+
+// Evaluation buffers of stage s: stage 0 reads the permuted x0 (B) and
+// packed buffer 0; stage s >= 1 reads what stage s-1's force pass wrote.
+void stage_view(const sph_engine *e, View &v, int s) {
+    int pin = s & 1, pout = (s + 1) & 1;
+    v.pk_pos_in = e->pk_pos[pin];
+    v.pk_vel_in = e->pk_vel[pin];
+    v.pk_pos_out = e->pk_pos[pout];
+    v.pk_vel_out = e->pk_vel[pout];
+    for (int a = 0; a < 3; ++a) {
+        v.xe_in[a] = s == 0 ? e->b_pos[a] : e->xe[(s - 1) & 1][a];
+        v.xe_out[a] = e->xe[s & 1][a];
+        v.ve_in[a] = s == 0 ? e->b_vel[a] : e->ve[a];
+        v.ve_out[a] = e->ve[a];
+    }
+    v.ue_in = s == 0 ? e->b_u : e->ue;
+    v.ue_out = e->ue;
+}
+
+// Rebuilds the host-side layout: cell offsets, concatenated Morton and
+// neighbour tables, particle offsets and reduction chunks; uploads them.
+int relayout(sph_engine *e) {
+    int cell_off = 0, part_off = 0;
+    e->any_thermostat = false;
+    for (auto &S : e->sims) {
+        if (!S.active) continue;
+        S.cell_off = cell_off;
+        S.part_off = part_off;
+        cell_off += S.ncells;
+        part_off += (int)S.n;
+        if (S.prm.thermostat) e->any_thermostat = true;
+    }
+    TRY(alloc_cells(e, std::max(cell_off, 1)));
+    e->ncells_total = cell_off;
+    e->np_b = part_off;
+    std::vector<int> mort(std::max(cell_off, 1)), nbr((size_t)std::max(cell_off, 1) * e->nb, -1);
+    std::vector<int> csim, cstart, clen;
+    for (auto &S : e->sims) {
+        if (!S.active) continue;
+        for (int lin = 0; lin < S.ncells; ++lin) mort[S.cell_off + lin] = S.morton[lin];
+        for (int r = 0; r < S.ncells; ++r) {
+            int lin = S.rank_lin[r];
+            int c[3] = {lin % S.nc[0], (lin / S.nc[0]) % S.nc[1], lin / (S.nc[0] * S.nc[1])};
+            for (int t = 0; t < e->nb; ++t) {
+                int o[3] = {t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1};
+                bool ok = true;
+                int l2 = 0, mul = 1;
+                for (int a = 0; a < e->dim; ++a) {
+                    if (S.nc[a] < 3 && o[a] != 0) {
+                        ok = false;
+                        break;
+                    }
+                    int x = (c[a] + o[a] + S.nc[a]) % S.nc[a];
+                    l2 += x * mul;
+                    mul *= S.nc[a];
+                }
+                nbr[(size_t)(S.cell_off + r) * e->nb + t] = ok ? S.cell_off + S.morton[l2] : -1;
+            }
+        }
+        for (int64_t b = 0; b < S.n; b += 1024) {
+            csim.push_back((int)(&S - &e->sims[0]));
+            cstart.push_back(S.part_off + (int)b);
+            clen.push_back((int)std::min<int64_t>(1024, S.n - b));
+        }
+    }
+    e->nchunks = (int)csim.size();
+    if (e->nchunks > e->cap_chunks) {
+        cudaFree(e->chunk_sim);
+        cudaFree(e->chunk_start);
+        cudaFree(e->chunk_len);
+        cudaFree(e->tsum_part);
+        int64_t c = std::max<int64_t>(e->nchunks, 2 * e->cap_chunks);
+        TRY(dalloc(&e->chunk_sim, c));
+        TRY(dalloc(&e->chunk_start, c));
+        TRY(dalloc(&e->chunk_len, c));
+        TRY(dalloc(&e->tsum_part, c));
+        e->cap_chunks = c;
+    }
+    cudaStream_t st = e->stream;
+    if (cell_off > 0) {
+        CK(cudaMemcpyAsync(e->morton, mort.data(), sizeof(int) * cell_off, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(e->nbr, nbr.data(), sizeof(int) * (size_t)cell_off * e->nb,
+                           cudaMemcpyHostToDevice, st));
+    }
+    if (e->nchunks > 0) {
+        CK(cudaMemcpyAsync(e->chunk_sim, csim.data(), sizeof(int) * e->nchunks, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(e->chunk_start, cstart.data(), sizeof(int) * e->nchunks, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(e->chunk_len, clen.data(), sizeof(int) * e->nchunks, cudaMemcpyHostToDevice, st));
+    }
+    std::vector<SimDev> sd(e->cap_s);
+    for (int s = 0; s < e->cap_s; ++s) {
+        if (s < (int)e->sims.size()) sd[s] = make_simdev(e, e->sims[s]);
+        else memset(&sd[s], 0, sizeof(SimDev));
+    }
+    CK(cudaMemcpyAsync(e->sims_d, sd.data(), sizeof(SimDev) * e->cap_s, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    free_graph(e);
+    e->layout_dirty = false;
+    return SPH_OK;
+}
+
+// Counting sort of A into B plus the packed first-evaluation copies.
+void enqueue_prepare(sph_engine *e, cudaStream_t st) {
+    View v = make_view(e);
+    stage_view(e, v, 0);
+    v.pk_pos_out = e->pk_pos[0];
+    v.pk_vel_out = e->pk_vel[0];
+    cudaMemsetAsync(e->cell_count, 0, sizeof(int) * std::max(e->ncells_total, 1), st);
+    cudaMemsetAsync(e->pair_count, 0, sizeof(unsigned long long) * e->cap_s, st);
+    launch_bin(v, e->a_extent, st);
+    launch_scan(e->cell_count, e->cell_start, e->ncells_total, e->scan_tmp, st);
+    launch_scatter(v, e->a_extent, st);
+    launch_cellsort(v, e->ncells_total, st);
+    launch_permute(v, e->precision, st);
+}
+
+void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
+    View v = make_view(e);
+    stage_view(e, v, s);
+    int blk = e->tune.block_size;
+    launch_density(v, e->precision, e->group.kernel, s, blk, st);
+    if (e->group.heat_flux) launch_heat(v, e->precision, e->group.kernel, blk, st);
+    if (mode == 1 && s == e->nstage - 1 && e->any_thermostat)
+        launch_tsum(v, e->precision, (int)e->sims.size(), st);
+    launch_force(v, e->precision, e->group.kernel, e->group.viscosity, e->group.heat_flux,
+                 e->group.integrator, s, mode, blk, st);
+}
+
+void enqueue_step(sph_engine *e, cudaStream_t st) {
+    enqueue_prepare(e, st);
+    for (int s = 0; s < e->nstage; ++s) enqueue_stage(e, s, 1, st);
+}
+
+void after_advance(sph_engine *e, int steps) {
+    e->a_extent = e->np_b;
+    for (auto &S : e->sims)
+        if (S.active) {
+            S.a_off = S.part_off;
+            S.steps += steps;
+        }
+    e->props_valid = true;
+}
+
+int ensure_layout(sph_engine *e) {
+    if (e->layout_dirty) TRY(relayout(e));
+    return SPH_OK;
+}
+
+int check_sim(sph_engine *e, int32_t id) {
+    if (!e || id < 0 || id >= (int)e->sims.size() || !e->sims[id].active) return SPH_ENOTFOUND;
+    return SPH_OK;
+}
+
+// Copies n*k doubles from caller memory into the engine's staging buffer.
+int stage_in(sph_engine *e, const double *src, size_t count, int mem, double **out) {
+    if (mem == SPH_DEVICE) {
+        *out = const_cast<double *>(src);
+        return SPH_OK;
+    }
+    CK(cudaMemcpyAsync(e->stage_buf, src, sizeof(double) * count, cudaMemcpyHostToDevice, e->stream));
+    *out = e->stage_buf;
+    return SPH_OK;
+}
+
+int write_state_range(sph_engine *e, int off, int64_t n, const double *r, const double *v,
+                      const double *m, const double *u, int mem) {
+    cudaStream_t st = e->stream;
+    double *pos[3] = {e->a_pos[0] + off, e->a_pos[1] + off, e->a_pos[2] + off};
+    double *vel[3] = {e->a_vel[0] + off, e->a_vel[1] + off, e->a_vel[2] + off};
+    double *src;
+    if (r) {
+        TRY(stage_in(e, r, (size_t)n * e->dim, mem, &src));
+        launch_load_aos(pos, src, (int)n, e->dim, st);
+    }
+    if (v) {
+        if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));  // staging buffer reuse
+        TRY(stage_in(e, v, (size_t)n * e->dim, mem, &src));
+        launch_load_aos(vel, src, (int)n, e->dim, st);
+    }
+    cudaMemcpyKind k = mem == SPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (m) CK(cudaMemcpyAsync(e->a_m + off, m, sizeof(double) * n, k, st));
+    if (u) CK(cudaMemcpyAsync(e->a_u + off, u, sizeof(double) * n, k, st));
+    if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));
+    return SPH_OK;
+}
+
+int copy_out(sph_engine *e, double *dst, size_t count, int mem, double *dev_src) {
+    if (mem == SPH_DEVICE) return SPH_OK;  // written in place
+    CK(cudaMemcpyAsync(dst, dev_src, sizeof(double) * count, cudaMemcpyDeviceToHost, e->stream));
+    return SPH_OK;
+}
+
+// Gathers an R array (B order) of simulation s into caller order.
+int gather_R(sph_engine *e, const Sim &S, void *src, double *dst, int mem) {
+    if (!dst) return SPH_OK;
+    double *d = mem == SPH_DEVICE ? dst : e->stage_buf;
+    launch_store_R(d, src, e->precision, e->b_id, S.part_off, (int)S.n, e->stream);
+    TRY(copy_out(e, dst, (size_t)S.n, mem, d));
+    if (mem == SPH_HOST) CK(cudaStreamSynchronize(e->stream));
+    return SPH_OK;
+}
+
+int gather_R_vec(sph_engine *e, const Sim &S, void *const src[3], double *dst, int mem) {
+    if (!dst) return SPH_OK;
+    double *d = mem == SPH_DEVICE ? dst : e->stage_buf;
+    // component-wise into AoS: store each component with stride dim via temp
+    for (int a = 0; a < e->dim; ++a) {
+        double *tmp = e->stage_buf + (size_t)e->cap_p * 2;  // scratch third
+        launch_store_R(tmp, src[a], e->precision, e->b_id, S.part_off, (int)S.n, e->stream);
+        CK(cudaMemcpy2DAsync(d + a, sizeof(double) * e->dim, tmp, sizeof(double), sizeof(double),
+                             (size_t)S.n, cudaMemcpyDeviceToDevice, e->stream));
+    }
+    TRY(copy_out(e, dst, (size_t)S.n * e->dim, mem, d));
+    if (mem == SPH_HOST) CK(cudaStreamSynchronize(e->stream));
+    return SPH_OK;
+}
+
+int alloc_particles(sph_engine *e) {
+    int64_t P = e->cap_p;
+    for (int a = 0; a < 3; ++a) {
+        TRY(dalloc(&e->a_pos[a], P));
+        TRY(dalloc(&e->a_vel[a], P));
+        TRY(dalloc(&e->b_pos[a], P));
+        TRY(dalloc(&e->b_vel[a], P));
+        TRY(dalloc(&e->xe[0][a], P));
+        TRY(dalloc(&e->xe[1][a], P));
+        TRY(dalloc(&e->ve[a], P));
+        TRY(dalloc((char **)&e->q[a], P * e->rsize));
+        TRY(dalloc((char **)&e->vdot[a], P * e->rsize));
+        TRY(dalloc((char **)&e->f0v[a], P * e->rsize));
+        if (e->group.integrator == SPH_RK4) {
+            TRY(dalloc(&e->acc_r[a], P));
+            TRY(dalloc(&e->acc_v[a], P));
+        }
+    }
+    TRY(dalloc(&e->a_u, P));
+    TRY(dalloc(&e->a_m, P));
+    TRY(dalloc(&e->a_id, P));
+    TRY(dalloc(&e->a_sim, P));
+    TRY(dalloc(&e->b_u, P));
+    TRY(dalloc(&e->b_m, P));
+    TRY(dalloc(&e->b_id, P));
+    TRY(dalloc(&e->b_sim, P));
+    TRY(dalloc(&e->cell_of, P));
+    TRY(dalloc(&e->rank, P));
+    TRY(dalloc(&e->order_tmp, P));
+    TRY(dalloc(&e->order, P));
+    TRY(dalloc(&e->cell_b, P));
+    TRY(dalloc(&e->ue, P));
+    for (int b = 0; b < 2; ++b) {
+        TRY(dalloc((char **)&e->pk_pos[b], P * e->v4size));
+        TRY(dalloc((char **)&e->pk_vel[b], P * e->v4size));
+    }
+    TRY(dalloc((char **)&e->pk_f, P * e->v4size));
+    TRY(dalloc((char **)&e->pk_q, P * e->v4size));
+    void **rs[] = {&e->rho, &e->rho_l, &e->temp, &e->pres, &e->pco, &e->rho0, &e->pres0,
+                   &e->pco0, &e->udot, &e->f0u};
+    for (void **p : rs) TRY(dalloc((char **)p, P * e->rsize));
+    if (e->group.integrator == SPH_RK4) TRY(dalloc(&e->acc_u, P));
+    TRY(dalloc(&e->stage_buf, P * 3));
+    // pk_q must read as zero when heat flux is off
+    CK(cudaMemset(e->pk_q, 0, P * e->v4size));
+    CK(cudaMemset(e->a_sim, 0xff, P * sizeof(int)));
+    return SPH_OK;
+}
+
+int alloc_sims(sph_engine *e) {
+    int S = e->cap_s;
+    TRY(dalloc(&e->sims_d, S));
+    TRY(dalloc(&e->t_scale, S));
+    TRY(dalloc(&e->steps_d, S));
+    TRY(dalloc(&e->pair_count, S));
+    TRY(dalloc(&e->err, S));
+    TRY(dalloc(&e->err_any, 1));
+    CK(cudaMemset(e->err, 0, sizeof(int) * S));
+    CK(cudaMemset(e->err_any, 0, sizeof(int)));
+    CK(cudaMemset(e->steps_d, 0, sizeof(long long) * S));
+    CK(cudaMemset(e->pair_count, 0, sizeof(unsigned long long) * S));
+    std::vector<double> one(S, 1.0);
+    CK(cudaMemcpy(e->t_scale, one.data(), sizeof(double) * S, cudaMemcpyHostToDevice));
+    return SPH_OK;
+}
+
+void free_all(sph_engine *e) {
+    free_graph(e);
+    void *ptrs[] = {e->a_u, e->a_m, e->a_id, e->a_sim, e->b_u, e->b_m, e->b_id, e->b_sim,
+                    e->cell_of, e->rank, e->order_tmp, e->order, e->cell_b, e->cell_count,
+                    e->cell_start, e->nbr, e->morton, e->scan_tmp, e->pk_pos[0], e->pk_pos[1],
+                    e->pk_vel[0], e->pk_vel[1], e->pk_f, e->pk_q, e->ue, e->rho, e->rho_l,
+                    e->temp, e->pres, e->pco, e->rho0, e->pres0, e->pco0, e->udot, e->f0u,
+                    e->acc_u, e->stage_buf, e->sims_d, e->t_scale, e->tsum_part, e->steps_d,
+                    e->pair_count, e->err, e->err_any, e->chunk_sim, e->chunk_start,
+                    e->chunk_len};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (int a = 0; a < 3; ++a) {
+        void *pa[] = {e->a_pos[a], e->a_vel[a], e->b_pos[a], e->b_vel[a], e->xe[0][a],
+                      e->xe[1][a], e->ve[a], e->q[a], e->vdot[a], e->f0v[a], e->acc_r[a],
+                      e->acc_v[a]};
+        for (void *p : pa)
+            if (p) cudaFree(p);
+    }
+}
+
+// Moves every live particle to the front of A in the current sorted layout.
+int compact(sph_engine *e) {
+    TRY(ensure_layout(e));
+    cudaStream_t st = e->stream;
+    enqueue_prepare(e, st);
+    size_t n = (size_t)e->np_b;
+    for (int a = 0; a < e->dim; ++a) {
+        CK(cudaMemcpyAsync(e->a_pos[a], e->b_pos[a], n * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(e->a_vel[a], e->b_vel[a], n * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    CK(cudaMemcpyAsync(e->a_u, e->b_u, n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(e->a_m, e->b_m, n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(e->a_id, e->b_id, n * 4, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(e->a_sim, e->b_sim, n * 4, cudaMemcpyDeviceToDevice, st));
+    if ((int64_t)n < e->cap_p)
+        CK(cudaMemsetAsync(e->a_sim + n, 0xff, (e->cap_p - n) * sizeof(int), st));
+    CK(cudaStreamSynchronize(st));
+    e->a_extent = (int)n;
+    for (auto &S : e->sims)
+        if (S.active) S.a_off = S.part_off;
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *sph_status_string(int status) {
+    switch (status) {
+        case SPH_OK: return "SPH_OK";
+        case SPH_EINVAL: return "SPH_EINVAL: invalid argument";
+        case SPH_ENOMEM: return "SPH_ENOMEM: device allocation failed";
+        case SPH_ECELL_OVERFLOW: return "SPH_ECELL_OVERFLOW: cell occupancy too large";
+        case SPH_ETIMEOUT: return "SPH_ETIMEOUT: bounded device wait gave up";
+        case SPH_ENAN: return "SPH_ENAN: non-finite density, pressure or rate";
+        case SPH_ECUDA: return "SPH_ECUDA: CUDA runtime error";
+        case SPH_ESKIN: return "SPH_ESKIN: displacement within a step exceeded the cell slack";
+        case SPH_ECAPACITY: return "SPH_ECAPACITY: engine capacity exceeded";
+        case SPH_ENOTFOUND: return "SPH_ENOTFOUND: unknown simulation id";
+        default: return "unknown status";
+    }
+}
+
+int sph_version(void) { return 10000; }
+
+int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precision,
+                      int64_t max_particles, int32_t max_sims, void *stream) {
+    if (!out || !group) return SPH_EINVAL;
+    *out = nullptr;
+    if (group->dim != 2 && group->dim != 3) return SPH_EINVAL;
+    if (group->kernel < 1 || group->kernel > 4) return SPH_EINVAL;
+    if (group->integrator < 0 || group->integrator > 2) return SPH_EINVAL;
+    if (precision != SPH_FP64 && precision != SPH_MIXED) return SPH_EINVAL;
+    if (max_particles <= 0 || max_particles > (int64_t)0x7fffffff / 2 || max_sims <= 0)
+        return SPH_EINVAL;
+    sph_engine *e = new sph_engine();
+    e->group = *group;
+    e->precision = precision;
+    e->dim = group->dim;
+    e->nb = group->dim == 2 ? 9 : 27;
+    e->nstage = nstage_of(group->integrator);
+    e->rsize = precision == SPH_MIXED ? 4 : 8;
+    e->v4size = precision == SPH_MIXED ? 16 : 32;
+    e->cap_p = max_particles;
+    e->cap_s = max_sims;
+    e->tune.block_size = 128;
+    e->tune.cells_per_warp = 0;
+    e->tune.cell_ratio = 1.0;
+    e->tune.use_graph = 1;
+    e->tune.steps_per_graph = 1;
+    if (stream) {
+        e->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete e;
+            return SPH_ECUDA;
+        }
+        e->own_stream = true;
+    }
+    int st = alloc_particles(e);
+    if (st == SPH_OK) st = alloc_sims(e);
+    if (st == SPH_OK) st = alloc_cells(e, 1024);
+    if (st != SPH_OK) {
+        free_all(e);
+        if (e->own_stream) cudaStreamDestroy(e->stream);
+        delete e;
+        return st;
+    }
+    *out = e;
+    return SPH_OK;
+}
+
+int sph_engine_destroy(sph_engine *e) {
+    if (!e) return SPH_EINVAL;
+    cudaStreamSynchronize(e->stream);
+    free_all(e);
+    if (e->own_stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return SPH_OK;
+}
+
+int sph_sim_add(sph_engine *e, const sph_params *p, int64_t n, const double *r, const double *v,
+                const double *m, const double *u, int32_t mem, int32_t *sim_id) {
+    if (!e || !p || !r || !v || !m || !u || !sim_id || n <= 0) return SPH_EINVAL;
+    TRY(validate_params(e, p));
+    // simulation slot
+    int id = -1;
+    for (int s = 0; s < (int)e->sims.size(); ++s)
+        if (!e->sims[s].active) {
+            id = s;
+            break;
+        }
+    if (id < 0) {
+        if ((int)e->sims.size() >= e->cap_s) return SPH_ECAPACITY;
+        id = (int)e->sims.size();
+        e->sims.emplace_back();
+    }
+    int64_t live = 0;
+    for (auto &S : e->sims)
+        if (S.active) live += S.n;
+    if (live + n > e->cap_p) return SPH_ECAPACITY;
+    if (e->a_extent + n > e->cap_p) TRY(compact(e));
+    // velocity bound for the cell slack and a host-side position check
+    std::vector<double> hv((size_t)n * p->dim), hr((size_t)n * p->dim);
+    cudaMemcpyKind k = mem == SPH_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    CK(cudaMemcpy(hv.data(), v, sizeof(double) * hv.size(), k));
+    CK(cudaMemcpy(hr.data(), r, sizeof(double) * hr.size(), k));
+    double vmax = 0.0;
+    for (double x : hv) vmax = std::max(vmax, std::fabs(x));
+    for (int64_t i = 0; i < n; ++i)
+        for (int a = 0; a < p->dim; ++a) {
+            double x = hr[(size_t)i * p->dim + a];
+            // within a quarter box of [0, L]: the reference's single minimum-image
+            // shift then equals the true minimum image for every pair
+            if (!(x >= -0.25 * p->box[a] && x <= 1.25 * p->box[a])) return SPH_EINVAL;
+        }
+    Sim &S = e->sims[id];
+    S = Sim();
+    S.prm = *p;
+    S.n = n;
+    S.vmax = vmax;
+    make_grid(S, e->dim, e->tune.cell_ratio);
+    int off = e->a_extent;
+    TRY(write_state_range(e, off, n, r, v, m, u, mem));
+    launch_iota_sim(e->a_id + off, e->a_sim + off, id, (int)n, e->stream);
+    CK(cudaMemsetAsync(e->err + id, 0, sizeof(int), e->stream));
+    CK(cudaMemsetAsync(e->steps_d + id, 0, sizeof(long long), e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    S.active = true;
+    S.a_off = off;
+    e->a_extent += (int)n;
+    e->layout_dirty = true;
+    e->props_valid = false;
+    *sim_id = id;
+    return SPH_OK;
+}
+
+int sph_sim_remove(sph_engine *e, int32_t id) {
+    TRY(check_sim(e, id));
+    Sim &S = e->sims[id];
+    launch_fill_int(e->a_sim + S.a_off, -1, (int)S.n, e->stream);
+    CK(cudaStreamSynchronize(e->stream));
+    S.active = false;
+    e->layout_dirty = true;
+    e->props_valid = false;
+    return SPH_OK;
+}
+
+int sph_sim_set_state(sph_engine *e, int32_t id, const double *r, const double *v,
+                      const double *m, const double *u, int32_t mem) {
+    TRY(check_sim(e, id));
+    Sim &S = e->sims[id];
+    // A holds the simulation in slot order a_off + k with id[k]; the caller
+    // gives original order, so reset ids to identity for the range.
+    TRY(write_state_range(e, S.a_off, S.n, r, v, m, u, mem));
+    if (r && v && m && u) launch_iota_sim(e->a_id + S.a_off, e->a_sim + S.a_off, id, (int)S.n, e->stream);
+    else if (r || v || m || u) {
+        // partial updates need the identity order first
+        return SPH_EINVAL;
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    e->props_valid = false;
+    return SPH_OK;
+}
+
+int sph_sim_get_state(sph_engine *e, int32_t id, double *r, double *v, double *u, int32_t mem) {
+    TRY(check_sim(e, id));
+    Sim &S = e->sims[id];
+    cudaStream_t st = e->stream;
+    int n = (int)S.n;
+    if (r) {
+        double *d = mem == SPH_DEVICE ? r : e->stage_buf;
+        launch_store_aos(d, e->a_pos, e->a_id, S.a_off, n, e->dim, st);
+        TRY(copy_out(e, r, (size_t)n * e->dim, mem, d));
+        if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));
+    }
+    if (v) {
+        double *d = mem == SPH_DEVICE ? v : e->stage_buf;
+        launch_store_aos(d, e->a_vel, e->a_id, S.a_off, n, e->dim, st);
+        TRY(copy_out(e, v, (size_t)n * e->dim, mem, d));
+        if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));
+    }
+    if (u) {
+        double *d = mem == SPH_DEVICE ? u : e->stage_buf;
+        launch_store_scalar(d, e->a_u, e->a_id, S.a_off, n, st);
+        TRY(copy_out(e, u, (size_t)n, mem, d));
+        if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));
+    }
+    CK(cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_sim_count(sph_engine *e, int32_t id, int64_t *n) {
+    TRY(check_sim(e, id));
+    *n = e->sims[id].n;
+    return SPH_OK;
+}
+
+int sph_advance(sph_engine *e, int32_t nsteps) {
+    if (!e || nsteps < 0) return SPH_EINVAL;
+    if (nsteps == 0) return SPH_OK;
+    TRY(ensure_layout(e));
+    if (e->np_b == 0) return SPH_OK;
+    cudaStream_t st = e->stream;
+    int per = std::max(1, e->tune.steps_per_graph);
+    int done = 0;
+    // The binning pass covers A's used extent.  After simulations joined or
+    // left, A holds dropped or unsorted particles beyond the live count;
+    // that first step runs eagerly, after which A is compact (extent == live).
+    if (e->a_extent != e->np_b) {
+        enqueue_step(e, st);
+        after_advance(e, 1);
+        ++done;
+    }
+    if (e->tune.use_graph && nsteps - done >= per) {
+        if (!e->graph_exec || e->graph_steps != per) {
+            free_graph(e);
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < per; ++k) enqueue_step(e, st);
+            CK(cudaStreamEndCapture(st, &e->graph));
+            CK(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
+            e->graph_steps = per;
+        }
+        while (nsteps - done >= per) {
+            CK(cudaGraphLaunch(e->graph_exec, st));
+            after_advance(e, per);
+            done += per;
+        }
+    }
+    while (done < nsteps) {
+        enqueue_step(e, st);
+        after_advance(e, 1);
+        ++done;
+    }
+    CK(cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_sim_derivatives(sph_engine *e, int32_t id, double *rho, double *rho_lr, double *t,
+                        double *p, double *pco, double *vdot, double *udot, double *jq,
+                        int32_t mem) {
+    TRY(check_sim(e, id));
+    TRY(ensure_layout(e));
+    cudaStream_t st = e->stream;
+    enqueue_prepare(e, st);
+    enqueue_stage(e, 0, 0, st);
+    CK(cudaGetLastError());
+    e->props_valid = true;
+    const Sim &S = e->sims[id];
+    TRY(gather_R(e, S, e->rho, rho, mem));
+    TRY(gather_R(e, S, e->rho_l, rho_lr, mem));
+    TRY(gather_R(e, S, e->temp, t, mem));
+    TRY(gather_R(e, S, e->pres, p, mem));
+    TRY(gather_R(e, S, e->pco, pco, mem));
+    TRY(gather_R(e, S, e->udot, udot, mem));
+    TRY(gather_R_vec(e, S, e->vdot, vdot, mem));
+    if (jq) {
+        if (e->group.heat_flux) TRY(gather_R_vec(e, S, e->q, jq, mem));
+        else if (mem == SPH_DEVICE) CK(cudaMemsetAsync(jq, 0, sizeof(double) * S.n * e->dim, st));
+        else memset(jq, 0, sizeof(double) * S.n * e->dim);
+    }
+    CK(cudaStreamSynchronize(st));
+    return SPH_OK;
+}
+
+int sph_sim_get_properties(sph_engine *e, int32_t id, double *rho, double *rho_lr, double *t,
+                           double *p, double *pco, double *vdot, double *udot, double *jq,
+                           int32_t mem) {
+    TRY(check_sim(e, id));
+    if (!e->props_valid || e->layout_dirty) return sph_sim_derivatives(e, id, rho, rho_lr, t, p, pco, vdot, udot, jq, mem);
+    const Sim &S = e->sims[id];
+    TRY(gather_R(e, S, e->rho0, rho, mem));
+    TRY(gather_R(e, S, e->rho_l, rho_lr, mem));
+    TRY(gather_R(e, S, e->temp, t, mem));
+    TRY(gather_R(e, S, e->pres0, p, mem));
+    TRY(gather_R(e, S, e->pco0, pco, mem));
+    TRY(gather_R(e, S, e->udot, udot, mem));
+    TRY(gather_R_vec(e, S, e->vdot, vdot, mem));
+    if (jq) {
+        if (e->group.heat_flux) TRY(gather_R_vec(e, S, e->q, jq, mem));
+        else if (mem == SPH_DEVICE) CK(cudaMemsetAsync(jq, 0, sizeof(double) * S.n * e->dim, e->stream));
+        else memset(jq, 0, sizeof(double) * S.n * e->dim);
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    return SPH_OK;
+}
+
+int sph_sim_pair_count(sph_engine *e, int32_t id, int64_t *nip) {
+    TRY(check_sim(e, id));
+    TRY(ensure_layout(e));
+    cudaStream_t st = e->stream;
+    enqueue_prepare(e, st);
+    View v = make_view(e);
+    stage_view(e, v, 0);
+    launch_density(v, e->precision, e->group.kernel, 0, e->tune.block_size, st);
+    unsigned long long c = 0;
+    CK(cudaMemcpyAsync(&c, e->pair_count + id, sizeof(c), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *nip = (int64_t)(c / 2);
+    return SPH_OK;
+}
+
+int sph_sim_export_pairs(sph_engine *e, int32_t id, int64_t cap, int64_t *iap, double *drij,
+                         double *rsq, double *dv, int64_t *nip, int32_t mem) {
+    TRY(check_sim(e, id));
+    if (!nip) return SPH_EINVAL;
+    TRY(ensure_layout(e));
+    cudaStream_t st = e->stream;
+    enqueue_prepare(e, st);
+    const Sim &S = e->sims[id];
+    View v = make_view(e);
+    stage_view(e, v, 0);
+    long long *rows = nullptr;
+    TRY(dalloc(&rows, (size_t)S.n + 1));
+    CK(cudaMemsetAsync(rows, 0, sizeof(long long) * (S.n + 1), st));
+    launch_pair_rows(v, e->precision, S.part_off, (int)S.n, rows, st);
+    launch_scan64(rows, (int)S.n, st);
+    long long total = 0;
+    CK(cudaMemcpyAsync(&total, rows + S.n, sizeof(total), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *nip = total;
+    if (total > cap) {
+        cudaFree(rows);
+        return SPH_ECAPACITY;
+    }
+    if (total > 0 && (iap || drij || rsq || dv)) {
+        long long *d_iap = nullptr;
+        double *d_drij = nullptr, *d_rsq = nullptr, *d_dv = nullptr;
+        bool host = mem == SPH_HOST;
+        int st1 = SPH_OK;
+        if (host || !iap) st1 = dalloc(&d_iap, (size_t)total * 2);
+        else d_iap = (long long *)iap;
+        if (st1 == SPH_OK && drij) {
+            if (host) st1 = dalloc(&d_drij, (size_t)total * e->dim);
+            else d_drij = drij;
+        }
+        if (st1 == SPH_OK && rsq) {
+            if (host) st1 = dalloc(&d_rsq, (size_t)total);
+            else d_rsq = rsq;
+        }
+        if (st1 == SPH_OK && dv) {
+            if (host) st1 = dalloc(&d_dv, (size_t)total * e->dim);
+            else d_dv = dv;
+        }
+        if (st1 == SPH_OK) {
+            launch_pair_write(v, e->precision, S.part_off, (int)S.n, rows, d_iap, d_drij, d_rsq,
+                              d_dv, st);
+            if (host) {
+                if (iap) cudaMemcpyAsync(iap, d_iap, sizeof(long long) * total * 2, cudaMemcpyDeviceToHost, st);
+                if (drij) cudaMemcpyAsync(drij, d_drij, sizeof(double) * total * e->dim, cudaMemcpyDeviceToHost, st);
+                if (rsq) cudaMemcpyAsync(rsq, d_rsq, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
+                if (dv) cudaMemcpyAsync(dv, d_dv, sizeof(double) * total * e->dim, cudaMemcpyDeviceToHost, st);
+            }
+            cudaStreamSynchronize(st);
+        }
+        if (host || !iap) cudaFree(d_iap);
+        if (host) {
+            cudaFree(d_drij);
+            cudaFree(d_rsq);
+            cudaFree(d_dv);
+        }
+        if (st1 != SPH_OK) {
+            cudaFree(rows);
+            return st1;
+        }
+    }
+    cudaFree(rows);
+    CK(cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_last_pair_total(sph_engine *e, int64_t *pairs) {
+    if (!e || !pairs) return SPH_EINVAL;
+    std::vector<unsigned long long> c(e->cap_s);
+    CK(cudaMemcpyAsync(c.data(), e->pair_count, sizeof(unsigned long long) * e->cap_s,
+                       cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    unsigned long long t = 0;
+    for (int s = 0; s < (int)e->sims.size(); ++s)
+        if (e->sims[s].active) t += c[s];
+    *pairs = (int64_t)(t / 2);
+    return SPH_OK;
+}
+
+int sph_sim_diagnostics(sph_engine *e, int32_t id, double out[6]) {
+    TRY(check_sim(e, id));
+    const Sim &S = e->sims[id];
+    size_t n = (size_t)S.n, d = (size_t)e->dim;
+    std::vector<double> v(n * d), u(n), m(n), t(n, 0.0);
+    TRY(sph_sim_get_state(e, id, nullptr, v.data(), u.data(), SPH_HOST));
+    CK(cudaMemcpy(m.data(), e->a_m + S.a_off, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    double ke = 0, ue = 0, mom[3] = {0, 0, 0}, tav = 0;
+    for (size_t i = 0; i < n; ++i) {
+        double v2 = 0;
+        for (size_t a = 0; a < d; ++a) {
+            v2 += v[i * d + a] * v[i * d + a];
+            mom[a] += m[i] * v[i * d + a];
+        }
+        ke += 0.5 * m[i] * v2;
+        ue += u[i];
+    }
+    if (e->props_valid && !e->layout_dirty) {
+        TRY(gather_R(e, S, e->temp, t.data(), SPH_HOST));
+        for (double x : t) tav += x;
+        tav /= (double)n;
+    }
+    out[0] = ke;
+    out[1] = ue;
+    out[2] = mom[0];
+    out[3] = mom[1];
+    out[4] = mom[2];
+    out[5] = tav;
+    return SPH_OK;
+}
+
+int sph_get_tuning(sph_engine *e, sph_tuning *t) {
+    if (!e || !t) return SPH_EINVAL;
+    *t = e->tune;
+    return SPH_OK;
+}
+
+int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
+    if (!e || !t) return SPH_EINVAL;
+    if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) || !(t->cell_ratio >= 1.0))
+        return SPH_EINVAL;
+    bool regrid = t->cell_ratio != e->tune.cell_ratio;
+    e->tune = *t;
+    free_graph(e);
+    if (regrid) {
+        for (auto &S : e->sims)
+            if (S.active) make_grid(S, e->dim, e->tune.cell_ratio);
+        e->layout_dirty = true;
+        e->props_valid = false;
+    }
+    return SPH_OK;
+}
+
+int sph_sync(sph_engine *e) {
+    if (!e) return SPH_EINVAL;
+    CK(cudaStreamSynchronize(e->stream));
+    CK(cudaGetLastError());
+    int code = 0;
+    CK(cudaMemcpy(&code, e->err_any, sizeof(int), cudaMemcpyDeviceToHost));
+    if (code) CK(cudaMemset(e->err_any, 0, sizeof(int)));
+    return code;
+}
+
+int sph_sim_status(sph_engine *e, int32_t id, int32_t *status) {
+    TRY(check_sim(e, id));
+    if (!status) return SPH_EINVAL;
+    CK(cudaStreamSynchronize(e->stream));
+    CK(cudaMemcpy(status, e->err + id, sizeof(int), cudaMemcpyDeviceToHost));
+    return SPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// sph_internal.h -- device data layout shared by the engine and its kernels.
+//
+// HBM layout (all arrays flattened over the engine's simulations):
+//  * state A  (canonical, cell-sorted as of the last step):  pos[3][P], vel[3][P],
+//    u[P], m[P] in FP64 SoA, plus id[P] (original index within its simulation)
+//    and sim[P].  New simulations are appended unsorted at the tail.
+//  * state B  (this step's start state x0 after the counting sort): same fields.
+//  * evaluation arrays (B order): packed cell-local positions / velocities
+//    (float4 in mixed mode, double4 in FP64 mode), FP64 raw evaluation
+//    positions xe (exact pair test), ue, ve; densities, EOS outputs, packed
+//    force factors, heat flux, rates and integrator accumulators.
+//  * cell table: per simulation a Morton-ordered cell range; cell_start[C+1]
+//    and a neighbour table nbr[C][3^dim] of global cell ids (-1: none).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sph.h"
+
+namespace sph {
+
+constexpr int kMaxNbr = 27;
+
+// Per-simulation constants on the device.
+struct SimDev {
+    double L[3], half_L[3];
+    double edge[3], inv_edge[3];
+    double slack_half[3];   // max displacement per axis between binning and an evaluation
+    int nc[3];
+    int small_mask;         // bit a set: axis a has one cell (minimum image in the pair pass)
+    int active;
+    int cell_off, ncells;
+    int part_off, n;        // range in B (sorted) order
+    int nbr_count;          // 3^dim, neighbour slots per cell
+    int thermostat;
+    double thr;             // cutoff^2 + tolerance^2 (FP64, the reference's value)
+    double hs, hl;          // smoothing lengths
+    double sig_s, sig_l;    // kernel normalisations
+    double ws0, wl0;        // self terms W(0, h)
+    double a, b, kb;        // van der Waals
+    double alpha, beta, eps, c;   // Monaghan viscosity
+    double kappa;           // conductivity
+    double dt;
+    double T0, T1;          // thermostat ramp ends
+    long long ramp;
+};
+
+// Pointers of the engine buffers (device addresses), passed by value.
+struct View {
+    int np;                 // particles in B (sorted, active)
+    int dim;
+    SimDev *sims;
+    // state A
+    double *a_pos[3], *a_vel[3], *a_u, *a_m;
+    int *a_id, *a_sim;
+    // state B
+    double *b_pos[3], *b_vel[3], *b_u, *b_m;
+    int *b_id, *b_sim;
+    // sort scratch
+    int *cell_of;           // A order: global cell, -1 dropped
+    int *rank;              // A order: arrival rank within cell
+    int *order_tmp, *order; // B slot -> A index
+    int *cell_count, *cell_start, *cell_b;  // cell_b: B order cell id
+    int *nbr, *morton;
+    // evaluation (stage s reads *_in, its force pass writes stage s+1's *_out)
+    void *pk_pos_in, *pk_vel_in;     // float4 / double4: {xl, yl, zl, m}, {vx, vy, vz, 0}
+    void *pk_pos_out, *pk_vel_out;
+    void *pk_f, *pk_q;               // {p/rho^2, pco/rho_l^2, rho, T}, {q/rho^2, 0}
+    double *xe_in[3], *xe_out[3];    // FP64 raw evaluation positions (exact pair test)
+    double *ve_in[3], *ve_out[3];    // FP64 evaluation velocities (rdot)
+    double *ue_in, *ue_out;          // FP64 evaluation internal energy
+    void *rho, *rho_l, *temp, *pres, *pco;  // R arrays of the current evaluation
+    void *rho0, *pres0, *pco0;              // first evaluation of the step
+    void *q[3];                             // heat flux vector (jq)
+    void *vdot[3], *udot;                   // rates of the current evaluation
+    void *f0v[3], *f0u;                     // stage-0 rates (improved Euler)
+    double *acc_r[3], *acc_v[3], *acc_u;    // RK4 accumulators
+    // reductions
+    double *tsum_part;      // per chunk
+    int *chunk_sim, *chunk_start, *chunk_len;
+    int nchunks;
+    double *t_scale;        // per sim thermostat factor
+    long long *steps;       // per sim steps done
+    unsigned long long *pair_count;  // per sim (pairs x2 counted by gather)
+    int *err;               // per sim error word
+    int *err_any;
+};
+
+// ---- launch wrappers (sph_sort.cu) ----
+void launch_bin(const View &v, int np_a, cudaStream_t s);
+void launch_scan(int *count, int *start, int n, int *block_tmp, cudaStream_t s);
+void launch_scatter(const View &v, int np_a, cudaStream_t s);
+void launch_cellsort(const View &v, int ncells, cudaStream_t s);
+void launch_permute(const View &v, int precision, cudaStream_t s);
+void launch_load_aos(double *dst[3], const double *src, int n, int dim, cudaStream_t s);
+void launch_store_aos(double *dst, double *const src[3], const int *id, int off, int n, int dim,
+                      cudaStream_t s);
+void launch_store_scalar(double *dst, const double *src, const int *id, int off, int n,
+                         cudaStream_t s);
+void launch_store_R(double *dst, const void *src, int precision, const int *id, int off, int n,
+                    cudaStream_t s);
+void launch_fill_int(int *dst, int val, int n, cudaStream_t s);
+void launch_iota_sim(int *id, int *sim, int sim_id, int n, cudaStream_t s);
+
+// ---- launch wrappers (sph_pairs.cu) ----
+// stage: evaluation index within the step; nstage: evaluations per step;
+// mode: 0 derivative only, 1 advance.
+void launch_density(const View &v, int precision, int kernel, int stage, int block,
+                    cudaStream_t s);
+void launch_heat(const View &v, int precision, int kernel, int block, cudaStream_t s);
+void launch_force(const View &v, int precision, int kernel, int viscosity, int heat,
+                  int integrator, int stage, int mode, int block, cudaStream_t s);
+void launch_tsum(const View &v, int precision, int nsims, cudaStream_t s);
+void launch_pair_rows(const View &v, int precision, int sim_off, int n, long long *row_count,
+                      cudaStream_t s);
+void launch_pair_write(const View &v, int precision, int sim_off, int n,
+                       const long long *row_start, long long *iap, double *drij, double *rsq,
+                       double *dv, cudaStream_t s);
+void launch_scan64(long long *data, int n, cudaStream_t s);
+
+}  // namespace sph

@@ -1,0 +1,591 @@
+// sph_pairs.cu -- the pair passes of one derivative evaluation and the
+// fused integrator epilogue.
+//
+//   k_density : rho_s, rho_l summation (self term W(0,h), no m_i:
+//               properties.py:77-91), fused EOS epilogue (T from u, clamp,
+//               p, pco: properties.py:38-49, spam_complete_force.py:134-152)
+//   k_heat    : Fourier heat flux q_i (f_properties.py:129-130 restated)
+//   k_force   : pressure + cohesive accelerations, Monaghan viscosity, energy
+//               rate incl. conduction (forces.py:338-405, c_forces.pyx:96-111,
+//               163-178, 224-237) fused with the integrator stage update
+//               (integrator.py:14-103), periodic teleport (box.py:33-47) and the
+//               thermostat (particles.py:450-457).
+//
+// Every pass is a gather: thread i sums over all neighbours j in the 3^dim
+// cells around its own cell, so each unordered pair is evaluated from both
+// sides and no atomics touch particle data.  Positions are cell-local
+// (relative to the particle's cell centre), which keeps FP32 differences
+// accurate; the pair-set test runs on those FP32 distances with a 2^-12
+// guard band and falls back to the reference's FP64 test for pairs inside
+// the band, so the pair set is bit-exact.
+#include "sph_device.cuh"
+
+namespace sph {
+
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+
+template <typename R, int D>
+struct PairFrame {
+    R thr_lo, thr_hi;
+    R edge[3], L[3], hL[3];
+    int small_mask;
+    __device__ __forceinline__ void init(const SimDev &S) {
+        thr_lo = (R)(S.thr * (1.0 - Margin<R>::rel));
+        thr_hi = (R)(S.thr * (1.0 + Margin<R>::rel));
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            edge[a] = (R)S.edge[a];
+            L[a] = (R)S.L[a];
+            hL[a] = (R)S.half_L[a];
+        }
+        small_mask = S.small_mask;
+    }
+    // neighbour-cell displacement for neighbour slot t (t = ox+1 + 3(oy+1) + 9(oz+1))
+    __device__ __forceinline__ void shift(int t, R *sh) const {
+        sh[0] = (R)((t % 3) - 1) * edge[0];
+        sh[1] = (R)(((t / 3) % 3) - 1) * edge[1];
+        sh[2] = (D == 3) ? (R)((t / 9) - 1) * edge[2] : (R)0;
+    }
+    __device__ __forceinline__ void min_image(R *d) const {
+        if (small_mask) {
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+                if (small_mask & (1 << a)) {
+                    if (d[a] > hL[a]) d[a] -= L[a];
+                    if (d[a] < -hL[a]) d[a] += L[a];
+                }
+        }
+    }
+};
+
+template <int D> struct NbrCount { static constexpr int value = D == 2 ? 9 : 27; };
+
+// Iterates the pair set of particle i.  body(j, d[3], rsq) is called for
+// every j != i with the exact pair test passed.
+template <typename R, int D, typename T4, typename F>
+__device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
+                                          const PairFrame<R, D> &fr, const T4 *__restrict__ P,
+                                          int i, const T4 &pi, F body) {
+    constexpr int NB = NbrCount<D>::value;
+    const int *nb = v.nbr + (size_t)v.cell_b[i] * NB;
+    for (int t = 0; t < NB; ++t) {
+        int cj = nb[t];
+        if (cj < 0) continue;
+        R sh[3];
+        fr.shift(t, sh);
+        R ox = sh[0] - pi.x, oy = sh[1] - pi.y, oz = sh[2] - pi.z;
+        int jb = v.cell_start[cj], je = v.cell_start[cj + 1];
+        for (int j = jb; j < je; ++j) {
+            if (j == i) continue;
+            T4 pj = P[j];
+            R d[3];
+            d[0] = pj.x + ox;
+            d[1] = pj.y + oy;
+            d[2] = (D == 3) ? pj.z + oz : (R)0;
+            fr.min_image(d);
+            R rsq = d[0] * d[0] + d[1] * d[1];
+            if (D == 3) rsq += d[2] * d[2];
+            if (rsq > fr.thr_hi) continue;
+            if (rsq >= fr.thr_lo && !(exact_rsq<D>(v.xe_in, S, i, j) < S.thr)) continue;
+            body(j, pj, d, rsq);
+        }
+    }
+}
+
+// Warp-aggregated per-simulation counter update.
+__device__ __forceinline__ void add_pair_count(unsigned long long *cnt, int s, unsigned c) {
+    unsigned act = __activemask();
+    unsigned grp = __match_any_sync(act, s);
+    unsigned long long tot = 0;
+    // sum over the group (lanes with the same simulation)
+    for (int l = 0; l < 32; ++l) {
+        if (!(act & (1u << l))) continue;
+        unsigned x = __shfl_sync(act, c, l);
+        if (grp & (1u << l)) tot += x;
+    }
+    int leader = __ffs(grp) - 1;
+    if ((threadIdx.x & 31) == leader) atomicAdd(&cnt[s], tot);
+}
+
+template <typename R, int D, int K>
+__global__ void __launch_bounds__(256) k_density(View v, int stage) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.np) return;
+    using T4 = typename V4<R>::T;
+    const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
+    int s = v.b_sim[i];
+    const SimDev &S = v.sims[s];
+    PairFrame<R, D> fr;
+    fr.init(S);
+    KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
+    KConst<R> kl = make_kconst<R>(K, S.hl, S.sig_l);
+    T4 pi = P[i];
+    Acc<R> rs, rl;
+    rs.init((R)S.ws0);
+    rl.init((R)S.wl0);
+    unsigned cnt = 0;
+    for_pairs<R, D>(v, S, fr, P, i, pi, [&](int j, const T4 &pj, const R *d, R rsq) {
+        R r = rsqrt_<R>(rsq);
+        R w, g;
+        kernel_wg<K, R>(ks, r, &w, &g);
+        rs.add(pj.w * w);
+        kernel_wg<K, R>(kl, r, &w, &g);
+        rl.add(pj.w * w);
+        ++cnt;
+    });
+    R rho = rs.get(), rhol = rl.get();
+    double T = (v.ue_in[i] + S.a * (double)rho) / S.kb;
+    if (T < 0.0) T = 0.0;
+    R Tr = (R)T;
+    R p = (rho * (R)S.kb * Tr) / ((R)1 - rho * (R)S.b);
+    R pco = -(R)S.a * rhol * rhol;
+    ((R *)v.rho)[i] = rho;
+    ((R *)v.rho_l)[i] = rhol;
+    ((R *)v.temp)[i] = Tr;
+    ((R *)v.pres)[i] = p;
+    ((R *)v.pco)[i] = pco;
+    if (stage == 0) {
+        ((R *)v.rho0)[i] = rho;
+        ((R *)v.pres0)[i] = p;
+        ((R *)v.pco0)[i] = pco;
+    }
+    ((T4 *)v.pk_f)[i] = make_v4<R>(p / (rho * rho), pco / (rhol * rhol), rho, Tr);
+    if (!isfinite((double)p) || !isfinite((double)rho) || !isfinite((double)pco))
+        set_err(v.err, v.err_any, s, SPH_ENAN);
+    add_pair_count(v.pair_count, s, cnt);
+}
+
+template <typename R, int D, int K>
+__global__ void __launch_bounds__(256) k_heat(View v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.np) return;
+    using T4 = typename V4<R>::T;
+    const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
+    const T4 *__restrict__ F = (const T4 *)v.pk_f;
+    int s = v.b_sim[i];
+    const SimDev &S = v.sims[s];
+    PairFrame<R, D> fr;
+    fr.init(S);
+    KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
+    T4 pi = P[i];
+    T4 fi = F[i];
+    Acc<R> q[3];
+    q[0].init(0);
+    q[1].init(0);
+    q[2].init(0);
+    for_pairs<R, D>(v, S, fr, P, i, pi, [&](int j, const T4 &pj, const R *d, R rsq) {
+        R r = rsqrt_<R>(rsq);
+        R g = kernel_g<K, R>(ks, r);
+        T4 fj = F[j];
+        R f = (pj.w / fj.z) * (fj.w - fi.w) * g;
+        q[0].add(f * d[0]);
+        q[1].add(f * d[1]);
+        if (D == 3) q[2].add(f * d[2]);
+    });
+    R kap = (R)S.kappa;
+    R qq[3] = {kap * q[0].get(), kap * q[1].get(), kap * q[2].get()};
+    R ir2 = (R)1 / (fi.z * fi.z);
+    for (int a = 0; a < D; ++a) ((R *)v.q[a])[i] = qq[a];
+    ((T4 *)v.pk_q)[i] = make_v4<R>(qq[0] * ir2, qq[1] * ir2, qq[2] * ir2, (R)0);
+}
+
+// Next evaluation state: positions/velocities/energy in FP64 plus packed
+// cell-local copies relative to the particle's cell (binned at x0).
+template <typename R, int D>
+__device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S, int i,
+                                                 const double *x, const double *vel, double u,
+                                                 double m) {
+    using T4 = typename V4<R>::T;
+    R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double sh;
+        int ci = cell_coord(v.b_pos[a][i], S, a, &sh);
+        xl[a] = (R)((x[a] - sh) - cell_centre(ci, S, a));
+        vv[a] = (R)vel[a];
+        v.xe_out[a][i] = x[a];
+        v.ve_out[a][i] = vel[a];
+        double disp = fabs(x[a] - v.b_pos[a][i]);
+        if (disp > S.slack_half[a]) set_err(v.err, v.err_any, v.b_sim[i], SPH_ESKIN);
+    }
+    v.ue_out[i] = u;
+    ((T4 *)v.pk_pos_out)[i] = make_v4<R>(xl[0], xl[1], xl[2], (R)m);
+    ((T4 *)v.pk_vel_out)[i] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
+}
+
+// Final state of the step into A (same slot as B), with the teleport wrap.
+template <typename R, int D>
+__device__ __forceinline__ void write_final_state(const View &v, const SimDev &S, int i,
+                                                  double *x, const double *vel, double u) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double L = S.L[a];
+        if (x[a] > L) x[a] = 0;
+        if (x[a] < 0) x[a] = L;
+        v.a_pos[a][i] = x[a];
+        v.a_vel[a][i] = vel[a];
+    }
+    v.a_u[i] = u;
+    v.a_m[i] = v.b_m[i];
+    v.a_id[i] = v.b_id[i];
+    v.a_sim[i] = v.b_sim[i];
+}
+
+template <typename R, int D, int K>
+__global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int integ, int visc,
+                                               int heat) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.np) return;
+    using T4 = typename V4<R>::T;
+    const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
+    const T4 *__restrict__ V = (const T4 *)v.pk_vel_in;
+    const T4 *__restrict__ F = (const T4 *)v.pk_f;
+    const T4 *__restrict__ Q = (const T4 *)v.pk_q;
+    int s = v.b_sim[i];
+    const SimDev &S = v.sims[s];
+    PairFrame<R, D> fr;
+    fr.init(S);
+    KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
+    KConst<R> kl = make_kconst<R>(K, S.hl, S.sig_l);
+    const R hs = (R)S.hs, eps_h2 = (R)(S.eps * S.hs * S.hs);
+    const R alpha_c = (R)(S.alpha * S.c), beta = (R)S.beta;
+    T4 pi = P[i], vi = V[i], fi = F[i];
+    T4 qi = heat ? Q[i] : make_v4<R>(0, 0, 0, 0);
+    Acc<R> ax[3], ud;
+    ax[0].init(0);
+    ax[1].init(0);
+    ax[2].init(0);
+    ud.init(0);
+    for_pairs<R, D>(v, S, fr, P, i, pi, [&](int j, const T4 &pj, const R *d, R rsq) {
+        R r = rsqrt_<R>(rsq);
+        R gs = kernel_g<K, R>(ks, r);
+        R gl = kernel_g<K, R>(kl, r);
+        T4 fj = F[j], vj = V[j];
+        R dvdx = (vj.x - vi.x) * d[0] + (vj.y - vi.y) * d[1];
+        if (D == 3) dvdx += (vj.z - vi.z) * d[2];
+        R ps = fi.x + fj.x;
+        if (visc && dvdx < (R)0) {
+            R mu = hs * dvdx / (rsq + eps_h2);
+            ps += (-alpha_c * mu + beta * mu * mu) / ((R)0.5 * (fi.z + fj.z));
+        }
+        R pl = fi.y + fj.y;
+        R gsum = ps * gs + pl * gl;
+        ax[0].add(gsum * d[0]);
+        ax[1].add(gsum * d[1]);
+        if (D == 3) ax[2].add(gsum * d[2]);
+        R du = (R)0.5 * gsum * dvdx * pj.w;
+        if (heat) {
+            T4 qj = Q[j];
+            R dq = (qi.x + qj.x) * d[0] + (qi.y + qj.y) * d[1];
+            if (D == 3) dq += (qi.z + qj.z) * d[2];
+            du -= dq * gs * pj.w;
+        }
+        ud.add(du);
+    });
+    R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
+    R udr = ud.get();
+    for (int a = 0; a < D; ++a) ((R *)v.vdot[a])[i] = vdr[a];
+    ((R *)v.udot)[i] = udr;
+    if (!isfinite((double)vdr[0]) || !isfinite((double)udr)) set_err(v.err, v.err_any, s, SPH_ENAN);
+    if (mode == 0) return;
+
+    // ---- integrator stage (c = xdot * dt as in integrator.py) ----
+    const double dt = S.dt;
+    double x0[3] = {0, 0, 0}, v0[3] = {0, 0, 0}, rd[3] = {0, 0, 0}, vd[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        x0[a] = v.b_pos[a][i];
+        v0[a] = v.b_vel[a][i];
+        rd[a] = v.ve_in[a][i];
+        vd[a] = (double)vdr[a];
+    }
+    double u0 = v.b_u[i], udd = (double)udr, m = v.b_m[i];
+    double x[3] = {0, 0, 0}, vel[3] = {0, 0, 0}, u;
+    bool final_stage = false;
+    if (integ == SPH_EULER) {
+        for (int a = 0; a < D; ++a) {
+            x[a] = dadd(x0[a], dmul(rd[a], dt));
+            vel[a] = dadd(v0[a], dmul(vd[a], dt));
+        }
+        u = dadd(u0, dmul(udd, dt));
+        final_stage = true;
+    } else if (integ == SPH_IEULER) {
+        if (stage == 0) {
+            for (int a = 0; a < D; ++a) {
+                ((R *)v.f0v[a])[i] = vdr[a];
+                x[a] = dadd(x0[a], dmul(rd[a], dt));
+                vel[a] = dadd(v0[a], dmul(vd[a], dt));
+            }
+            ((R *)v.f0u)[i] = udr;
+            u = dadd(u0, dmul(udd, dt));
+            write_eval_state<R, D>(v, S, i, x, vel, u, m);
+        } else {
+            for (int a = 0; a < D; ++a) {
+                double c1r = dmul(v0[a], dt), c2r = dmul(rd[a], dt);
+                x[a] = dadd(x0[a], dmul(dadd(c1r, c2r), 0.5));
+                double c1v = dmul((double)((const R *)v.f0v[a])[i], dt), c2v = dmul(vd[a], dt);
+                vel[a] = dadd(v0[a], dmul(dadd(c1v, c2v), 0.5));
+            }
+            double c1u = dmul((double)((const R *)v.f0u)[i], dt), c2u = dmul(udd, dt);
+            u = dadd(u0, dmul(dadd(c1u, c2u), 0.5));
+            final_stage = true;
+        }
+    } else {  // RK4
+        double cr[3], cv[3], cu = dmul(udd, dt);
+        for (int a = 0; a < D; ++a) {
+            cr[a] = dmul(rd[a], dt);
+            cv[a] = dmul(vd[a], dt);
+        }
+        if (stage == 0) {
+            for (int a = 0; a < D; ++a) {
+                v.acc_r[a][i] = cr[a];
+                v.acc_v[a][i] = cv[a];
+                x[a] = dadd(x0[a], cr[a] / 2.0);
+                vel[a] = dadd(v0[a], cv[a] / 2.0);
+            }
+            v.acc_u[i] = cu;
+            u = dadd(u0, cu / 2.0);
+            write_eval_state<R, D>(v, S, i, x, vel, u, m);
+        } else if (stage < 3) {
+            for (int a = 0; a < D; ++a) {
+                v.acc_r[a][i] = dadd(v.acc_r[a][i], dmul(2.0, cr[a]));
+                v.acc_v[a][i] = dadd(v.acc_v[a][i], dmul(2.0, cv[a]));
+                x[a] = stage == 1 ? dadd(x0[a], cr[a] / 2.0) : dadd(x0[a], cr[a]);
+                vel[a] = stage == 1 ? dadd(v0[a], cv[a] / 2.0) : dadd(v0[a], cv[a]);
+            }
+            v.acc_u[i] = dadd(v.acc_u[i], dmul(2.0, cu));
+            u = stage == 1 ? dadd(u0, cu / 2.0) : dadd(u0, cu);
+            write_eval_state<R, D>(v, S, i, x, vel, u, m);
+        } else {
+            for (int a = 0; a < D; ++a) {
+                x[a] = dadd(x0[a], dmul(1.0 / 6.0, dadd(v.acc_r[a][i], cr[a])));
+                vel[a] = dadd(v0[a], dmul(1.0 / 6.0, dadd(v.acc_v[a][i], cv[a])));
+            }
+            u = dadd(u0, dmul(1.0 / 6.0, dadd(v.acc_u[i], cu)));
+            final_stage = true;
+        }
+    }
+    if (final_stage) {
+        if (S.thermostat) {
+            // particles.py:450-457: T <- T * target / mean(T); u <- k_B T - a rho
+            R *tp = (R *)v.temp;
+            double T = (double)tp[i] * v.t_scale[s];
+            u = dadd(dmul(T, S.kb), -dmul(S.a, (double)((const R *)v.rho0)[i]));
+            tp[i] = (R)T;
+        }
+        write_final_state<R, D>(v, S, i, x, vel, u);
+    }
+}
+
+// ---- dispatch ----
+#define SPH_DISPATCH(PREC, DIM, KERN, CALL)                                       \
+    do {                                                                          \
+        if (PREC == SPH_MIXED) {                                                  \
+            using R = float;                                                      \
+            if (DIM == 2) { constexpr int D = 2; SPH_DISPATCH_K(KERN, CALL); }    \
+            else { constexpr int D = 3; SPH_DISPATCH_K(KERN, CALL); }             \
+        } else {                                                                  \
+            using R = double;                                                     \
+            if (DIM == 2) { constexpr int D = 2; SPH_DISPATCH_K(KERN, CALL); }    \
+            else { constexpr int D = 3; SPH_DISPATCH_K(KERN, CALL); }             \
+        }                                                                         \
+    } while (0)
+#define SPH_DISPATCH_K(KERN, CALL)                                                \
+    switch (KERN) {                                                               \
+        case SPH_KERNEL_GAUSSIAN: { constexpr int K = SPH_KERNEL_GAUSSIAN; CALL; break; } \
+        case SPH_KERNEL_LUCY: { constexpr int K = SPH_KERNEL_LUCY; CALL; break; }         \
+        case SPH_KERNEL_DEBRUN: { constexpr int K = SPH_KERNEL_DEBRUN; CALL; break; }     \
+        default: { constexpr int K = SPH_KERNEL_CUBIC; CALL; break; }                     \
+    }
+
+void launch_density(const View &v, int precision, int kernel, int stage, int block,
+                    cudaStream_t s) {
+    if (v.np <= 0) return;
+    int nb = (v.np + block - 1) / block;
+    SPH_DISPATCH(precision, v.dim, kernel,
+                 (k_density<R, D, K><<<nb, block, 0, s>>>(v, stage)));
+}
+
+void launch_heat(const View &v, int precision, int kernel, int block, cudaStream_t s) {
+    if (v.np <= 0) return;
+    int nb = (v.np + block - 1) / block;
+    SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K><<<nb, block, 0, s>>>(v)));
+}
+
+void launch_force(const View &v, int precision, int kernel, int viscosity, int heat,
+                  int integrator, int stage, int mode, int block, cudaStream_t s) {
+    if (v.np <= 0) return;
+    int nb = (v.np + block - 1) / block;
+    SPH_DISPATCH(precision, v.dim, kernel,
+                 (k_force<R, D, K><<<nb, block, 0, s>>>(v, stage, mode, integrator, viscosity,
+                                                       heat)));
+}
+
+// ---- thermostat: per-chunk FP64 partial sums of T, then one thread per
+// simulation sums its chunks in order (deterministic) ----
+template <typename R>
+__global__ void k_tsum_chunks(View v) {
+    int c = blockIdx.x;
+    int b = v.chunk_start[c], n = v.chunk_len[c];
+    double x = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) x += (double)((const R *)v.temp)[b + k];
+    __shared__ double sh[256];
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) v.tsum_part[c] = sh[0];
+}
+
+__global__ void k_tsum_sims(View v, int nsims) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsims) return;
+    SimDev &S = v.sims[s];
+    if (!S.active) return;
+    long long done = v.steps[s] + 1;
+    v.steps[s] = done;
+    if (!S.thermostat) return;
+    double sum = 0.0;
+    for (int c = 0; c < v.nchunks; ++c)
+        if (v.chunk_sim[c] == s) sum += v.tsum_part[c];
+    double tav = sum / (double)S.n;
+    double target = S.T0;
+    if (S.ramp > 0) {
+        double f = (double)done / (double)S.ramp;
+        if (f > 1.0) f = 1.0;
+        target = S.T0 + (S.T1 - S.T0) * f;
+    }
+    v.t_scale[s] = target / tav;
+}
+
+void launch_tsum(const View &v, int precision, int nsims, cudaStream_t s) {
+    if (v.nchunks > 0) {
+        if (precision == SPH_MIXED) k_tsum_chunks<float><<<v.nchunks, 256, 0, s>>>(v);
+        else k_tsum_chunks<double><<<v.nchunks, 256, 0, s>>>(v);
+    }
+    k_tsum_sims<<<(nsims + 127) / 128, 128, 0, s>>>(v, nsims);
+}
+
+// ---- pair-set export (VerletList.build + NeighbourList.separations
+// attributes); exact FP64 test on every candidate, not on the hot path ----
+template <int D>
+__global__ void k_pair_rows(View v, int off, int n, long long *row_count) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int i = off + k;
+    const SimDev &S = v.sims[v.b_sim[i]];
+    constexpr int NB = NbrCount<D>::value;
+    const int *nb = v.nbr + (size_t)v.cell_b[i] * NB;
+    int idi = v.b_id[i];
+    long long c = 0;
+    for (int t = 0; t < NB; ++t) {
+        int cj = nb[t];
+        if (cj < 0) continue;
+        for (int j = v.cell_start[cj]; j < v.cell_start[cj + 1]; ++j) {
+            if (j == i || v.b_id[j] < idi) continue;
+            if (exact_rsq<D>(v.xe_in, S, i, j) < S.thr) ++c;
+        }
+    }
+    row_count[idi] = c;
+}
+
+template <int D>
+__global__ void k_pair_write(View v, int off, int n, const long long *row_start, long long *iap,
+                             double *drij, double *rsq, double *dv) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int i = off + k;
+    const SimDev &S = v.sims[v.b_sim[i]];
+    constexpr int NB = NbrCount<D>::value;
+    const int *nb = v.nbr + (size_t)v.cell_b[i] * NB;
+    int idi = v.b_id[i];
+    long long base = row_start[idi];
+    long long m = 0;
+    for (int t = 0; t < NB; ++t) {
+        int cj = nb[t];
+        if (cj < 0) continue;
+        for (int j = v.cell_start[cj]; j < v.cell_start[cj + 1]; ++j) {
+            if (j == i || v.b_id[j] < idi) continue;
+            double r2 = exact_rsq<D>(v.xe_in, S, i, j);
+            if (!(r2 < S.thr)) continue;
+            // insertion into the row, ordered by j's original index
+            int idj = v.b_id[j];
+            long long p = base + m;
+            while (p > base && iap[2 * (p - 1) + 1] > idj) {
+                iap[2 * p] = iap[2 * (p - 1)];
+                iap[2 * p + 1] = iap[2 * (p - 1) + 1];
+                if (rsq) rsq[p] = rsq[p - 1];
+                if (drij)
+                    for (int a = 0; a < D; ++a) drij[p * D + a] = drij[(p - 1) * D + a];
+                if (dv)
+                    for (int a = 0; a < D; ++a) dv[p * D + a] = dv[(p - 1) * D + a];
+                --p;
+            }
+            iap[2 * p] = idi;
+            iap[2 * p + 1] = idj;
+            if (rsq) rsq[p] = r2;
+            for (int a = 0; a < D; ++a) {
+                double d = __dsub_rn(v.xe_in[a][j], v.xe_in[a][i]);
+                if (d > S.half_L[a]) d = __dsub_rn(d, S.L[a]);
+                if (d < -S.half_L[a]) d = __dadd_rn(d, S.L[a]);
+                if (drij) drij[p * D + a] = d;
+                if (dv) dv[p * D + a] = __dsub_rn(v.ve_in[a][j], v.ve_in[a][i]);
+            }
+            ++m;
+        }
+    }
+}
+
+void launch_pair_rows(const View &v, int precision, int sim_off, int n, long long *row_count,
+                      cudaStream_t s) {
+    (void)precision;
+    if (n <= 0) return;
+    int nb = (n + 127) / 128;
+    if (v.dim == 2) k_pair_rows<2><<<nb, 128, 0, s>>>(v, sim_off, n, row_count);
+    else k_pair_rows<3><<<nb, 128, 0, s>>>(v, sim_off, n, row_count);
+}
+
+void launch_pair_write(const View &v, int precision, int sim_off, int n,
+                       const long long *row_start, long long *iap, double *drij, double *rsq,
+                       double *dv, cudaStream_t s) {
+    (void)precision;
+    if (n <= 0) return;
+    int nb = (n + 127) / 128;
+    if (v.dim == 2)
+        k_pair_write<2><<<nb, 128, 0, s>>>(v, sim_off, n, row_start, iap, drij, rsq, dv);
+    else
+        k_pair_write<3><<<nb, 128, 0, s>>>(v, sim_off, n, row_start, iap, drij, rsq, dv);
+}
+
+// exclusive scan of n+1 int64 entries in place (export path only)
+__global__ void k_scan64(long long *data, int n) {
+    __shared__ long long sh[1024];
+    __shared__ long long carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base <= n; base += 1024) {
+        int i = base + threadIdx.x;
+        long long x = (i <= n) ? data[i] : 0;
+        sh[threadIdx.x] = x;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            long long y = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += y;
+            __syncthreads();
+        }
+        if (i <= n) data[i] = sh[threadIdx.x] - x + carry;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += sh[1023];
+        __syncthreads();
+    }
+}
+
+void launch_scan64(long long *data, int n, cudaStream_t s) {
+    k_scan64<<<1, 1024, 0, s>>>(data, n);
+}
+
+}  // namespace sph

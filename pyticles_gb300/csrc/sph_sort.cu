@@ -1,0 +1,284 @@
+// sph_sort.cu -- counting-sort cell binning into Morton-ordered cells, the
+// permutation of the state into cell order, and host<->engine layout copies.
+//
+// Per step: k_bin (cell id + arrival rank, one atomic per particle) ->
+// exclusive scan of the cell counts -> k_scatter -> k_cellsort (within each
+// cell, order members by their previous slot, which makes the sort stable
+// and the whole step deterministic) -> k_permute (gather the FP64 state into
+// B and write the packed cell-local FP32/FP64 copies of the first evaluation).
+#include "sph_device.cuh"
+
+namespace sph {
+
+__global__ void k_bin(View v, int np_a) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np_a) return;
+    int s = v.a_sim[k];
+    int c = -1, rk = 0;
+    if (s >= 0) {
+        const SimDev &S = v.sims[s];
+        if (S.active) {
+            int lin = 0, mul = 1;
+            for (int a = 0; a < v.dim; ++a) {
+                double sh;
+                int ci = cell_coord(v.a_pos[a][k], S, a, &sh);
+                lin += ci * mul;
+                mul *= S.nc[a];
+            }
+            c = S.cell_off + v.morton[S.cell_off + lin];
+            rk = atomicAdd(&v.cell_count[c], 1);
+        }
+    }
+    v.cell_of[k] = c;
+    v.rank[k] = rk;
+}
+
+void launch_bin(const View &v, int np_a, cudaStream_t s) {
+    if (np_a <= 0) return;
+    k_bin<<<(np_a + 255) / 256, 256, 0, s>>>(v, np_a);
+}
+
+// ---- exclusive scan of int counts: start[i] = sum count[<i], start[n] = total ----
+constexpr int kScanBlock = 1024;
+constexpr int kScanPer = 4;
+constexpr int kScanTile = kScanBlock * kScanPer;
+
+__device__ __forceinline__ int block_excl_scan(int x, int *total) {
+    __shared__ int warp_sums[33];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int nw = blockDim.x >> 5;
+        int ws = lane < nw ? warp_sums[lane] : 0;
+        int wi = ws;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        if (lane < nw) warp_sums[lane] = wi - ws;
+        if (lane == nw - 1) warp_sums[32] = wi;
+    }
+    __syncthreads();
+    int res = incl - x + warp_sums[wid];
+    *total = warp_sums[32];
+    __syncthreads();
+    return res;
+}
+
+__global__ void k_scan_reduce(const int *count, int n, int *block_tmp) {
+    int base = blockIdx.x * kScanTile;
+    int sum = 0;
+    for (int t = 0; t < kScanPer; ++t) {
+        int i = base + t * kScanBlock + threadIdx.x;
+        if (i < n) sum += count[i];
+    }
+    int total;
+    block_excl_scan(sum, &total);
+    if (threadIdx.x == 0) block_tmp[blockIdx.x] = total;
+}
+
+__global__ void k_scan_top(int *block_tmp, int nb) {
+    // single block, sequential chunks of 1024
+    int carry = 0;
+    for (int base = 0; base < nb; base += kScanBlock) {
+        int i = base + threadIdx.x;
+        int x = i < nb ? block_tmp[i] : 0;
+        int total;
+        int e = block_excl_scan(x, &total);
+        if (i < nb) block_tmp[i] = e + carry;
+        carry += total;
+    }
+    if (threadIdx.x == 0) block_tmp[nb] = carry;
+}
+
+__global__ void k_scan_apply(const int *count, int *start, int n, const int *block_tmp, int nb) {
+    int base = blockIdx.x * kScanTile;
+    // each thread owns kScanPer consecutive elements
+    int i0 = base + threadIdx.x * kScanPer;
+    int loc[kScanPer];
+    int sum = 0;
+#pragma unroll
+    for (int t = 0; t < kScanPer; ++t) {
+        loc[t] = (i0 + t < n) ? count[i0 + t] : 0;
+        sum += loc[t];
+    }
+    int total;
+    int e = block_excl_scan(sum, &total) + block_tmp[blockIdx.x];
+#pragma unroll
+    for (int t = 0; t < kScanPer; ++t) {
+        if (i0 + t < n) start[i0 + t] = e;
+        e += loc[t];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) start[n] = block_tmp[nb];
+}
+
+void launch_scan(int *count, int *start, int n, int *block_tmp, cudaStream_t s) {
+    int nb = (n + kScanTile - 1) / kScanTile;
+    if (nb < 1) nb = 1;
+    k_scan_reduce<<<nb, kScanBlock, 0, s>>>(count, n, block_tmp);
+    k_scan_top<<<1, kScanBlock, 0, s>>>(block_tmp, nb);
+    k_scan_apply<<<nb, kScanBlock, 0, s>>>(count, start, n, block_tmp, nb);
+}
+
+__global__ void k_scatter(View v, int np_a) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np_a) return;
+    int c = v.cell_of[k];
+    if (c >= 0) v.order_tmp[v.cell_start[c] + v.rank[k]] = k;
+}
+
+void launch_scatter(const View &v, int np_a, cudaStream_t s) {
+    if (np_a <= 0) return;
+    k_scatter<<<(np_a + 255) / 256, 256, 0, s>>>(v, np_a);
+}
+
+// One warp per cell: the rank of each member is the number of members with a
+// smaller previous slot, so the within-cell order no longer depends on the
+// order in which the atomics of k_bin arrived.
+__global__ void k_cellsort(View v, int ncells) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= ncells) return;
+    int b = v.cell_start[warp], e = v.cell_start[warp + 1];
+    int m = e - b;
+    for (int x = lane; x < m; x += 32) {
+        int val = v.order_tmp[b + x];
+        int r = 0;
+        for (int t = 0; t < m; ++t) r += (v.order_tmp[b + t] < val) ? 1 : 0;
+        v.order[b + r] = val;
+        v.cell_b[b + r] = warp;
+    }
+}
+
+void launch_cellsort(const View &v, int ncells, cudaStream_t s) {
+    if (ncells <= 0) return;
+    int threads = ncells * 32;
+    k_cellsort<<<(threads + 255) / 256, 256, 0, s>>>(v, ncells);
+}
+
+// Gather the state into B (cell order) and pack the first evaluation's
+// cell-local coordinates: xl = wrap(x) - centre of the particle's cell.
+template <typename R>
+__global__ void k_permute(View v) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= v.np) return;
+    int k = v.order[j];
+    int s = v.a_sim[k];
+    const SimDev &S = v.sims[s];
+    R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
+    for (int a = 0; a < v.dim; ++a) {
+        double x = v.a_pos[a][k];
+        double vel = v.a_vel[a][k];
+        v.b_pos[a][j] = x;
+        v.b_vel[a][j] = vel;
+        double sh;
+        int ci = cell_coord(x, S, a, &sh);
+        xl[a] = (R)((x - sh) - cell_centre(ci, S, a));
+        vv[a] = (R)vel;
+    }
+    double m = v.a_m[k];
+    v.b_u[j] = v.a_u[k];
+    v.b_m[j] = m;
+    v.b_id[j] = v.a_id[k];
+    v.b_sim[j] = s;
+    using T4 = typename V4<R>::T;
+    ((T4 *)v.pk_pos_out)[j] = make_v4<R>(xl[0], xl[1], xl[2], (R)m);
+    ((T4 *)v.pk_vel_out)[j] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
+}
+
+void launch_permute(const View &v, int precision, cudaStream_t s) {
+    if (v.np <= 0) return;
+    int nb = (v.np + 255) / 256;
+    if (precision == SPH_MIXED) k_permute<float><<<nb, 256, 0, s>>>(v);
+    else k_permute<double><<<nb, 256, 0, s>>>(v);
+}
+
+// ---- layout copies ----
+__global__ void k_load_aos(double *d0, double *d1, double *d2, const double *src, int n, int dim) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d0[i] = src[(size_t)i * dim + 0];
+    d1[i] = src[(size_t)i * dim + 1];
+    if (dim == 3) d2[i] = src[(size_t)i * dim + 2];
+}
+
+void launch_load_aos(double *dst[3], const double *src, int n, int dim, cudaStream_t s) {
+    if (n <= 0) return;
+    k_load_aos<<<(n + 255) / 256, 256, 0, s>>>(dst[0], dst[1], dst[2], src, n, dim);
+}
+
+__global__ void k_store_aos(double *dst, const double *s0, const double *s1, const double *s2,
+                            const int *id, int off, int n, int dim) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int i = id[off + k];
+    dst[(size_t)i * dim + 0] = s0[off + k];
+    dst[(size_t)i * dim + 1] = s1[off + k];
+    if (dim == 3) dst[(size_t)i * dim + 2] = s2[off + k];
+}
+
+void launch_store_aos(double *dst, double *const src[3], const int *id, int off, int n, int dim,
+                      cudaStream_t s) {
+    if (n <= 0) return;
+    k_store_aos<<<(n + 255) / 256, 256, 0, s>>>(dst, src[0], src[1], src[2], id, off, n, dim);
+}
+
+__global__ void k_store_scalar(double *dst, const double *src, const int *id, int off, int n) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dst[id[off + k]] = src[off + k];
+}
+
+void launch_store_scalar(double *dst, const double *src, const int *id, int off, int n,
+                         cudaStream_t s) {
+    if (n <= 0) return;
+    k_store_scalar<<<(n + 255) / 256, 256, 0, s>>>(dst, src, id, off, n);
+}
+
+template <typename R>
+__global__ void k_store_R(double *dst, const R *src, const int *id, int off, int n) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dst[id[off + k]] = (double)src[off + k];
+}
+
+void launch_store_R(double *dst, const void *src, int precision, const int *id, int off, int n,
+                    cudaStream_t s) {
+    if (n <= 0) return;
+    int nb = (n + 255) / 256;
+    if (precision == SPH_MIXED) k_store_R<float><<<nb, 256, 0, s>>>(dst, (const float *)src, id, off, n);
+    else k_store_R<double><<<nb, 256, 0, s>>>(dst, (const double *)src, id, off, n);
+}
+
+__global__ void k_fill_int(int *dst, int val, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = val;
+}
+
+void launch_fill_int(int *dst, int val, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_fill_int<<<(n + 255) / 256, 256, 0, s>>>(dst, val, n);
+}
+
+__global__ void k_iota_sim(int *id, int *sim, int sim_id, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        id[i] = i;
+        sim[i] = sim_id;
+    }
+}
+
+void launch_iota_sim(int *id, int *sim, int sim_id, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_iota_sim<<<(n + 255) / 256, 256, 0, s>>>(id, sim, sim_id, n);
+}
+
+}  // namespace sph

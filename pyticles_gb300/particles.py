@@ -1,0 +1,249 @@
+"""Particle systems, mirroring pyticles' particles.py.
+
+SmoothParticleSystem keeps the reference's constructor, state arrays
+(r, v, m, rho, rho_lr, t, u, p, pco, vdot, udot, jq, h, hlr ...), its
+nlists / forces / nl_default wiring and update(dt).  update() uploads the
+host state to libsph, runs one integrator step on the GPU (density ->
+EOS -> forces/rates -> integrator -> periodic wrap -> thermostat) and copies
+the state and properties back, with the reference's post-update semantics
+(particles.py:459-494, 496-542).  run(dt, nsteps) advances several steps
+with a single upload and download.
+
+The engine configuration is derived from the attached objects:
+  box      PeriodicBox (box.py:28-47) -> periodic extents
+  nlist    VerletList(cutoff, tolerance) -> pair set; NeighbourList -> all pairs
+  forces   SpamComplete -> Lucy (or its `kernel`), viscosity eta/zeta,
+           optional heat flux; SpamForce + CohesiveSpamForce -> no viscosity;
+           SpamConduction -> heat flux
+  h, hlr   uniform short / long smoothing lengths
+"""
+import time
+
+import numpy as np
+
+from . import _abi
+from .box import MirrorBox, PeriodicBox
+from .engine import Engine
+from .forces import CohesiveSpamForce, SpamComplete, SpamConduction, SpamForce
+
+XMAX = 5
+YMAX = 5
+ZMAX = 1
+VMAX = 0.1
+VSPLIT = 10.0
+RAMAL = 0.5
+
+# properties.py:18-20
+ADASH = 2.0
+BDASH = 0.5
+KBDASH = 1.0
+
+
+class ParticleSystem:
+    """Particles with basic mechanical properties (particles.py:69-195)."""
+
+    def __init__(self, n, d=3, maxn=125, controllers=(), xmax=XMAX, ymax=YMAX, zmax=ZMAX,
+                 vmax=VMAX, simbox=None, mass=1.0, rinit=None, source=None, side=(5, 5, 5),
+                 integrator="rk4", spacing=0.1):
+        if d not in (2, 3):
+            raise ValueError("the GB300 engine runs 2D and 3D systems")
+        self.n = n
+        self.dim = d
+        self.maxn = maxn
+        self.dt = 0.0
+        self.steps = 0
+        self.box = simbox if simbox else MirrorBox(p=self, xmax=xmax, ymax=ymax, zmax=zmax)
+        if integrator not in _abi.INTEGRATORS:
+            raise KeyError(integrator)
+        self.integrator = integrator
+        self.r = self.box.xmax * np.random.random([self.maxn, self.dim])
+        self.m = np.zeros(self.maxn, dtype=float)
+        self.v = vmax * (np.random.random([self.maxn, self.dim]) - 0.5)
+        self.rdot = np.zeros(self.r.shape)
+        self.vdot = np.zeros(self.v.shape)
+        self.mdot = np.zeros(self.m.shape)
+        if rinit in ("grid", "fcc", "load"):
+            raise NotImplementedError(f"rinit={rinit!r} needs pyticles' absent configuration / "
+                                      "netCDF modules; set p.r directly")
+        self.m[:] = mass
+        self.colour = 1.0, 0.0, 0.0
+        self.nlists = []
+        self.forces = []
+        self.controllers = list(controllers)
+        self.timing = {"force time": -1, "deriv time": -1, "pairsep time": -1,
+                       "update time": -1, "integrate time": -1}
+
+    def rebuild_lists(self):
+        for nl in self.nlists:
+            if nl.rebuild_list:
+                nl.build()
+
+
+class SmoothParticleSystem(ParticleSystem):
+    """Long/short smoothing-length SPH system (particles.py:256-571).
+
+    precision -- 'fp64' (default: the reference's arithmetic) or 'mixed'
+                 (FP32 pair arithmetic, FP64 pair test and integrator)
+    """
+
+    def __init__(self, n, d=3, maxn=100, controllers=(), xmax=XMAX, ymax=YMAX, zmax=ZMAX,
+                 vmax=VMAX, rinit=None, side=None, mass=1.0, spacing=None, temperature=1.0,
+                 thermostat_temp=1.0, thermostat=False, hshort=1.0, hlong=3.0, source=None,
+                 integrator="ieuler", simbox=None, precision="fp64"):
+        ParticleSystem.__init__(self, n=n, d=d, xmax=xmax, ymax=ymax, zmax=zmax, rinit=rinit,
+                                side=side, mass=mass, source=source, spacing=spacing,
+                                integrator=integrator, vmax=vmax, maxn=maxn, simbox=simbox,
+                                controllers=controllers)
+        self.V_split = VSPLIT
+        self.r_amalg = RAMAL
+        self.rho = np.zeros(self.maxn)
+        self.rho_lr = np.zeros(self.maxn)
+        self.rhodot = np.zeros(self.rho.shape)
+        self.gradv = np.zeros([self.maxn, self.dim, self.dim])
+        self.jq = np.zeros([self.maxn, self.dim])
+        self.t = np.ones(self.maxn)
+        self.t[:] = temperature
+        self.thermostat = thermostat
+        self.u = np.ones(self.maxn, dtype=float)
+        self.udot = np.zeros(self.maxn, dtype=float)
+        self.h = np.zeros(self.maxn)
+        self.hlr = np.zeros(self.maxn)
+        self.h[:] = hshort
+        self.hlr[:] = hlong
+        self.p = np.zeros([self.maxn])
+        self.pco = np.zeros([self.maxn])
+        self.P = np.zeros([self.maxn, self.dim, self.dim])
+        self.thermostat_temp = thermostat_temp
+        self.precision = precision
+        self.timing["SPAM time"] = -1
+        self.timing["nlist rebuild time"] = -1
+        self._engine = None
+        self._engine_key = None
+        self._sim = None
+
+    # -- engine configuration ------------------------------------------------
+    def _nlist(self):
+        nl = getattr(self, "nl_default", None)
+        if nl is None and self.nlists:
+            nl = self.nlists[0]
+        if nl is None:
+            raise RuntimeError("attach a neighbour list (p.nlists / p.nl_default)")
+        return nl
+
+    def engine_params(self, dt):
+        """sph_params for the attached box, neighbour list and forces."""
+        if not isinstance(self.box, PeriodicBox):
+            raise NotImplementedError("the GB300 engine needs a PeriodicBox "
+                                      f"(got {type(self.box).__name__})")
+        n = self.n
+        hs, hl = self.h[:n], self.hlr[:n]
+        if n and (np.any(hs != hs[0]) or np.any(hl != hl[0])):
+            raise NotImplementedError("per-particle smoothing lengths are not supported")
+        nl = self._nlist()
+        cutoff, tol = nl._cutoff_tol()
+        kw = dict(dim=self.dim, box=self.box.extents, h_short=float(hs[0]),
+                  h_long=float(hl[0]), cutoff=cutoff, tolerance=tol, dt=float(dt),
+                  integrator=self.integrator, thermostat=bool(self.thermostat),
+                  thermostat_temp=float(self.thermostat_temp), adash=ADASH, bdash=BDASH,
+                  kbdash=KBDASH)
+        comp = [f for f in self.forces if isinstance(f, SpamComplete)]
+        kinds = {type(f) for f in self.forces}
+        if comp:
+            f = comp[0]
+            kw.update(kernel=f.kernel, adash=f.adash, bdash=f.bdash, kbdash=f.kbdash,
+                      viscosity=(f.eta != 0.0 or f.zeta != 0.0), visc_alpha=f.eta,
+                      visc_beta=f.zeta, visc_eps=f.visc_eps, sound_speed=f.sound_speed,
+                      heat_flux=bool(f.heat_flux), thermalk=f.thermalk)
+        elif SpamForce in kinds and CohesiveSpamForce in kinds:
+            kw.update(kernel="lucy", viscosity=False)
+        else:
+            raise NotImplementedError("the GB300 engine evaluates SpamComplete or the "
+                                      "SpamForce + CohesiveSpamForce pair")
+        if SpamConduction in kinds:
+            kw["heat_flux"] = True
+        return _abi.make_params(**kw)
+
+    def _ensure_engine(self, dt):
+        prm = self.engine_params(dt)
+        key = (repr(sorted(_abi.params_dict(prm).items())), self.n, self.precision)
+        n = self.n
+        if self._engine is None or self._engine_key != key:
+            if self._engine is not None:
+                self._engine.close()
+            self._engine = Engine(prm, precision=self.precision, max_particles=max(n, 1),
+                                  max_sims=1)
+            self._sim = self._engine.add(prm, self.r[:n], self.v[:n], self.m[:n], self.u[:n])
+            self._engine_key = key
+        else:
+            self._engine.set_state(self._sim, self.r[:n], self.v[:n], self.m[:n], self.u[:n])
+        return self._engine
+
+    def _download(self, props_fn):
+        n = self.n
+        e = self._engine
+        r, v, u = e.get_state(self._sim)
+        self.r[:n] = r
+        self.v[:n] = v
+        self.u[:n] = u
+        out = props_fn(self._sim)
+        self.rho[:n] = out["rho"]
+        self.rho_lr[:n] = out["rho_lr"]
+        self.t[:n] = out["t"]
+        self.p[:n] = out["p"]
+        self.pco[:n] = out["pco"]
+        self.vdot[:n] = out["vdot"]
+        self.udot[:n] = out["udot"]
+        self.jq[:n] = out["jq"]
+        self.rdot = self.v
+
+    # -- the reference's step API ---------------------------------------------
+    def derivatives(self):
+        """One evaluation of the rates at the current state on the GPU
+        (particles.py:544-567 with SpamComplete.apply)."""
+        t = time.time()
+        e = self._ensure_engine(self.dt if self.dt > 0 else 1.0)
+        out = e.derivatives(self._sim)
+        e.sync()
+        n = self.n
+        self.rho[:n] = out["rho"]
+        self.rho_lr[:n] = out["rho_lr"]
+        self.t[:n] = out["t"]
+        self.p[:n] = out["p"]
+        self.pco[:n] = out["pco"]
+        self.vdot[:n] = out["vdot"]
+        self.udot[:n] = out["udot"]
+        self.jq[:n] = out["jq"]
+        self.rdot = self.v
+        self.timing["force time"] = time.time() - t
+
+    def update(self, dt):
+        """One integrator step (particles.py:459-494)."""
+        self.run(dt, 1)
+
+    def run(self, dt, nsteps):
+        """nsteps integrator steps with one upload and one download."""
+        t1 = time.time()
+        self.dt = dt
+        t = time.time()
+        self.rebuild_lists()
+        self.timing["nlist rebuild time"] = time.time() - t
+        e = self._ensure_engine(dt)
+        t = time.time()
+        e.advance(nsteps)
+        e.sync()
+        self.timing["integrate time"] = time.time() - t
+        self._download(e.properties)
+        self.steps += nsteps
+        self.timing["update time"] = time.time() - t1
+
+    def apply_thermostat(self, target_temp):
+        """Scaling thermostat on the host arrays (particles.py:450-457); the
+        GPU step applies it itself when `thermostat` is set."""
+        tav = self.t.mean()
+        self.t = self.t * (target_temp / tav)
+        self.u = self.t * KBDASH - ADASH * self.rho
+
+    def close(self):
+        if self._engine is not None:
+            self._engine.close()
+            self._engine = None
