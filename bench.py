@@ -1,0 +1,388 @@
+"""Benchmark of the SPH step on GB300: pair-interactions/s.
+
+Workload (one "step" = one improved-Euler step = 2 derivative evaluations):
+2D van der Waals fluid, N = 1,048,576 (1024^2 lattice, spacing 1, jitter
++-0.1, T = 0.6, Lucy kernel, h_s = 3, h_l = 6, a = 2, b = 0.5, artificial
+viscosity, dt = 1e-3), periodic box, mixed precision, every step captured in
+one CUDA graph.  Synthetic seeded inputs (no dataset exists for this path).
+
+metric value = (unordered pairs with r < h_l by the FP64 minimum-image
+test) x 2 evaluations x K steps / device time of the K steps.
+
+    python bench.py [--steps K] [--warmup W] [--side 1024] [--impl ours|reference]
+
+Under torchrun (N > 1) each rank runs an independent replica (the
+simulations do not exchange data); value sums the ranks' work over the
+slowest rank's time.
+"""
+import argparse
+import json
+import math
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "pair-interactions/s & p50/p99 job latency, mixed vs plain FP64, 1 GB300"
+UNIT = "pair-interactions/s"
+L2_BYTES = 129e6
+# algorithmic flops per unordered pair per evaluation (add/mul/div/sqrt = 1,
+# fma = 2; compares and minimum image = 0): density 3d+24, force 10d+42,
+# 3D heat flux adds 7d+12 + 3d+4
+FLOPS_DENSITY = {2: 30, 3: 33}
+FLOPS_FORCE = {2: 62, 3: 72}
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def force_bytes_per_particle(dim, rsize, stage_final):
+    """Unique bytes the force pass moves per particle (each array read or
+    written once): packed position/velocity/force factors, cell and
+    simulation ids, FP64 x0, v0, evaluation velocity, u0, m; writes of the
+    rates plus either the next evaluation state or the final state."""
+    v4 = 4 * rsize
+    reads = 3 * v4 + 8 + 3 * 8 * dim + 16
+    if stage_final:
+        reads += (dim + 1) * rsize            # stage-0 rates
+        writes = (dim + 1) * rsize + 8 * (2 * dim + 2) + 8
+    else:
+        writes = 2 * (dim + 1) * rsize + 8 * (2 * dim + 1) + 2 * v4
+    return reads + writes
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        time.sleep(0.25)
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured", float(d.get("sm_max_mhz", 2070.0))
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback", 2070.0
+
+
+def committed_traffic(name):
+    """DRAM bytes per particle of one force launch from the committed ncu
+    summary (`dram_bytes_per_particle: X` line), or None."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_particle:\s*([0-9.eE+-]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+def initial_state(side, seed):
+    from pyticles_gb300 import workloads
+    prm, r, v, m, T0 = workloads.config_2d(side, seed, viscosity=True)
+    return prm, r, v, m, T0
+
+
+def gpu_initial_energy(prm, r, v, m, T0, stream):
+    """u0 = k_B T0 - a rho0 with rho0 from one GPU density evaluation."""
+    from pyticles_gb300 import Engine
+    with Engine(prm, "fp64", max_particles=len(r), stream=stream) as e:
+        s = e.add(prm, r, v, m, np.zeros(len(r)))
+        rho = e.derivatives(s)["rho"]
+    return T0 * prm.kbdash - prm.adash * rho
+
+
+def run_timed(prm, r, v, m, u, precision, steps, warmup, torch, stream, profile=True):
+    """Device time of `steps` steps captured in one graph, with per-pass
+    CUDA events recorded inside the graph."""
+    from pyticles_gb300 import Engine
+    e = Engine(prm, precision, max_particles=len(r), stream=stream.cuda_stream)
+    s = e.add(prm, r, v, m, u)
+    e.set_tuning(steps_per_graph=max(1, steps), use_graph=1)
+    e.advance(max(1, warmup))
+    e.sync()
+    if profile:
+        e.profile(True)
+    e.prepare()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    e.advance(steps)
+    t1.record(stream)
+    t1.synchronize()
+    ms = t0.elapsed_time(t1)
+    e.sync()
+    passes = e.profile_read() if profile else None
+    pairs = e.last_pair_total()
+    kps = e.kernels_per_step()
+    e.profile(False)
+    e.close()
+    return ms, pairs, passes, kps
+
+
+def run_e2e(prm, r, v, m, u, steps, torch, stream):
+    """Through the C ABI with host (pinned) buffers: every step copies the
+    state in, advances one step and reads the state back."""
+    from pyticles_gb300 import Engine
+    n, d = r.shape
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    hr, hv, hm, hu = pin((n, d)), pin((n, d)), pin((n,)), pin((n,))
+    hr[:], hv[:], hm[:], hu[:] = r, v, m, u
+    e = Engine(prm, "mixed", max_particles=n, stream=stream.cuda_stream)
+    s = e.add(prm, hr, hv, hm, hu)
+    e.set_tuning(steps_per_graph=1, use_graph=1)
+    for _ in range(3):
+        e.set_state(s, hr, hv, hm, hu)
+        e.advance(1)
+        e.get_state(s, hr, hv, hu)
+    e.sync()
+    t = time.perf_counter()
+    for _ in range(steps):
+        e.set_state(s, hr, hv, hm, hu)
+        e.advance(1)
+        e.get_state(s, hr, hv, hu)
+    e.sync()
+    wall = time.perf_counter() - t
+    pairs = e.last_pair_total()
+    e.close()
+    return wall, pairs, n * (2 * d + 2) * 8, n * (2 * d + 1) * 8
+
+
+def oracle_rate(side, seed, budget_s, max_steps):
+    """FP64 C oracle (OpenMP, all host threads) on a bounded sample."""
+    from oracle import oracle
+    prm, r, v, m, T0 = initial_state(side, seed)
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    nip = oracle.derivatives(prm, r, v, m, u)["nip"]
+    steps, t = 0, 0.0
+    while steps < max_steps and (steps == 0 or t < budget_s):
+        t0 = time.perf_counter()
+        r, v, u, _ = oracle.advance(prm, r, v, m, u, 1)
+        t += time.perf_counter() - t0
+        steps += 1
+    return nip * 2 * steps / t, steps, t, oracle.threads(), len(r)
+
+
+def reference_arm(args):
+    """The reference path's CPU implementation: the FP64 oracle port (the
+    reference is Python and its compiled parts do not build), all host
+    threads, one improved-Euler step of a 512^2 sample of the workload per
+    bench step."""
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return 0
+    side = min(args.side, 512)
+    from oracle import oracle
+    prm, r, v, m, T0 = initial_state(side, 1000)
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    nip = oracle.derivatives(prm, r, v, m, u)["nip"]
+    r, v, u, _ = oracle.advance(prm, r, v, m, u, max(0, min(args.warmup, 2)))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, v, u, _ = oracle.advance(prm, r, v, m, u, 1)
+    wall = time.perf_counter() - t0
+    value = nip * 2 * args.steps / wall
+    sample = (f"2D van der Waals fluid N={len(r)} ({side}^2 lattice, same density, kernels, "
+              f"viscosity and dt as the GPU workload), {args.steps} improved-Euler steps")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "2d_vdw_fluid", "n": len(r), "pairs_per_eval": nip,
+                       "evals_per_step": 2, "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.threads(),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--side", type=int, default=1024)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    from pyticles_gb300 import build
+    build.build()
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    prm, r, v, m, T0 = initial_state(args.side, 1000 + rank)
+    u = gpu_initial_energy(prm, r, v, m, T0, stream.cuda_stream)
+    n = len(r)
+    hbm_peak, peak_kind, sm_max = measured_peaks()
+
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clocks:
+        ms, pairs, passes, kps = run_timed(prm, r, v, m, u, "mixed", args.steps, args.warmup,
+                                           torch, stream)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        w = torch.tensor([float(pairs)], device="cuda")
+        dist.all_reduce(w, op=dist.ReduceOp.SUM)
+        pairs_all = float(w.item())
+    else:
+        pairs_all = float(pairs)
+    value = pairs_all * 2 * args.steps / (ms * 1e-3)
+
+    # plain FP64 GPU step on the same workload
+    ms64, pairs64, _, _ = run_timed(prm, r, v, m, u, "fp64", args.fp64_steps, 3, torch, stream,
+                                    profile=False)
+    fp64_value = pairs64 * 2 * args.fp64_steps / (ms64 * 1e-3)
+
+    # end to end through the C ABI with pinned host buffers
+    wall, pairs_e, h2d, d2h = run_e2e(prm, r, v, m, u, args.e2e_steps, torch, stream)
+    e2e_value = pairs_e * 2 * args.e2e_steps / wall
+
+    # roofline of the dominant pass (force + integrator epilogue)
+    f = passes["force"]
+    nlaunch = max(1, f["launches"])
+    avg_ms = f["ms"] / nlaunch
+    bpp = 0.5 * (force_bytes_per_particle(2, 4, False) + force_bytes_per_particle(2, 4, True))
+    achieved = bpp * n / (avg_ms * 1e-3) / 1e9
+    trafpp = committed_traffic("k_force_2d_mixed.md")
+    flops = FLOPS_FORCE[2] * pairs / (avg_ms * 1e-3) / 1e12
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    total_pass_ms = sum(p["ms"] for p in passes.values())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, csteps, ct, cores, cn = oracle_rate(min(args.side, 512), 1000, args.cpu_seconds,
+                                                  50)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"FP64 C oracle, 2D vdW fluid N={cn}, {csteps} improved-Euler steps, "
+                         f"{ct:.1f} s"}
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    working_set = n * (2 * 56 + 2 * 16 + 16 + 16 + 40 + 48)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded lattice + jitter, Maxwell velocities)",
+        "config": {
+            "workload": "2D van der Waals fluid, 1024^2 lattice, Lucy h_s=3 h_l=6, viscosity, "
+                        "improved Euler dt=1e-3, periodic",
+            "n": n, "pairs_per_eval": pairs, "evals_per_step": 2,
+            "precision": "mixed: f32 pair arithmetic + compensated sums, f64 pair test, "
+                         "integrator and reductions",
+            "graph": f"{args.steps} steps in one CUDA graph",
+            "l2": f"working set ~{working_set / 1e6:.0f} MB per step > 129 MB L2 (no flush)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value,
+            "pass_ms_per_step": {k: p["ms"] / args.steps for k, p in passes.items()},
+        },
+        "roofline": {
+            "bound": "hbm", "kernel": "k_force<float,2,lucy> (force + energy rate + integrator)",
+            "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+            "bytes_per_particle": bpp,
+            "traffic": None if trafpp is None else trafpp * n,
+            "fp32_pipe": {"achieved_tflops": flops, "peak_tflops": fp32_peak,
+                          "frac": flops / fp32_peak,
+                          "note": "algorithmic flops of the force pass; peak = 152 SMs x 128 "
+                                  "FP32 lanes x 2 x max SM clock (nominal)"},
+            "force_share_of_step": f["ms"] / total_pass_ms if total_pass_ms > 0 else None,
+        },
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
+        "gpu_launches": kps * args.steps,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

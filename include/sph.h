@@ -170,6 +170,30 @@ typedef struct sph_tuning {
 int sph_get_tuning(sph_engine *e, sph_tuning *t);
 int sph_set_tuning(sph_engine *e, const sph_tuning *t);
 
+/* Instantiates (and caches) the CUDA graph of tuning.steps_per_graph steps
+ * for the current layout without running it, so a later sph_advance starts
+ * without host-side graph construction. */
+int sph_prepare(sph_engine *e);
+
+/* Per-pass device timing with CUDA events recorded on the engine's stream,
+ * also inside captured graphs (the graph is rebuilt when this toggles).
+ * sph_profile(e, 1) clears the records and starts recording; after the
+ * work, sph_profile_read sums the elapsed time and the launch count per
+ * pass; sph_profile(e, 0) stops.  When a graph is replayed several times
+ * the events hold its last replay. */
+enum sph_pass {
+    SPH_PASS_SORT = 0,      /* binning, scan, scatter, in-cell order, permute */
+    SPH_PASS_DENSITY = 1,
+    SPH_PASS_HEAT = 2,
+    SPH_PASS_TSUM = 3,      /* thermostat reductions */
+    SPH_PASS_FORCE = 4,     /* force + energy rate + integrator stage */
+    SPH_NPASS = 5
+};
+int sph_profile(sph_engine *e, int32_t enable);
+int sph_profile_read(sph_engine *e, double ms[5], int64_t launches[5]);
+/* CUDA kernels one step launches (for launch accounting). */
+int sph_kernels_per_step(sph_engine *e, int64_t *n);
+
 /* Waits for the engine's stream; returns the first device-side error
  * (SPH_ENAN, SPH_ESKIN, ...) raised since the last call, then clears it. */
 int sph_sync(sph_engine *e);

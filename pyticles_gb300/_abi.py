@@ -22,6 +22,7 @@ SPH_ECUDA = 6
 SPH_ESKIN = 7
 SPH_ECAPACITY = 8
 SPH_ENOTFOUND = 9
+PASSES = ("sort", "density", "heat", "tsum", "force")
 
 STATUS_NAMES = {
     0: "SPH_OK", 1: "SPH_EINVAL", 2: "SPH_ENOMEM", 3: "SPH_ECELL_OVERFLOW",
@@ -165,6 +166,10 @@ def _declare(lib):
         "sph_sim_diagnostics": [vp, c_i32, P(ctypes.c_double)],
         "sph_get_tuning": [vp, P(SphTuning)],
         "sph_set_tuning": [vp, P(SphTuning)],
+        "sph_prepare": [vp],
+        "sph_profile": [vp, c_i32],
+        "sph_profile_read": [vp, P(ctypes.c_double), P(c_i64)],
+        "sph_kernels_per_step": [vp, P(c_i64)],
         "sph_sync": [vp],
         "sph_sim_status": [vp, c_i32, P(c_i32)],
         "sph_status_string": [ctypes.c_int],
@@ -184,7 +189,8 @@ def exported_symbols():
             "sph_sim_set_state", "sph_sim_get_state", "sph_sim_get_properties",
             "sph_sim_count", "sph_advance", "sph_sim_derivatives", "sph_sim_pair_count",
             "sph_sim_export_pairs", "sph_last_pair_total", "sph_sim_diagnostics",
-            "sph_get_tuning", "sph_set_tuning", "sph_sync", "sph_sim_status",
+            "sph_get_tuning", "sph_set_tuning", "sph_prepare", "sph_profile",
+            "sph_profile_read", "sph_kernels_per_step", "sph_sync", "sph_sim_status",
             "sph_status_string", "sph_version"]
 
 

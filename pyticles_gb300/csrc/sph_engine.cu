@@ -103,13 +103,20 @@ struct sph_engine {
     void *rho0 = nullptr, *pres0 = nullptr, *pco0 = nullptr;
     void *q[3] = {}, *vdot[3] = {}, *udot = nullptr, *f0v[3] = {}, *f0u = nullptr;
     double *acc_r[3] = {}, *acc_v[3] = {}, *acc_u = nullptr;
-    double *stage_buf = nullptr;  // AoS staging (cap_p * 3 doubles)
+    double *stage_buf = nullptr;  // AoS staging (3 cap_p) + one component (cap_p)
     SimDev *sims_d = nullptr;
     double *t_scale = nullptr, *tsum_part = nullptr;
     long long *steps_d = nullptr;
     unsigned long long *pair_count = nullptr;
     int *err = nullptr, *err_any = nullptr;
     int *chunk_sim = nullptr, *chunk_start = nullptr, *chunk_len = nullptr;
+
+    // profiling: event pairs recorded around each pass
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_pool;
+    size_t prof_used = 0;
+    struct ProfRec { int kind; cudaEvent_t a, b; };
+    std::vector<ProfRec> prof_recs;
 
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -444,8 +451,29 @@ int relayout(sph_engine *e) {
     return SPH_OK;
 }
 
+// Event pair around one pass when profiling is on (pool grows outside capture).
+struct ProfScope {
+    sph_engine *e;
+    cudaStream_t st;
+    int kind;
+    cudaEvent_t b = nullptr;
+    ProfScope(sph_engine *e_, int kind_, cudaStream_t st_) : e(e_), st(st_), kind(kind_) {
+        if (!e->prof_on || e->prof_used + 2 > e->prof_pool.size()) return;
+        cudaEvent_t a = e->prof_pool[e->prof_used++];
+        b = e->prof_pool[e->prof_used++];
+        cudaEventRecord(a, st);
+        e->prof_recs.push_back({kind, a, b});
+    }
+    ~ProfScope() {
+        if (b) cudaEventRecord(b, st);
+    }
+};
+
+constexpr int kSortKernels = 7;  // bin, 3 scan, scatter, in-cell order, permute
+
 // Counting sort of A into B plus the packed first-evaluation copies.
 void enqueue_prepare(sph_engine *e, cudaStream_t st) {
+    ProfScope ps(e, SPH_PASS_SORT, st);
     View v = make_view(e);
     stage_view(e, v, 0);
     v.pk_pos_out = e->pk_pos[0];
@@ -463,18 +491,61 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
     View v = make_view(e);
     stage_view(e, v, s);
     int blk = e->tune.block_size;
-    launch_density(v, e->precision, e->group.kernel, s, blk, st);
-    if (e->group.heat_flux) launch_heat(v, e->precision, e->group.kernel, blk, st);
-    if (mode == 1 && s == e->nstage - 1 && e->any_thermostat)
+    {
+        ProfScope ps(e, SPH_PASS_DENSITY, st);
+        launch_density(v, e->precision, e->group.kernel, s, blk, st);
+    }
+    if (e->group.heat_flux) {
+        ProfScope ps(e, SPH_PASS_HEAT, st);
+        launch_heat(v, e->precision, e->group.kernel, blk, st);
+    }
+    if (mode == 1 && s == e->nstage - 1 && e->any_thermostat) {
+        ProfScope ps(e, SPH_PASS_TSUM, st);
         launch_tsum(v, e->precision, (int)e->sims.size(), st);
-    launch_force(v, e->precision, e->group.kernel, e->group.viscosity, e->group.heat_flux,
-                 e->group.integrator, s, mode, blk, st);
+    }
+    {
+        ProfScope ps(e, SPH_PASS_FORCE, st);
+        launch_force(v, e->precision, e->group.kernel, e->group.viscosity, e->group.heat_flux,
+                     e->group.integrator, s, mode, blk, st);
+    }
 }
 
 void enqueue_step(sph_engine *e, cudaStream_t st) {
     enqueue_prepare(e, st);
     for (int s = 0; s < e->nstage; ++s) enqueue_stage(e, s, 1, st);
 }
+
+int64_t kernels_per_step(const sph_engine *e) {
+    int64_t k = kSortKernels;
+    k += (int64_t)e->nstage * (2 + (e->group.heat_flux ? 1 : 0));
+    if (e->any_thermostat) k += 2;
+    return k;
+}
+
+int ensure_prof_pool(sph_engine *e, size_t need) {
+    while (e->prof_pool.size() < need) {
+        cudaEvent_t ev;
+        CK(cudaEventCreate(&ev));
+        e->prof_pool.push_back(ev);
+    }
+    return SPH_OK;
+}
+
+int build_graph(sph_engine *e, int per) {
+    if (e->graph_exec && e->graph_steps == per) return SPH_OK;
+    free_graph(e);
+    if (e->prof_on) {
+        TRY(ensure_prof_pool(e, e->prof_used + (size_t)per * 2 * (1 + 4 * e->nstage) + 8));
+    }
+    cudaStream_t st = e->stream;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < per; ++k) enqueue_step(e, st);
+    CK(cudaStreamEndCapture(st, &e->graph));
+    CK(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
+    e->graph_steps = per;
+    return SPH_OK;
+}
+
 
 void after_advance(sph_engine *e, int steps) {
     e->a_extent = e->np_b;
@@ -550,7 +621,7 @@ int gather_R_vec(sph_engine *e, const Sim &S, void *const src[3], double *dst, i
     double *d = mem == SPH_DEVICE ? dst : e->stage_buf;
     // component-wise into AoS: store each component with stride dim via temp
     for (int a = 0; a < e->dim; ++a) {
-        double *tmp = e->stage_buf + (size_t)e->cap_p * 2;  // scratch third
+        double *tmp = e->stage_buf + (size_t)e->cap_p * 3;  // past the 3 cap_p AoS region
         launch_store_R(tmp, src[a], e->precision, e->b_id, S.part_off, (int)S.n, e->stream);
         CK(cudaMemcpy2DAsync(d + a, sizeof(double) * e->dim, tmp, sizeof(double), sizeof(double),
                              (size_t)S.n, cudaMemcpyDeviceToDevice, e->stream));
@@ -602,7 +673,7 @@ int alloc_particles(sph_engine *e) {
                    &e->pco0, &e->udot, &e->f0u};
     for (void **p : rs) TRY(dalloc((char **)p, P * e->rsize));
     if (e->group.integrator == SPH_RK4) TRY(dalloc(&e->acc_u, P));
-    TRY(dalloc(&e->stage_buf, P * 3));
+    TRY(dalloc(&e->stage_buf, P * 4));
     // pk_q must read as zero when heat flux is off
     CK(cudaMemset(e->pk_q, 0, P * e->v4size));
     CK(cudaMemset(e->a_sim, 0xff, P * sizeof(int)));
@@ -743,6 +814,7 @@ int sph_engine_destroy(sph_engine *e) {
     if (!e) return SPH_EINVAL;
     cudaStreamSynchronize(e->stream);
     free_all(e);
+    for (cudaEvent_t ev : e->prof_pool) cudaEventDestroy(ev);
     if (e->own_stream) cudaStreamDestroy(e->stream);
     delete e;
     return SPH_OK;
@@ -876,20 +948,14 @@ int sph_advance(sph_engine *e, int32_t nsteps) {
     // The binning pass covers A's used extent.  After simulations joined or
     // left, A holds dropped or unsorted particles beyond the live count;
     // that first step runs eagerly, after which A is compact (extent == live).
+    if (e->prof_on) TRY(ensure_prof_pool(e, e->prof_used + (size_t)nsteps * 2 * (1 + 4 * e->nstage) + 8));
     if (e->a_extent != e->np_b) {
         enqueue_step(e, st);
         after_advance(e, 1);
         ++done;
     }
     if (e->tune.use_graph && nsteps - done >= per) {
-        if (!e->graph_exec || e->graph_steps != per) {
-            free_graph(e);
-            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < per; ++k) enqueue_step(e, st);
-            CK(cudaStreamEndCapture(st, &e->graph));
-            CK(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
-            e->graph_steps = per;
-        }
+        TRY(build_graph(e, per));
         while (nsteps - done >= per) {
             CK(cudaGraphLaunch(e->graph_exec, st));
             after_advance(e, per);
@@ -1101,6 +1167,52 @@ int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
         e->layout_dirty = true;
         e->props_valid = false;
     }
+    return SPH_OK;
+}
+
+int sph_prepare(sph_engine *e) {
+    if (!e) return SPH_EINVAL;
+    TRY(ensure_layout(e));
+    if (e->np_b == 0 || !e->tune.use_graph) return SPH_OK;
+    if (e->a_extent != e->np_b) return SPH_OK;  // first step after a change runs eagerly
+    return build_graph(e, std::max(1, e->tune.steps_per_graph));
+}
+
+int sph_profile(sph_engine *e, int32_t enable) {
+    if (!e) return SPH_EINVAL;
+    CK(cudaStreamSynchronize(e->stream));
+    bool on = enable != 0;
+    if (on != e->prof_on) free_graph(e);
+    e->prof_on = on;
+    e->prof_recs.clear();
+    e->prof_used = 0;
+    if (on) TRY(ensure_prof_pool(e, 64));
+    return SPH_OK;
+}
+
+int sph_profile_read(sph_engine *e, double ms[5], int64_t launches[5]) {
+    if (!e || !ms || !launches) return SPH_EINVAL;
+    CK(cudaStreamSynchronize(e->stream));
+    for (int k = 0; k < SPH_NPASS; ++k) {
+        ms[k] = 0.0;
+        launches[k] = 0;
+    }
+    for (auto &r : e->prof_recs) {
+        float t = 0.0f;
+        if (cudaEventElapsedTime(&t, r.a, r.b) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        ms[r.kind] += t;
+        launches[r.kind] += r.kind == SPH_PASS_SORT ? kSortKernels : (r.kind == SPH_PASS_TSUM ? 2 : 1);
+    }
+    return SPH_OK;
+}
+
+int sph_kernels_per_step(sph_engine *e, int64_t *n) {
+    if (!e || !n) return SPH_EINVAL;
+    TRY(ensure_layout(e));
+    *n = kernels_per_step(e);
     return SPH_OK;
 }
 

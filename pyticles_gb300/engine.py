@@ -197,3 +197,22 @@ class Engine:
                       float(cur["cell_ratio"]), int(cur["use_graph"]),
                       int(cur["steps_per_graph"]))
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), "sph_set_tuning")
+
+    # -- launch-ready graphs and per-pass timing --
+    def prepare(self):
+        check(self._lib.sph_prepare(self._h), "sph_prepare")
+
+    def profile(self, enable=True):
+        check(self._lib.sph_profile(self._h, 1 if enable else 0), "sph_profile")
+
+    def profile_read(self):
+        ms = (ctypes.c_double * 5)()
+        n = (ctypes.c_int64 * 5)()
+        check(self._lib.sph_profile_read(self._h, ms, n), "sph_profile_read")
+        return {name: {"ms": ms[k], "launches": n[k]} for k, name in enumerate(_abi.PASSES)}
+
+    def kernels_per_step(self):
+        n = ctypes.c_int64()
+        check(self._lib.sph_kernels_per_step(self._h, ctypes.byref(n)), "sph_kernels_per_step")
+        return n.value
+

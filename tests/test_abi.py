@@ -1,0 +1,64 @@
+"""The C ABI library builds, loads without a GPU and exports every entry
+point include/sph.h declares; host-side parameter handling.  CPU only."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from pyticles_gb300 import _abi, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "sph.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(?:int|const char \*)\s*(sph_\w+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    return build.build()
+
+
+def test_header_and_binding_agree():
+    assert declared_symbols() == sorted(_abi.exported_symbols())
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    lib = ctypes.CDLL(libpath)
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_library_loads_and_reports_status_strings(libpath):
+    lib = _abi.lib()
+    assert lib.sph_version() >= 10000
+    for code, name in _abi.STATUS_NAMES.items():
+        s = lib.sph_status_string(code).decode()
+        assert s.startswith(name)
+
+
+def test_struct_layout_matches_header():
+    # 6 int32 + 3 doubles box + 15 doubles + int64
+    assert ctypes.sizeof(_abi.SphParams) == 6 * 4 + 3 * 8 + 15 * 8 + 8
+    assert _abi.SphParams.box.offset == 24
+
+
+def test_make_params_defaults_follow_reference():
+    p = _abi.make_params()
+    assert (p.adash, p.bdash, p.kbdash) == (2.0, 0.5, 1.0)   # properties.py:18-20
+    assert (p.visc_alpha, p.visc_beta) == (1.0, 0.1)          # SpamComplete eta, zeta
+    assert p.sound_speed == 1.0 and p.thermalk == 1.0
+    assert p.cutoff == 6.0                                     # max(h) for Lucy
+    c = _abi.make_params(kernel="cubic", h_short=1.0, h_long=2.5)
+    assert c.cutoff == 5.0                                     # support 2h
+
+
+def test_params_roundtrip():
+    p = _abi.make_params(dim=3, kernel="gaussian", box=(3, 4, 5), thermostat=True,
+                         thermostat_temp=0.7, thermostat_temp_end=0.35,
+                         thermostat_ramp_steps=500)
+    q = _abi.params_from_dict(_abi.params_dict(p))
+    assert bytes(q) == bytes(p)

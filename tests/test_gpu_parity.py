@@ -1,0 +1,272 @@
+"""GPU parity: the CUDA path through the C ABI against the golden vectors
+of the reference and the FP64 oracle.
+
+Tolerances: FP64 engine vs reference / oracle, one evaluation <= 1e-12
+relative L2 and a few steps <= 1e-10 (summation order differs); mixed
+precision <= 1e-6 relative L2 for density, force and energy rate (the
+stated target); pair sets identical as sets, squared distances within 2 ulp
+(tests/test_oracle_golden.py explains the ulp).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from pyticles_gb300 import Engine, build, workloads
+from pyticles_gb300._abi import SPH_ENAN, SPH_ESKIN, SphError
+from tests.golden_cases import SYSTEMS, load, params_of, rel_l2, sort_pairs
+
+pytestmark = pytest.mark.gpu
+
+EVAL_TOL = 1e-12
+STEP_TOL = 1e-10
+MIXED_TOL = 1e-6
+KEYS = ("rho", "rho_lr", "t", "p", "pco", "vdot", "udot")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    build.build()
+
+
+def one(prm, r, v, m, u, precision):
+    e = Engine(prm, precision, max_particles=len(r), max_sims=1)
+    return e, e.add(prm, r, v, m, u)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", SYSTEMS)
+def test_evaluation_matches_reference(name, precision):
+    g = load(name)
+    prm = params_of(g)
+    e, s = one(prm, g["r0"], g["v0"], g["m"], g["u0"], precision)
+    with e:
+        d = e.derivatives(s)
+        e.sync()
+        tol = EVAL_TOL if precision == "fp64" else MIXED_TOL
+        errs = {k: rel_l2(d[k], g["ev_" + k]) for k in KEYS}
+        print(name, precision, errs)
+        for k, err in errs.items():
+            assert err < tol, (k, err)
+        assert e.pair_count(s) == len(g["iap"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", SYSTEMS)
+def test_pair_set_bit_exact(name, precision):
+    g = load(name)
+    prm = params_of(g)
+    e, s = one(prm, g["r0"], g["v0"], g["m"], g["u0"], precision)
+    with e:
+        out = e.pairs(s)
+        ref, idx = sort_pairs(g["iap"])
+        assert np.array_equal(out["iap"], ref)
+        ref_rsq = g["rsq"][idx]
+        assert np.all(np.abs(out["rsq"] - ref_rsq) <= 2 * np.spacing(ref_rsq))
+        if "drij" in g:
+            assert np.array_equal(out["drij"], g["drij"][idx])
+            assert np.array_equal(out["dv"], g["dv"][idx])
+
+
+@pytest.mark.parametrize("case", ["exact_cut", "tol3d", "faces2d"])
+def test_pair_edge_cases(case):
+    g = load("pairs_edge")
+    dim = int(g[case + "_dim"])
+    prm = params_of({"dim": dim, "kernel": "lucy", "box": g[case + "_box"], "h_short": 1.0,
+                     "h_long": 1.0, "cutoff": float(g[case + "_cutoff"]),
+                     "tolerance": float(g[case + "_tol"]), "dt": 1e-3, "integrator": "ieuler",
+                     "thermostat": 0, "thermostat_temp": 1.0})
+    r = g[case + "_r"]
+    n = len(r)
+    ref, idx = sort_pairs(g[case + "_iap"])
+    for precision in ("fp64", "mixed"):
+        e, s = one(prm, r, np.zeros((n, dim)), np.ones(n), np.zeros(n), precision)
+        with e:
+            out = e.pairs(s)
+            assert np.array_equal(out["iap"], ref)
+            assert e.pair_count(s) == len(ref)
+
+
+@pytest.mark.parametrize("name", SYSTEMS)
+def test_fp64_steps_match_reference(name):
+    g = load(name)
+    prm = params_of(g)
+    e, s = one(prm, g["r0"], g["v0"], g["m"], g["u0"], "fp64")
+    with e:
+        e.advance(int(g["steps"]))
+        e.sync()
+        r, v, u = e.get_state(s)
+        assert rel_l2(r, g["r_final"]) < STEP_TOL
+        assert rel_l2(v, g["v_final"]) < STEP_TOL
+        assert rel_l2(u, g["u_final"]) < STEP_TOL
+        props = e.properties(s)
+        for k in KEYS:
+            assert rel_l2(props[k], g["after_" + k]) < STEP_TOL, k
+
+
+@pytest.mark.parametrize("name", SYSTEMS)
+def test_mixed_steps_track_reference(name):
+    g = load(name)
+    prm = params_of(g)
+    e, s = one(prm, g["r0"], g["v0"], g["m"], g["u0"], "mixed")
+    with e:
+        e.advance(int(g["steps"]))
+        e.sync()
+        r, v, u = e.get_state(s)
+        assert rel_l2(r, g["r_final"]) < MIXED_TOL
+        assert rel_l2(v, g["v_final"]) < MIXED_TOL
+        assert rel_l2(u, g["u_final"]) < MIXED_TOL
+
+
+def full_physics_cases():
+    """Terms without reference source (viscosity, heat flux, cubic spline):
+    checked against the oracle's restatement."""
+    p2, r2, v2, m2, T2 = workloads.config_2d(32, 1000, viscosity=True)
+    p3, r3, v3, m3, T3 = workloads.config_3d(12, 3000)
+    pg, rg, vg, mg, Tg = workloads.config_3d(10, 3001, kernel="lucy", h_short=1.4,
+                                             h_long=2.5)
+    return {"visc2d_1024": (p2, r2, v2, m2, T2), "cubic3d_heat_1728": (p3, r3, v3, m3, T3),
+            "lucy3d_heat_1000": (pg, rg, vg, mg, Tg)}
+
+
+@pytest.mark.parametrize("case", ["visc2d_1024", "cubic3d_heat_1728", "lucy3d_heat_1000"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_full_physics_vs_oracle(case, precision):
+    prm, r, v, m, T0 = full_physics_cases()[case]
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    ref = oracle.derivatives(prm, r, v, m, u)
+    e, s = one(prm, r, v, m, u, precision)
+    with e:
+        d = e.derivatives(s)
+        e.sync()
+        tol = EVAL_TOL if precision == "fp64" else MIXED_TOL
+        keys = KEYS + (("jq",) if prm.heat_flux else ())
+        errs = {k: rel_l2(d[k], ref[k]) for k in keys}
+        print(case, precision, errs)
+        for k, err in errs.items():
+            assert err < tol, (k, err)
+        assert e.pair_count(s) == ref["nip"]
+        e.advance(5)
+        e.sync()
+        rr, vv, uu = e.get_state(s)
+        r5, v5, u5, _ = oracle.advance(prm, r, v, m, u, 5)
+        stol = STEP_TOL if precision == "fp64" else MIXED_TOL
+        assert rel_l2(rr, r5) < stol
+        assert rel_l2(vv, v5) < stol
+        assert rel_l2(uu, u5) < stol
+
+
+def test_batched_results_equal_alone():
+    """Simulations of different sizes in one engine give bit-identical
+    results to the same simulations run alone (per-particle sums keep their
+    order whatever else is in the batch)."""
+    sims = workloads.batched_2d(4, seed_base=4100, n_lo=256, n_hi=4096, ramp_steps=20)
+    states = []
+    for prm, r, v, m, T0 in sims:
+        states.append((prm, r, v, m, oracle.initial_energy(prm, r, v, m, T0)))
+    total = sum(len(s[1]) for s in states)
+    with Engine(states[0][0], "mixed", max_particles=total, max_sims=4) as eb:
+        ids = [eb.add(*st) for st in states]
+        eb.advance(3)
+        eb.sync()
+        together = [eb.get_state(i) for i in ids]
+    for st, tog in zip(states, together):
+        e, s = one(*st, "mixed")
+        with e:
+            e.advance(3)
+            e.sync()
+            alone = e.get_state(s)
+        for a, b in zip(alone, tog):
+            assert np.array_equal(a, b)
+
+
+def test_simulations_join_and_leave():
+    sims = workloads.batched_2d(3, seed_base=4200, n_lo=256, n_hi=2048, ramp_steps=10)
+    st = [(p, r, v, m, oracle.initial_energy(p, r, v, m, T)) for p, r, v, m, T in sims]
+    total = sum(len(s[1]) for s in st)
+    with Engine(st[0][0], "mixed", max_particles=total, max_sims=3) as e:
+        a = e.add(*st[0])
+        b = e.add(*st[1])
+        e.advance(2)
+        e.remove(b)
+        c = e.add(*st[2])
+        e.advance(2)
+        e.sync()
+        ra = e.get_state(a)
+        rc = e.get_state(c)
+    e1, s1 = one(*st[0], "mixed")
+    with e1:
+        e1.advance(4)
+        e1.sync()
+        assert all(np.array_equal(x, y) for x, y in zip(e1.get_state(s1), ra))
+    e2, s2 = one(*st[2], "mixed")
+    with e2:
+        e2.advance(2)
+        e2.sync()
+        assert all(np.array_equal(x, y) for x, y in zip(e2.get_state(s2), rc))
+
+
+def test_large_pair_set_exact():
+    """N = 65,536 (2D) pair set identical to the oracle's; N = 262,144 pair
+    count identical."""
+    prm, r, v, m, T0 = workloads.config_2d(256, 2000)
+    u = np.zeros(len(r))
+    with Engine(prm, "mixed", max_particles=len(r)) as e:
+        s = e.add(prm, r, v, m, u)
+        out = e.pairs(s, with_geometry=True)
+        iap, rsq = oracle.pairs(prm, r)
+        assert np.array_equal(out["iap"], iap)
+        assert np.array_equal(out["rsq"], rsq)
+    prm, r, v, m, T0 = workloads.config_2d(512, 2001)
+    with Engine(prm, "mixed", max_particles=len(r)) as e:
+        s = e.add(prm, r, v, m, np.zeros(len(r)))
+        n_ref = len(oracle.pairs(prm, r)[0])
+        assert e.pair_count(s) == n_ref
+
+
+def test_full_size_invariants():
+    """N = 1,048,576 (2D): total acceleration cancels pairwise (m = 1),
+    steps are deterministic, the pair count is stable and no error flag."""
+    prm, r, v, m, T0 = workloads.config_2d(1024, 2002)
+    u = workloads.vdw_energy(np.full(len(r), 1.0), T0)
+    runs = []
+    for _ in range(2):
+        with Engine(prm, "mixed", max_particles=len(r)) as e:
+            s = e.add(prm, r, v, m, u)
+            d = e.derivatives(s)
+            net = np.abs(d["vdot"].sum(axis=0)) / np.abs(d["vdot"]).sum(axis=0)
+            assert np.all(net < 1e-6), net
+            e.advance(3)
+            e.sync()
+            runs.append(e.get_state(s))
+            assert e.last_pair_total() > 0
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
+
+
+def test_nan_in_host_input_is_flagged():
+    prm, r, v, m, T0 = workloads.config_2d(16, 5000)
+    u = workloads.vdw_energy(np.full(len(r), 1.0), T0)
+    u[7] = np.nan
+    with Engine(prm, "mixed", max_particles=len(r)) as e:
+        s = e.add(prm, r, v, m, u)
+        e.advance(1)
+        with pytest.raises(SphError) as ei:
+            e.sync()
+        assert ei.value.status == SPH_ENAN
+        assert e.status(s) == SPH_ENAN
+
+
+def test_skin_violation_is_flagged():
+    """A particle that moves further in one predictor stage than the cell
+    slack allows raises SPH_ESKIN instead of silently missing pairs."""
+    prm, r, v, m, T0 = workloads.config_2d(32, 5001)
+    u = workloads.vdw_energy(np.full(len(r), 1.0), T0)
+    with Engine(prm, "mixed", max_particles=len(r)) as e:
+        s = e.add(prm, r, v, m, u)
+        v2 = v.copy()
+        v2[3] = [900.0, 0.0]   # 0.9 per step against a slack of 0.2
+        e.set_state(s, r, v2, m, u)
+        e.advance(1)
+        with pytest.raises(SphError) as ei:
+            e.sync()
+        assert ei.value.status == SPH_ESKIN
