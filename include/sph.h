@@ -161,8 +161,9 @@ int sph_sim_diagnostics(sph_engine *e, int32_t sim_id, double out[6]);
 
 /* Tuning knobs of the pair passes (chosen by the autotuner). */
 typedef struct sph_tuning {
-    int32_t block_size;       /* threads per block of the pair passes        */
-    int32_t cells_per_warp;   /* reserved for the staged sweep; 0 = auto     */
+    int32_t block_size;       /* threads per block of the per-lane sweep     */
+    int32_t sweep;            /* 0: tiled warp sweep with compacted neighbour
+                                 lists (default); 1: per-lane cell loop      */
     double cell_ratio;        /* cell edge / pair cutoff lower bound (>=1)    */
     int32_t use_graph;        /* capture each advance chunk as a CUDA graph   */
     int32_t steps_per_graph;  /* steps unrolled into one graph                */

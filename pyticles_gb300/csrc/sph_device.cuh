@@ -23,7 +23,7 @@ __device__ __forceinline__ typename V4<R>::T make_v4(R x, R y, R z, R w) {
 // binning kernel and every pass that needs a particle's cell centre call
 // this same function so the results agree bit for bit.
 __device__ __forceinline__ int cell_coord(double x, const SimDev &S, int a, double *shift) {
-    double k = floor(x * (1.0 / S.L[a]));
+    double k = floor(x * S.inv_L[a]);
     double sh = k * S.L[a];
     double xw = x - sh;
     int ci = (int)(xw * S.inv_edge[a]);
@@ -54,6 +54,23 @@ __device__ __forceinline__ double exact_rsq(double *const xe[3], const SimDev &S
     return rsq;
 }
 
+// The exact test behind the rare guard-band branch.  Kept out of line: when
+// inlined, the compiler predicates it and every candidate then pays its
+// FP64 instructions, which on GB300's narrow FP64 pipe dominate the pass.
+template <int D>
+__device__ __noinline__ bool exact_in_set(double *const *xe, const SimDev *S, int i, int j) {
+    double rsq = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        double d = __dsub_rn(xe[a][j], xe[a][i]);
+        if (d > S->half_L[a]) d = __dsub_rn(d, S->L[a]);
+        if (d < -S->half_L[a]) d = __dadd_rn(d, S->L[a]);
+        double sq = __dmul_rn(d, d);
+        rsq = (a == 0) ? sq : __dadd_rn(rsq, sq);
+    }
+    return rsq < S->thr;
+}
+
 // Compensated (Kahan) accumulation for FP32 sums; FP64 sums are plain.
 template <typename R> struct Acc;
 template <> struct Acc<float> {
@@ -66,12 +83,15 @@ template <> struct Acc<float> {
         s = t;
     }
     __device__ __forceinline__ float get() const { return s; }
+    // the compensated value in FP64: s - c carries the bits s lost
+    __device__ __forceinline__ double get64() const { return (double)s - (double)c; }
 };
 template <> struct Acc<double> {
     double s;
     __device__ __forceinline__ void init(double x) { s = x; }
     __device__ __forceinline__ void add(double x) { s += x; }
     __device__ __forceinline__ double get() const { return s; }
+    __device__ __forceinline__ double get64() const { return s; }
 };
 
 // Fast-test bounds around the pair threshold.  In mixed mode the squared
@@ -86,7 +106,7 @@ template <> struct Margin<double> { static constexpr double rel = 1e-9; };
 // Lucy (spkernel.py:86-118), Gaussian (spkernel.py:39-52, Lucy's gradient
 // sign), Debrun (spkernel.py:120-153), M4 cubic spline (support 2h).
 template <typename R> struct KConst {
-    R h, inv_h, sig, g0;  // g0: Lucy -12 sig/h^2, Gaussian -2/h^2, cubic sig/h^2
+    R h, inv_h, inv_h_lo, sig, g0;  // g0: Lucy -12 sig/h^2, Gaussian -2/h^2, cubic sig/h^2
 };
 
 template <typename R>
@@ -94,9 +114,12 @@ __device__ __forceinline__ KConst<R> make_kconst(int K, double h, double sig) {
     KConst<R> k;
     k.h = (R)h;
     k.inv_h = (R)(1.0 / h);
+    // 1/h as a hi/lo pair: q = fma(r, hi, r*lo) is then unbiased to ~0.5 ulp
+    // instead of carrying the rounding of 1/h into every term alike
+    k.inv_h_lo = (R)(1.0 / h - (double)k.inv_h);
     k.sig = (R)sig;
     if (K == SPH_KERNEL_LUCY) k.g0 = (R)(-12.0 * sig / (h * h));
-    else if (K == SPH_KERNEL_GAUSSIAN) k.g0 = (R)(-2.0 / (h * h));
+    else if (K == SPH_KERNEL_GAUSSIAN) k.g0 = (R)(-2.0 / (h * h));  // times sig in kernel_wg
     else if (K == SPH_KERNEL_CUBIC) k.g0 = (R)(sig / (h * h));
     else k.g0 = (R)(-3.0 * sig);
     return k;
@@ -109,41 +132,51 @@ template <typename R> __device__ __forceinline__ R rsqrt_(R x);
 template <> __device__ __forceinline__ float rsqrt_<float>(float x) { return sqrtf(x); }
 template <> __device__ __forceinline__ double rsqrt_<double>(double x) { return sqrt(x); }
 
+template <typename R> __device__ __forceinline__ R qof(const KConst<R> &k, R r);
+template <> __device__ __forceinline__ float qof<float>(const KConst<float> &k, float r) {
+    return __fmaf_rn(r, k.inv_h, r * k.inv_h_lo);
+}
+template <> __device__ __forceinline__ double qof<double>(const KConst<double> &k, double r) {
+    return r * k.inv_h;
+}
+
+// *w receives W/sigma (the normalisation is applied once per particle in
+// FP64, which keeps its rounding out of every term); *g the full (dW/dr)/r.
 template <int K, typename R>
 __device__ __forceinline__ void kernel_wg(const KConst<R> &k, R r, R *w, R *g) {
     if (K == SPH_KERNEL_LUCY) {
-        R q = r * k.inv_h;
+        R q = qof<R>(k, r);
         if (q < (R)1) {
             R s = (R)1 - q;
             R s2 = s * s;
-            *w = k.sig * ((R)1 + (R)3 * q) * (s2 * s);
+            *w = ((R)1 + (R)3 * q) * (s2 * s);
             *g = k.g0 * s2;
         } else {
             *w = (R)0;
             *g = (R)0;
         }
     } else if (K == SPH_KERNEL_GAUSSIAN) {
-        R q = r * k.inv_h;
-        R e = k.sig * rexp<R>(-q * q);
+        R q = qof<R>(k, r);
+        R e = rexp<R>(-q * q);
         *w = e;
-        *g = k.g0 * e;
+        *g = k.g0 * k.sig * e;
     } else if (K == SPH_KERNEL_DEBRUN) {
         if (r < k.h) {
             R s = k.h - r;
-            *w = k.sig * s * s * s;
+            *w = s * s * s;
             *g = (r > (R)0) ? k.g0 * s * s / r : (R)0;
         } else {
             *w = (R)0;
             *g = (R)0;
         }
     } else {  // cubic spline
-        R q = r * k.inv_h;
+        R q = qof<R>(k, r);
         if (q < (R)1) {
-            *w = k.sig * ((R)1 - (R)1.5 * q * q + (R)0.75 * q * q * q);
+            *w = (R)1 - (R)1.5 * q * q + (R)0.75 * q * q * q;
             *g = k.g0 * ((R)-3 + (R)2.25 * q);
         } else if (q < (R)2) {
             R s = (R)2 - q;
-            *w = (R)0.25 * k.sig * s * s * s;
+            *w = (R)0.25 * s * s * s;
             *g = (R)-0.75 * k.sig * s * s * k.inv_h / r;
         } else {
             *w = (R)0;

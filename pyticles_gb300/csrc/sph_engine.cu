@@ -96,6 +96,8 @@ struct sph_engine {
     int *cell_of = nullptr, *rank = nullptr, *order_tmp = nullptr, *order = nullptr;
     int *cell_b = nullptr;
     int *cell_count = nullptr, *cell_start = nullptr, *nbr = nullptr, *morton = nullptr;
+    int *cell_xyz = nullptr;
+    double *org[3] = {};
     int *scan_tmp = nullptr;
     void *pk_pos[2] = {}, *pk_vel[2] = {}, *pk_f = nullptr, *pk_q = nullptr;
     double *xe[2][3] = {}, *ve[3] = {}, *ue = nullptr;
@@ -200,6 +202,7 @@ void make_grid(Sim &S, int dim, double ratio) {
         }
         int nc = (int)std::floor(S.prm.box[a] / need);
         if (nc < 3) nc = 1;
+        if (nc > (a < 2 ? 2047 : 1023)) nc = (a < 2 ? 2047 : 1023);  // packed cell coordinates
         S.nc[a] = nc;
         S.edge[a] = S.prm.box[a] / nc;
         S.ncells *= nc;
@@ -229,6 +232,7 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
     for (int a = 0; a < 3; ++a) {
         d.L[a] = p.box[a];
         d.half_L[a] = p.box[a] / 2.;
+        d.inv_L[a] = 1.0 / p.box[a];
         d.edge[a] = S.edge[a];
         d.inv_edge[a] = 1.0 / S.edge[a];
         d.nc[a] = S.nc[a];
@@ -258,6 +262,8 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
     d.c = p.sound_speed;
     d.kappa = p.thermalk;
     d.dt = p.dt;
+    d.hdt = 0.5 * p.dt;
+    d.inv_kb = 1.0 / p.kbdash;
     d.T0 = p.thermostat_temp;
     d.T1 = p.thermostat_temp_end;
     d.ramp = p.thermostat_ramp_steps;
@@ -285,6 +291,8 @@ int alloc_cells(sph_engine *e, int64_t cells) {
     TRY(dalloc(&e->cell_start, c + 1));
     TRY(dalloc(&e->nbr, c * e->nb));
     TRY(dalloc(&e->morton, c));
+    cudaFree(e->cell_xyz);
+    TRY(dalloc(&e->cell_xyz, c));
     TRY(dalloc(&e->scan_tmp, c / 4096 + 2));
     e->cap_c = c;
     free_graph(e);
@@ -325,6 +333,8 @@ View make_view(const sph_engine *e) {
     v.cell_b = e->cell_b;
     v.nbr = e->nbr;
     v.morton = e->morton;
+    v.cell_xyz = e->cell_xyz;
+    for (int a = 0; a < 3; ++a) v.org[a] = e->org[a];
     v.pk_f = e->pk_f;
     v.pk_q = e->pk_q;
     v.rho = e->rho;
@@ -386,6 +396,7 @@ int relayout(sph_engine *e) {
     e->ncells_total = cell_off;
     e->np_b = part_off;
     std::vector<int> mort(std::max(cell_off, 1)), nbr((size_t)std::max(cell_off, 1) * e->nb, -1);
+    std::vector<int> cxyz(std::max(cell_off, 1), 0);
     std::vector<int> csim, cstart, clen;
     for (auto &S : e->sims) {
         if (!S.active) continue;
@@ -393,6 +404,7 @@ int relayout(sph_engine *e) {
         for (int r = 0; r < S.ncells; ++r) {
             int lin = S.rank_lin[r];
             int c[3] = {lin % S.nc[0], (lin / S.nc[0]) % S.nc[1], lin / (S.nc[0] * S.nc[1])};
+            cxyz[S.cell_off + r] = c[0] | (c[1] << 11) | (c[2] << 22);
             for (int t = 0; t < e->nb; ++t) {
                 int o[3] = {t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1};
                 bool ok = true;
@@ -433,6 +445,8 @@ int relayout(sph_engine *e) {
         CK(cudaMemcpyAsync(e->morton, mort.data(), sizeof(int) * cell_off, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(e->nbr, nbr.data(), sizeof(int) * (size_t)cell_off * e->nb,
                            cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(e->cell_xyz, cxyz.data(), sizeof(int) * cell_off,
+                           cudaMemcpyHostToDevice, st));
     }
     if (e->nchunks > 0) {
         CK(cudaMemcpyAsync(e->chunk_sim, csim.data(), sizeof(int) * e->nchunks, cudaMemcpyHostToDevice, st));
@@ -461,11 +475,12 @@ struct ProfScope {
         if (!e->prof_on || e->prof_used + 2 > e->prof_pool.size()) return;
         cudaEvent_t a = e->prof_pool[e->prof_used++];
         b = e->prof_pool[e->prof_used++];
-        cudaEventRecord(a, st);
+        // external record nodes when captured, so the events are timeable
+        cudaEventRecordWithFlags(a, st, cudaEventRecordExternal);
         e->prof_recs.push_back({kind, a, b});
     }
     ~ProfScope() {
-        if (b) cudaEventRecord(b, st);
+        if (b) cudaEventRecordWithFlags(b, st, cudaEventRecordExternal);
     }
 };
 
@@ -493,11 +508,11 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
     int blk = e->tune.block_size;
     {
         ProfScope ps(e, SPH_PASS_DENSITY, st);
-        launch_density(v, e->precision, e->group.kernel, s, blk, st);
+        launch_density(v, e->precision, e->group.kernel, s, blk, e->tune.sweep, st);
     }
     if (e->group.heat_flux) {
         ProfScope ps(e, SPH_PASS_HEAT, st);
-        launch_heat(v, e->precision, e->group.kernel, blk, st);
+        launch_heat(v, e->precision, e->group.kernel, blk, e->tune.sweep, st);
     }
     if (mode == 1 && s == e->nstage - 1 && e->any_thermostat) {
         ProfScope ps(e, SPH_PASS_TSUM, st);
@@ -506,7 +521,7 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
     {
         ProfScope ps(e, SPH_PASS_FORCE, st);
         launch_force(v, e->precision, e->group.kernel, e->group.viscosity, e->group.heat_flux,
-                     e->group.integrator, s, mode, blk, st);
+                     e->group.integrator, s, mode, blk, e->tune.sweep, st);
     }
 }
 
@@ -641,6 +656,7 @@ int alloc_particles(sph_engine *e) {
         TRY(dalloc(&e->xe[0][a], P));
         TRY(dalloc(&e->xe[1][a], P));
         TRY(dalloc(&e->ve[a], P));
+        TRY(dalloc(&e->org[a], P));
         TRY(dalloc((char **)&e->q[a], P * e->rsize));
         TRY(dalloc((char **)&e->vdot[a], P * e->rsize));
         TRY(dalloc((char **)&e->f0v[a], P * e->rsize));
@@ -706,11 +722,11 @@ void free_all(sph_engine *e) {
                     e->temp, e->pres, e->pco, e->rho0, e->pres0, e->pco0, e->udot, e->f0u,
                     e->acc_u, e->stage_buf, e->sims_d, e->t_scale, e->tsum_part, e->steps_d,
                     e->pair_count, e->err, e->err_any, e->chunk_sim, e->chunk_start,
-                    e->chunk_len};
+                    e->chunk_len, e->cell_xyz};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int a = 0; a < 3; ++a) {
-        void *pa[] = {e->a_pos[a], e->a_vel[a], e->b_pos[a], e->b_vel[a], e->xe[0][a],
+        void *pa[] = {e->org[a], e->a_pos[a], e->a_vel[a], e->b_pos[a], e->b_vel[a], e->xe[0][a],
                       e->xe[1][a], e->ve[a], e->q[a], e->vdot[a], e->f0v[a], e->acc_r[a],
                       e->acc_v[a]};
         for (void *p : pa)
@@ -784,7 +800,7 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->cap_p = max_particles;
     e->cap_s = max_sims;
     e->tune.block_size = 128;
-    e->tune.cells_per_warp = 0;
+    e->tune.sweep = 0;
     e->tune.cell_ratio = 1.0;
     e->tune.use_graph = 1;
     e->tune.steps_per_graph = 1;
@@ -1027,7 +1043,7 @@ int sph_sim_pair_count(sph_engine *e, int32_t id, int64_t *nip) {
     enqueue_prepare(e, st);
     View v = make_view(e);
     stage_view(e, v, 0);
-    launch_density(v, e->precision, e->group.kernel, 0, e->tune.block_size, st);
+    launch_density(v, e->precision, e->group.kernel, 0, e->tune.block_size, e->tune.sweep, st);
     unsigned long long c = 0;
     CK(cudaMemcpyAsync(&c, e->pair_count + id, sizeof(c), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1156,7 +1172,8 @@ int sph_get_tuning(sph_engine *e, sph_tuning *t) {
 
 int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
     if (!e || !t) return SPH_EINVAL;
-    if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) || !(t->cell_ratio >= 1.0))
+    if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) || !(t->cell_ratio >= 1.0) ||
+        t->sweep < 0 || t->sweep > 1)
         return SPH_EINVAL;
     bool regrid = t->cell_ratio != e->tune.cell_ratio;
     e->tune = *t;

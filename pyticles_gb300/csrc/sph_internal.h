@@ -24,7 +24,7 @@ constexpr int kMaxNbr = 27;
 
 // Per-simulation constants on the device.
 struct SimDev {
-    double L[3], half_L[3];
+    double L[3], half_L[3], inv_L[3];
     double edge[3], inv_edge[3];
     double slack_half[3];   // max displacement per axis between binning and an evaluation
     int nc[3];
@@ -41,7 +41,8 @@ struct SimDev {
     double a, b, kb;        // van der Waals
     double alpha, beta, eps, c;   // Monaghan viscosity
     double kappa;           // conductivity
-    double dt;
+    double dt, hdt;         // time step and dt/2
+    double inv_kb;
     double T0, T1;          // thermostat ramp ends
     long long ramp;
 };
@@ -63,6 +64,8 @@ struct View {
     int *order_tmp, *order; // B slot -> A index
     int *cell_count, *cell_start, *cell_b;  // cell_b: B order cell id
     int *nbr, *morton;
+    int *cell_xyz;          // global cell -> packed cell coordinates (11/11/10 bits)
+    double *org[3];         // B order: FP64 origin of the particle's cell-local frame
     // evaluation (stage s reads *_in, its force pass writes stage s+1's *_out)
     void *pk_pos_in, *pk_vel_in;     // float4 / double4: {xl, yl, zl, m}, {vx, vy, vz, 0}
     void *pk_pos_out, *pk_vel_out;
@@ -106,11 +109,11 @@ void launch_iota_sim(int *id, int *sim, int sim_id, int n, cudaStream_t s);
 // ---- launch wrappers (sph_pairs.cu) ----
 // stage: evaluation index within the step; nstage: evaluations per step;
 // mode: 0 derivative only, 1 advance.
-void launch_density(const View &v, int precision, int kernel, int stage, int block,
+void launch_density(const View &v, int precision, int kernel, int stage, int block, int sweep,
                     cudaStream_t s);
-void launch_heat(const View &v, int precision, int kernel, int block, cudaStream_t s);
+void launch_heat(const View &v, int precision, int kernel, int block, int sweep, cudaStream_t s);
 void launch_force(const View &v, int precision, int kernel, int viscosity, int heat,
-                  int integrator, int stage, int mode, int block, cudaStream_t s);
+                  int integrator, int stage, int mode, int block, int sweep, cudaStream_t s);
 void launch_tsum(const View &v, int precision, int nsims, cudaStream_t s);
 void launch_pair_rows(const View &v, int precision, int sim_off, int n, long long *row_count,
                       cudaStream_t s);

@@ -23,6 +23,16 @@
 namespace sph {
 
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+// 1/x for the EOS: FP64 division in FP64 mode; in mixed mode an FP32
+// reciprocal refined by one FP64 Newton step (relative error ~1e-14), which
+// spares the narrow FP64 pipe a full division per particle.
+template <typename R> __device__ __forceinline__ double recip64(double x);
+template <> __device__ __forceinline__ double recip64<double>(double x) { return 1.0 / x; }
+template <> __device__ __forceinline__ double recip64<float>(double x) {
+    double r = (double)__frcp_rn((float)x);
+    return r * fma(-x, r, 2.0);
+}
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 
 template <typename R, int D>
@@ -87,9 +97,205 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
             R rsq = d[0] * d[0] + d[1] * d[1];
             if (D == 3) rsq += d[2] * d[2];
             if (rsq > fr.thr_hi) continue;
-            if (rsq >= fr.thr_lo && !(exact_rsq<D>(v.xe_in, S, i, j) < S.thr)) continue;
+            if (rsq >= fr.thr_lo && !exact_in_set<D>(v.xe_in, &S, i, j)) continue;
             body(j, pj, d, rsq);
         }
+    }
+}
+
+// ---- tiled sweep: warp-uniform candidate loops + per-lane compacted lists ----
+//
+// A warp holds 32 consecutive cell-sorted particles, usually from one or two
+// Morton-adjacent cells.  Looping every lane over its own 3^d neighbour
+// cells serialises the warp whenever its lanes sit in different cells, and
+// evaluating the pair body right after the distance test leaves most lanes
+// idle (about a third of the candidates are in range).  Here the warp
+// iterates the union box of its lanes' neighbourhoods with one shared loop
+// (every lane tests the same candidate j against its own particle), appends
+// the in-range neighbours to a per-lane list in shared memory as
+// (neighbour slot t, index within that cell), and evaluates the pair body
+// over the lists with all lanes busy.  Box cells are visited in raster order
+// (z, y, x), which for every lane is the raster order of its own 3^d
+// neighbourhood: each particle sums its pairs in the same order as the
+// per-lane loop, so results do not depend on which particles share a warp.
+constexpr int kTileWarps = 4;
+constexpr int kTileThreads = 32 * kTileWarps;
+template <int D> struct TileCap { static constexpr int value = D == 2 ? 128 : 96; };
+
+template <typename R, int D>
+struct TileShared {
+    unsigned short list[TileCap<D>::value][32];
+    int nstart[NbrCount<D>::value][32];     // per lane: start of its neighbour cell t
+    R shx[NbrCount<D>::value], shy[NbrCount<D>::value], shz[NbrCount<D>::value];
+    int box_start[64], box_len[64];
+};
+
+// Per-lane loop over its own neighbour cells (fallback for wide boxes).
+template <typename R, int D, typename T4, typename F>
+__device__ __forceinline__ void for_pairs_direct(const View &v, const SimDev &S,
+                                                 const PairFrame<R, D> &fr,
+                                                 const T4 *__restrict__ P, int i, const T4 &pi,
+                                                 F body) {
+    for_pairs<R, D>(v, S, fr, P, i, pi, body);
+}
+
+template <typename R, int D, typename T4, typename F>
+__device__ __forceinline__ void for_pairs_tiled(const View &v, const T4 *__restrict__ P, int i,
+                                                bool active, F body) {
+    constexpr int NB = NbrCount<D>::value;
+    constexpr int CAP = TileCap<D>::value;
+    __shared__ TileShared<R, D> tsh[kTileWarps];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    TileShared<R, D> &ts = tsh[threadIdx.x >> 5];
+    const int s_me = active ? v.b_sim[i] : -1;
+    unsigned todo = __ballot_sync(FULL, active);
+    while (todo) {
+        const int leader = __ffs(todo) - 1;
+        const int s_lead = __shfl_sync(FULL, s_me, leader);
+        const unsigned grp = __ballot_sync(FULL, active && s_me == s_lead);
+        todo &= ~grp;
+        const bool mine = (grp >> lane) & 1u;
+        const SimDev &S = v.sims[s_lead];
+        PairFrame<R, D> fr;
+        fr.init(S);
+        const T4 pi = P[mine ? i : v.np - 1];
+        // cell coordinates relative to the leader's cell, unwrapped
+        const int cp = v.cell_xyz[v.cell_b[mine ? i : v.np - 1]];
+        const int cref = __shfl_sync(FULL, cp, leader);
+        int dc[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, w[3] = {1, 1, 1}, cr[3];
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            const int sh = a == 0 ? 0 : (a == 1 ? 11 : 22);
+            const int mask = a == 2 ? 1023 : 2047;
+            cr[a] = (cref >> sh) & mask;
+            const int nc = S.nc[a];
+            if (nc >= 3) {
+                int d = ((cp >> sh) & mask) - cr[a];
+                if (2 * d >= nc) d -= nc;
+                if (2 * d < -nc) d += nc;
+                dc[a] = d;
+                const int mn = __reduce_min_sync(FULL, mine ? d : 0x7fffffff);
+                const int mx = __reduce_max_sync(FULL, mine ? d : -0x7fffffff);
+                lo[a] = mn - 1;
+                w[a] = mx - mn + 3;
+                if (w[a] > 4 || w[a] > nc) ok = false;
+            }
+        }
+        if (!ok) {
+            if (mine) for_pairs_direct<R, D>(v, S, fr, P, i, pi, body);
+            __syncwarp();
+            continue;
+        }
+        const int nbox = w[0] * w[1] * w[2];
+        // box table: start and length of every box cell (raster order, x fastest)
+        int maxlen = 0;
+        for (int b = lane; b < nbox; b += 32) {
+            int o[3] = {b % w[0], (b / w[0]) % w[1], b / (w[0] * w[1])};
+            int lin = 0, mul = 1;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                int x = cr[a] + lo[a] + o[a];
+                const int nc = S.nc[a];
+                if (x < 0) x += nc;
+                if (x >= nc) x -= nc;
+                lin += x * mul;
+                mul *= nc;
+            }
+            const int gc = S.cell_off + v.morton[S.cell_off + lin];
+            const int st = v.cell_start[gc];
+            ts.box_start[b] = st;
+            ts.box_len[b] = v.cell_start[gc + 1] - st;
+            maxlen = max(maxlen, ts.box_len[b]);
+        }
+        if (__reduce_max_sync(FULL, maxlen) > 2047) {
+            // index within a cell does not fit the 11-bit list code
+            __syncwarp();
+            if (mine) for_pairs_direct<R, D>(v, S, fr, P, i, pi, body);
+            __syncwarp();
+            continue;
+        }
+        if (lane < NB) {
+            R sh[3];
+            fr.shift(lane, sh);
+            ts.shx[lane] = sh[0];
+            ts.shy[lane] = sh[1];
+            ts.shz[lane] = sh[2];
+        }
+        __syncwarp();
+        int cnt = 0;
+        auto flush = [&]() {
+            const int mc = __reduce_max_sync(FULL, cnt);
+            for (int e = 0; e < mc; ++e) {
+                if (e < cnt) {
+                    const unsigned code = ts.list[e][lane];
+                    const int t = code >> 11;
+                    const int j = ts.nstart[t][lane] + (int)(code & 2047u);
+                    const T4 pj = P[j];
+                    R d[3];
+                    d[0] = pj.x + (ts.shx[t] - pi.x);
+                    d[1] = pj.y + (ts.shy[t] - pi.y);
+                    d[2] = (D == 3) ? pj.z + (ts.shz[t] - pi.z) : (R)0;
+                    fr.min_image(d);
+                    R rsq = d[0] * d[0] + d[1] * d[1];
+                    if (D == 3) rsq += d[2] * d[2];
+                    body(j, pj, d, rsq);
+                }
+            }
+            cnt = 0;
+        };
+        for (int b = 0; b < nbox; ++b) {
+            const int st = ts.box_start[b], len = ts.box_len[b];
+            if (len == 0) continue;
+            // this box cell relative to the lane's own cell
+            int t = 0, mul = 1;
+            bool nbh = mine;
+            int o[3] = {b % w[0], (b / w[0]) % w[1], b / (w[0] * w[1])};
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                const int rel = lo[a] + o[a] - dc[a];
+                nbh = nbh && rel >= -1 && rel <= 1;
+                t += (rel + 1) * mul;
+                mul *= 3;
+            }
+            if (nbh) ts.nstart[t][lane] = st;
+            const R ox = nbh ? ts.shx[t] - pi.x : (R)0;
+            const R oy = nbh ? ts.shy[t] - pi.y : (R)0;
+            const R oz = (nbh && D == 3) ? ts.shz[t] - pi.z : (R)0;
+            // chunks that fit the lists; flush when the fullest list is full
+            for (int k0 = 0; k0 < len;) {
+                int room = CAP - __reduce_max_sync(FULL, cnt);
+                if (room == 0) {
+                    __syncwarp();
+                    flush();
+                    room = CAP;
+                }
+                const int k1 = min(len, k0 + room);
+                for (int k = k0; k < k1; ++k) {
+                    const int j = st + k;
+                    const T4 pj = P[j];
+                    if (nbh && j != i) {
+                        R d[3];
+                        d[0] = pj.x + ox;
+                        d[1] = pj.y + oy;
+                        d[2] = (D == 3) ? pj.z + oz : (R)0;
+                        fr.min_image(d);
+                        R rsq = d[0] * d[0] + d[1] * d[1];
+                        if (D == 3) rsq += d[2] * d[2];
+                        if (rsq <= fr.thr_hi &&
+                            (rsq < fr.thr_lo || exact_in_set<D>(v.xe_in, &S, i, j))) {
+                            ts.list[cnt][lane] = (unsigned short)((t << 11) | k);
+                            ++cnt;
+                        }
+                    }
+                }
+                k0 = k1;
+            }
+        }
+        __syncwarp();
+        flush();
+        __syncwarp();
     }
 }
 
@@ -108,24 +314,22 @@ __device__ __forceinline__ void add_pair_count(unsigned long long *cnt, int s, u
     if ((threadIdx.x & 31) == leader) atomicAdd(&cnt[s], tot);
 }
 
-template <typename R, int D, int K>
-__global__ void __launch_bounds__(256) k_density(View v, int stage) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.np) return;
+template <typename R, int D, int K, bool TILED>
+__global__ void __launch_bounds__(kTileThreads) k_density(View v, int stage) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < v.np;
+    const int ii = active ? i : v.np - 1;
     using T4 = typename V4<R>::T;
     const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
-    int s = v.b_sim[i];
+    const int s = v.b_sim[ii];
     const SimDev &S = v.sims[s];
-    PairFrame<R, D> fr;
-    fr.init(S);
     KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
     KConst<R> kl = make_kconst<R>(K, S.hl, S.sig_l);
-    T4 pi = P[i];
     Acc<R> rs, rl;
-    rs.init((R)S.ws0);
-    rl.init((R)S.wl0);
+    rs.init((R)0);
+    rl.init((R)0);
     unsigned cnt = 0;
-    for_pairs<R, D>(v, S, fr, P, i, pi, [&](int j, const T4 &pj, const R *d, R rsq) {
+    auto body = [&](int j, const T4 &pj, const R *d, R rsq) {
         R r = rsqrt_<R>(rsq);
         R w, g;
         kernel_wg<K, R>(ks, r, &w, &g);
@@ -133,59 +337,84 @@ __global__ void __launch_bounds__(256) k_density(View v, int stage) {
         kernel_wg<K, R>(kl, r, &w, &g);
         rl.add(pj.w * w);
         ++cnt;
-    });
-    R rho = rs.get(), rhol = rl.get();
-    double T = (v.ue_in[i] + S.a * (double)rho) / S.kb;
-    if (T < 0.0) T = 0.0;
-    R Tr = (R)T;
-    R p = (rho * (R)S.kb * Tr) / ((R)1 - rho * (R)S.b);
-    R pco = -(R)S.a * rhol * rhol;
-    ((R *)v.rho)[i] = rho;
-    ((R *)v.rho_l)[i] = rhol;
-    ((R *)v.temp)[i] = Tr;
-    ((R *)v.pres)[i] = p;
-    ((R *)v.pco)[i] = pco;
-    if (stage == 0) {
-        ((R *)v.rho0)[i] = rho;
-        ((R *)v.pres0)[i] = p;
-        ((R *)v.pco0)[i] = pco;
+    };
+    if (TILED) {
+        for_pairs_tiled<R, D>(v, P, i, active, body);
+    } else if (active) {
+        PairFrame<R, D> fr;
+        fr.init(S);
+        for_pairs<R, D>(v, S, fr, P, i, P[i], body);
     }
-    ((T4 *)v.pk_f)[i] = make_v4<R>(p / (rho * rho), pco / (rhol * rhol), rho, Tr);
-    if (!isfinite((double)p) || !isfinite((double)rho) || !isfinite((double)pco))
+    if (!active) return;
+    // EOS in FP64 from the compensated sums plus the FP64 self term
+    // (properties.py:77-78): the temperature T = (u + a rho)/k_B cancels
+    // strongly, so rho enters it with the bits the FP32 sum carried in its
+    // compensation.  p/rho^2 = k_B T / (rho (1 - b rho)); the cohesive factor
+    // pco/rho_l^2 is exactly -a and needs no storage.
+    double rho = S.ws0 + S.sig_s * rs.get64();
+    double rhol = S.wl0 + S.sig_l * rl.get64();
+    double T = (v.ue_in[i] + S.a * rho) * S.inv_kb;
+    if (T < 0.0) T = 0.0;
+    double den = rho * (1.0 - S.b * rho);
+    double fs = S.kb * T * recip64<R>(den);
+    double p = fs * rho * rho;
+    double pco = -S.a * rhol * rhol;
+    R Th = (R)T;
+    ((R *)v.rho)[i] = (R)rho;
+    ((R *)v.rho_l)[i] = (R)rhol;
+    ((R *)v.temp)[i] = Th;
+    ((R *)v.pres)[i] = (R)p;
+    ((R *)v.pco)[i] = (R)pco;
+    if (stage == 0) {
+        ((R *)v.rho0)[i] = (R)rho;
+        ((R *)v.pres0)[i] = (R)p;
+        ((R *)v.pco0)[i] = (R)pco;
+    }
+    // {p/rho^2, rho, T_hi, T_lo}: T as a hi/lo pair so that T_j - T_i in the
+    // heat pass does not lose the low bits
+    ((T4 *)v.pk_f)[i] = make_v4<R>((R)fs, (R)rho, Th, (R)(T - (double)Th));
+    if (!isfinite((R)p) || !isfinite((R)rho) || !isfinite((R)rhol))
         set_err(v.err, v.err_any, s, SPH_ENAN);
     add_pair_count(v.pair_count, s, cnt);
 }
 
-template <typename R, int D, int K>
-__global__ void __launch_bounds__(256) k_heat(View v) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.np) return;
+template <typename R, int D, int K, bool TILED>
+__global__ void __launch_bounds__(kTileThreads) k_heat(View v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < v.np;
+    const int ii = active ? i : v.np - 1;
     using T4 = typename V4<R>::T;
     const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
     const T4 *__restrict__ F = (const T4 *)v.pk_f;
-    int s = v.b_sim[i];
+    const int s = v.b_sim[ii];
     const SimDev &S = v.sims[s];
-    PairFrame<R, D> fr;
-    fr.init(S);
     KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
-    T4 pi = P[i];
-    T4 fi = F[i];
+    const T4 fi = F[ii];
     Acc<R> q[3];
     q[0].init(0);
     q[1].init(0);
     q[2].init(0);
-    for_pairs<R, D>(v, S, fr, P, i, pi, [&](int j, const T4 &pj, const R *d, R rsq) {
+    auto body = [&](int j, const T4 &pj, const R *d, R rsq) {
         R r = rsqrt_<R>(rsq);
         R g = kernel_g<K, R>(ks, r);
         T4 fj = F[j];
-        R f = (pj.w / fj.z) * (fj.w - fi.w) * g;
+        R dT = (fj.z - fi.z) + (fj.w - fi.w);
+        R f = (pj.w / fj.y) * dT * g;
         q[0].add(f * d[0]);
         q[1].add(f * d[1]);
         if (D == 3) q[2].add(f * d[2]);
-    });
+    };
+    if (TILED) {
+        for_pairs_tiled<R, D>(v, P, i, active, body);
+    } else if (active) {
+        PairFrame<R, D> fr;
+        fr.init(S);
+        for_pairs<R, D>(v, S, fr, P, i, P[i], body);
+    }
+    if (!active) return;
     R kap = (R)S.kappa;
     R qq[3] = {kap * q[0].get(), kap * q[1].get(), kap * q[2].get()};
-    R ir2 = (R)1 / (fi.z * fi.z);
+    R ir2 = (R)1 / (fi.y * fi.y);
     for (int a = 0; a < D; ++a) ((R *)v.q[a])[i] = qq[a];
     ((T4 *)v.pk_q)[i] = make_v4<R>(qq[0] * ir2, qq[1] * ir2, qq[2] * ir2, (R)0);
 }
@@ -198,17 +427,16 @@ __device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S,
                                                  double m) {
     using T4 = typename V4<R>::T;
     R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
+    bool skin = false;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-        double sh;
-        int ci = cell_coord(v.b_pos[a][i], S, a, &sh);
-        xl[a] = (R)((x[a] - sh) - cell_centre(ci, S, a));
+        xl[a] = (R)(x[a] - v.org[a][i]);
         vv[a] = (R)vel[a];
         v.xe_out[a][i] = x[a];
         v.ve_out[a][i] = vel[a];
-        double disp = fabs(x[a] - v.b_pos[a][i]);
-        if (disp > S.slack_half[a]) set_err(v.err, v.err_any, v.b_sim[i], SPH_ESKIN);
+        skin |= fabs(x[a] - v.b_pos[a][i]) > S.slack_half[a];
     }
+    if (skin) set_err(v.err, v.err_any, v.b_sim[i], SPH_ESKIN);
     v.ue_out[i] = u;
     ((T4 *)v.pk_pos_out)[i] = make_v4<R>(xl[0], xl[1], xl[2], (R)m);
     ((T4 *)v.pk_vel_out)[i] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
@@ -232,32 +460,32 @@ __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S
     v.a_sim[i] = v.b_sim[i];
 }
 
-template <typename R, int D, int K>
-__global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int integ, int visc,
-                                               int heat) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.np) return;
+template <typename R, int D, int K, bool TILED>
+__global__ void __launch_bounds__(kTileThreads) k_force(View v, int stage, int mode, int integ,
+                                                        int visc, int heat) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < v.np;
+    const int ii = active ? i : v.np - 1;
     using T4 = typename V4<R>::T;
     const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
     const T4 *__restrict__ V = (const T4 *)v.pk_vel_in;
     const T4 *__restrict__ F = (const T4 *)v.pk_f;
     const T4 *__restrict__ Q = (const T4 *)v.pk_q;
-    int s = v.b_sim[i];
+    const int s = v.b_sim[ii];
     const SimDev &S = v.sims[s];
-    PairFrame<R, D> fr;
-    fr.init(S);
     KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
     KConst<R> kl = make_kconst<R>(K, S.hl, S.sig_l);
     const R hs = (R)S.hs, eps_h2 = (R)(S.eps * S.hs * S.hs);
     const R alpha_c = (R)(S.alpha * S.c), beta = (R)S.beta;
-    T4 pi = P[i], vi = V[i], fi = F[i];
-    T4 qi = heat ? Q[i] : make_v4<R>(0, 0, 0, 0);
+    const R pl2 = (R)(-2.0 * S.a);  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
+    const T4 vi = V[ii], fi = F[ii];
+    const T4 qi = heat ? Q[ii] : make_v4<R>(0, 0, 0, 0);
     Acc<R> ax[3], ud;
     ax[0].init(0);
     ax[1].init(0);
     ax[2].init(0);
     ud.init(0);
-    for_pairs<R, D>(v, S, fr, P, i, pi, [&](int j, const T4 &pj, const R *d, R rsq) {
+    auto body = [&](int j, const T4 &pj, const R *d, R rsq) {
         R r = rsqrt_<R>(rsq);
         R gs = kernel_g<K, R>(ks, r);
         R gl = kernel_g<K, R>(kl, r);
@@ -267,10 +495,9 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
         R ps = fi.x + fj.x;
         if (visc && dvdx < (R)0) {
             R mu = hs * dvdx / (rsq + eps_h2);
-            ps += (-alpha_c * mu + beta * mu * mu) / ((R)0.5 * (fi.z + fj.z));
+            ps += (-alpha_c * mu + beta * mu * mu) / ((R)0.5 * (fi.y + fj.y));
         }
-        R pl = fi.y + fj.y;
-        R gsum = ps * gs + pl * gl;
+        R gsum = ps * gs + pl2 * gl;
         ax[0].add(gsum * d[0]);
         ax[1].add(gsum * d[1]);
         if (D == 3) ax[2].add(gsum * d[2]);
@@ -282,12 +509,20 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
             du -= dq * gs * pj.w;
         }
         ud.add(du);
-    });
+    };
+    if (TILED) {
+        for_pairs_tiled<R, D>(v, P, i, active, body);
+    } else if (active) {
+        PairFrame<R, D> fr;
+        fr.init(S);
+        for_pairs<R, D>(v, S, fr, P, i, P[i], body);
+    }
+    if (!active) return;
     R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
     R udr = ud.get();
     for (int a = 0; a < D; ++a) ((R *)v.vdot[a])[i] = vdr[a];
     ((R *)v.udot)[i] = udr;
-    if (!isfinite((double)vdr[0]) || !isfinite((double)udr)) set_err(v.err, v.err_any, s, SPH_ENAN);
+    if (!isfinite(vdr[0]) || !isfinite(udr)) set_err(v.err, v.err_any, s, SPH_ENAN);
     if (mode == 0) return;
 
     // ---- integrator stage (c = xdot * dt as in integrator.py) ----
@@ -303,32 +538,33 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
     double u0 = v.b_u[i], udd = (double)udr, m = v.b_m[i];
     double x[3] = {0, 0, 0}, vel[3] = {0, 0, 0}, u;
     bool final_stage = false;
+    // Euler and improved Euler in FMA form: x0 + dt f and x0 + dt/2 (f0 + f1)
+    // (integrator.py:14-59 round c = f dt and (c1 + c2)/2 separately; the
+    // difference is one rounding per step, far below the FP64 tolerance)
     if (integ == SPH_EULER) {
         for (int a = 0; a < D; ++a) {
-            x[a] = dadd(x0[a], dmul(rd[a], dt));
-            vel[a] = dadd(v0[a], dmul(vd[a], dt));
+            x[a] = fma(dt, rd[a], x0[a]);
+            vel[a] = fma(dt, vd[a], v0[a]);
         }
-        u = dadd(u0, dmul(udd, dt));
+        u = fma(dt, udd, u0);
         final_stage = true;
     } else if (integ == SPH_IEULER) {
         if (stage == 0) {
             for (int a = 0; a < D; ++a) {
                 ((R *)v.f0v[a])[i] = vdr[a];
-                x[a] = dadd(x0[a], dmul(rd[a], dt));
-                vel[a] = dadd(v0[a], dmul(vd[a], dt));
+                x[a] = fma(dt, rd[a], x0[a]);
+                vel[a] = fma(dt, vd[a], v0[a]);
             }
             ((R *)v.f0u)[i] = udr;
-            u = dadd(u0, dmul(udd, dt));
+            u = fma(dt, udd, u0);
             write_eval_state<R, D>(v, S, i, x, vel, u, m);
         } else {
+            const double hdt = S.hdt;
             for (int a = 0; a < D; ++a) {
-                double c1r = dmul(v0[a], dt), c2r = dmul(rd[a], dt);
-                x[a] = dadd(x0[a], dmul(dadd(c1r, c2r), 0.5));
-                double c1v = dmul((double)((const R *)v.f0v[a])[i], dt), c2v = dmul(vd[a], dt);
-                vel[a] = dadd(v0[a], dmul(dadd(c1v, c2v), 0.5));
+                x[a] = fma(hdt, v0[a] + rd[a], x0[a]);
+                vel[a] = fma(hdt, (double)((const R *)v.f0v[a])[i] + vd[a], v0[a]);
             }
-            double c1u = dmul((double)((const R *)v.f0u)[i], dt), c2u = dmul(udd, dt);
-            u = dadd(u0, dmul(dadd(c1u, c2u), 0.5));
+            u = fma(hdt, (double)((const R *)v.f0u)[i] + udd, u0);
             final_stage = true;
         }
     } else {  // RK4
@@ -399,27 +635,49 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
         default: { constexpr int K = SPH_KERNEL_CUBIC; CALL; break; }                     \
     }
 
-void launch_density(const View &v, int precision, int kernel, int stage, int block,
+// sweep: 0 tiled warp sweep (block of kTileThreads), 1 per-lane loop (block
+// of `block` threads).
+void launch_density(const View &v, int precision, int kernel, int stage, int block, int sweep,
                     cudaStream_t s) {
     if (v.np <= 0) return;
-    int nb = (v.np + block - 1) / block;
-    SPH_DISPATCH(precision, v.dim, kernel,
-                 (k_density<R, D, K><<<nb, block, 0, s>>>(v, stage)));
+    if (sweep == 0) {
+        int nb = (v.np + kTileThreads - 1) / kTileThreads;
+        SPH_DISPATCH(precision, v.dim, kernel,
+                     (k_density<R, D, K, true><<<nb, kTileThreads, 0, s>>>(v, stage)));
+    } else {
+        int nb = (v.np + block - 1) / block;
+        SPH_DISPATCH(precision, v.dim, kernel,
+                     (k_density<R, D, K, false><<<nb, block, 0, s>>>(v, stage)));
+    }
 }
 
-void launch_heat(const View &v, int precision, int kernel, int block, cudaStream_t s) {
+void launch_heat(const View &v, int precision, int kernel, int block, int sweep,
+                 cudaStream_t s) {
     if (v.np <= 0) return;
-    int nb = (v.np + block - 1) / block;
-    SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K><<<nb, block, 0, s>>>(v)));
+    if (sweep == 0) {
+        int nb = (v.np + kTileThreads - 1) / kTileThreads;
+        SPH_DISPATCH(precision, v.dim, kernel,
+                     (k_heat<R, D, K, true><<<nb, kTileThreads, 0, s>>>(v)));
+    } else {
+        int nb = (v.np + block - 1) / block;
+        SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K, false><<<nb, block, 0, s>>>(v)));
+    }
 }
 
 void launch_force(const View &v, int precision, int kernel, int viscosity, int heat,
-                  int integrator, int stage, int mode, int block, cudaStream_t s) {
+                  int integrator, int stage, int mode, int block, int sweep, cudaStream_t s) {
     if (v.np <= 0) return;
-    int nb = (v.np + block - 1) / block;
-    SPH_DISPATCH(precision, v.dim, kernel,
-                 (k_force<R, D, K><<<nb, block, 0, s>>>(v, stage, mode, integrator, viscosity,
-                                                       heat)));
+    if (sweep == 0) {
+        int nb = (v.np + kTileThreads - 1) / kTileThreads;
+        SPH_DISPATCH(precision, v.dim, kernel,
+                     (k_force<R, D, K, true><<<nb, kTileThreads, 0, s>>>(
+                         v, stage, mode, integrator, viscosity, heat)));
+    } else {
+        int nb = (v.np + block - 1) / block;
+        SPH_DISPATCH(precision, v.dim, kernel,
+                     (k_force<R, D, K, false><<<nb, block, 0, s>>>(v, stage, mode, integrator,
+                                                                  viscosity, heat)));
+    }
 }
 
 // ---- thermostat: per-chunk FP64 partial sums of T, then one thread per

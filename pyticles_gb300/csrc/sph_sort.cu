@@ -181,7 +181,9 @@ __global__ void k_permute(View v) {
         v.b_vel[a][j] = vel;
         double sh;
         int ci = cell_coord(x, S, a, &sh);
-        xl[a] = (R)((x - sh) - cell_centre(ci, S, a));
+        double org = sh + cell_centre(ci, S, a);
+        v.org[a][j] = org;
+        xl[a] = (R)(x - org);
         vv[a] = (R)vel;
     }
     double m = v.a_m[k];
