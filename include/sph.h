@@ -159,14 +159,16 @@ int sph_last_pair_total(sph_engine *e, int64_t *pairs);
  * out[5] mean temperature of the last evaluation. */
 int sph_sim_diagnostics(sph_engine *e, int32_t sim_id, double out[6]);
 
-/* Tuning knobs of the pair passes (chosen by the autotuner). */
+/* Tuning knobs (chosen by the autotuner, pyticles_gb300/autotune.py). */
 typedef struct sph_tuning {
-    int32_t block_size;       /* threads per block of the per-lane sweep     */
-    int32_t sweep;            /* 0: tiled warp sweep with compacted neighbour
-                                 lists (default); 1: per-lane cell loop      */
-    double cell_ratio;        /* cell edge / pair cutoff lower bound (>=1)    */
-    int32_t use_graph;        /* capture each advance chunk as a CUDA graph   */
-    int32_t steps_per_graph;  /* steps unrolled into one graph                */
+    int32_t block_size;       /* threads per block of the pair passes          */
+    int32_t use_graph;        /* capture each advance chunk as a CUDA graph     */
+    int32_t steps_per_graph;  /* steps unrolled into one graph                  */
+    int32_t reserved;         /* must be 0                                      */
+    double cell_ratio;        /* cell edge / (cutoff + skin): 1 -> cells of the
+                                 cutoff and a 3^d window, 1/2 -> half-size cells
+                                 and a 5^d window, 1/3 -> 7^d; cells beyond the
+                                 cutoff from a particle are skipped            */
 } sph_tuning;
 int sph_get_tuning(sph_engine *e, sph_tuning *t);
 int sph_set_tuning(sph_engine *e, const sph_tuning *t);

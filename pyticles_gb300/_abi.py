@@ -72,10 +72,10 @@ class SphTuning(ctypes.Structure):
     """struct sph_tuning (include/sph.h)."""
     _fields_ = [
         ("block_size", ctypes.c_int32),
-        ("sweep", ctypes.c_int32),
-        ("cell_ratio", ctypes.c_double),
         ("use_graph", ctypes.c_int32),
         ("steps_per_graph", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("cell_ratio", ctypes.c_double),
     ]
 
 

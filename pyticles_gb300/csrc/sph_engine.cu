@@ -42,6 +42,7 @@ struct Sim {
     int64_t n = 0;
     bool active = false;
     int nc[3] = {1, 1, 1};
+    int win[3] = {0, 0, 0};
     double edge[3] = {1, 1, 1};
     int ncells = 0;
     std::vector<int> morton;   // linear cell -> Morton rank
@@ -95,7 +96,7 @@ struct sph_engine {
     int *b_id = nullptr, *b_sim = nullptr;
     int *cell_of = nullptr, *rank = nullptr, *order_tmp = nullptr, *order = nullptr;
     int *cell_b = nullptr;
-    int *cell_count = nullptr, *cell_start = nullptr, *nbr = nullptr, *morton = nullptr;
+    int *cell_count = nullptr, *cell_start = nullptr, *morton = nullptr;
     int *cell_xyz = nullptr;
     double *org[3] = {};
     int *scan_tmp = nullptr;
@@ -186,23 +187,33 @@ int validate_params(const sph_engine *e, const sph_params *p) {
     return SPH_OK;
 }
 
-// Cell grid of one simulation: edge >= cutoff * ratio plus room for the
-// largest displacement of one step (8 dt vmax), at least 3 cells per axis or
-// else a single cell on that axis (the pass then applies the minimum image).
+// Cell grid of one simulation.  reach = cutoff + 8 dt vmax: the cutoff plus
+// room for the largest displacement between binning and an evaluation of
+// the step (checked on the device, SPH_ESKIN).  With ratio r < 1 the cells
+// are reach/W wide (W = round(1/r)) and the pair passes scan +-W cells per
+// axis, culling cells beyond the cutoff; r >= 1 gives cells of r * reach
+// and W = 1.  An axis with fewer than 2W+1 cells becomes a single cell
+// (the passes then apply the minimum image on it).
 void make_grid(Sim &S, int dim, double ratio) {
     double rc = std::sqrt(S.prm.cutoff * S.prm.cutoff + S.prm.tolerance * S.prm.tolerance);
-    double need = rc * std::max(1.0, ratio) + 8.0 * S.prm.dt * S.vmax;
-    need *= (1.0 + 1e-9);
+    double reach = rc + 8.0 * S.prm.dt * S.vmax;
+    int W = ratio < 1.0 ? std::max(1, (int)std::lround(1.0 / ratio)) : 1;
+    double need = (ratio < 1.0 ? reach / W : reach * ratio) * (1.0 + 1e-9);
     S.ncells = 1;
     for (int a = 0; a < 3; ++a) {
+        S.win[a] = 0;
         if (a >= dim) {
             S.nc[a] = 1;
             S.edge[a] = 1.0;
             continue;
         }
         int nc = (int)std::floor(S.prm.box[a] / need);
-        if (nc < 3) nc = 1;
-        if (nc > (a < 2 ? 2047 : 1023)) nc = (a < 2 ? 2047 : 1023);  // packed cell coordinates
+        if (nc < 2 * W + 1) {
+            nc = 1;
+        } else {
+            if (nc > (a < 2 ? 2047 : 1023)) nc = (a < 2 ? 2047 : 1023);  // packed coordinates
+            S.win[a] = W;
+        }
         S.nc[a] = nc;
         S.edge[a] = S.prm.box[a] / nc;
         S.ncells *= nc;
@@ -236,7 +247,8 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
         d.edge[a] = S.edge[a];
         d.inv_edge[a] = 1.0 / S.edge[a];
         d.nc[a] = S.nc[a];
-        d.slack_half[a] = (a < e->dim) ? (S.nc[a] >= 3 ? 0.5 * (S.edge[a] - rc) : 1e300) : 1e300;
+        d.win[a] = S.win[a];
+        d.slack_half[a] = (a < e->dim && S.win[a] > 0) ? 0.5 * (S.win[a] * S.edge[a] - rc) : 1e300;
         if (a < e->dim && S.nc[a] == 1) d.small_mask |= (1 << a);
     }
     d.active = S.active ? 1 : 0;
@@ -244,7 +256,6 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
     d.ncells = S.ncells;
     d.part_off = S.part_off;
     d.n = (int)S.n;
-    d.nbr_count = e->nb;
     d.thermostat = p.thermostat;
     d.thr = p.cutoff * p.cutoff + p.tolerance * p.tolerance;
     d.hs = p.h_short;
@@ -283,13 +294,11 @@ int alloc_cells(sph_engine *e, int64_t cells) {
     int64_t c = std::max<int64_t>(cells, e->cap_c * 2);
     cudaFree(e->cell_count);
     cudaFree(e->cell_start);
-    cudaFree(e->nbr);
     cudaFree(e->morton);
     cudaFree(e->scan_tmp);
     e->cap_c = 0;
     TRY(dalloc(&e->cell_count, c));
     TRY(dalloc(&e->cell_start, c + 1));
-    TRY(dalloc(&e->nbr, c * e->nb));
     TRY(dalloc(&e->morton, c));
     cudaFree(e->cell_xyz);
     TRY(dalloc(&e->cell_xyz, c));
@@ -331,7 +340,6 @@ View make_view(const sph_engine *e) {
     v.cell_count = e->cell_count;
     v.cell_start = e->cell_start;
     v.cell_b = e->cell_b;
-    v.nbr = e->nbr;
     v.morton = e->morton;
     v.cell_xyz = e->cell_xyz;
     for (int a = 0; a < 3; ++a) v.org[a] = e->org[a];
@@ -395,7 +403,7 @@ int relayout(sph_engine *e) {
     TRY(alloc_cells(e, std::max(cell_off, 1)));
     e->ncells_total = cell_off;
     e->np_b = part_off;
-    std::vector<int> mort(std::max(cell_off, 1)), nbr((size_t)std::max(cell_off, 1) * e->nb, -1);
+    std::vector<int> mort(std::max(cell_off, 1));
     std::vector<int> cxyz(std::max(cell_off, 1), 0);
     std::vector<int> csim, cstart, clen;
     for (auto &S : e->sims) {
@@ -405,21 +413,6 @@ int relayout(sph_engine *e) {
             int lin = S.rank_lin[r];
             int c[3] = {lin % S.nc[0], (lin / S.nc[0]) % S.nc[1], lin / (S.nc[0] * S.nc[1])};
             cxyz[S.cell_off + r] = c[0] | (c[1] << 11) | (c[2] << 22);
-            for (int t = 0; t < e->nb; ++t) {
-                int o[3] = {t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1};
-                bool ok = true;
-                int l2 = 0, mul = 1;
-                for (int a = 0; a < e->dim; ++a) {
-                    if (S.nc[a] < 3 && o[a] != 0) {
-                        ok = false;
-                        break;
-                    }
-                    int x = (c[a] + o[a] + S.nc[a]) % S.nc[a];
-                    l2 += x * mul;
-                    mul *= S.nc[a];
-                }
-                nbr[(size_t)(S.cell_off + r) * e->nb + t] = ok ? S.cell_off + S.morton[l2] : -1;
-            }
         }
         for (int64_t b = 0; b < S.n; b += 1024) {
             csim.push_back((int)(&S - &e->sims[0]));
@@ -443,8 +436,6 @@ int relayout(sph_engine *e) {
     cudaStream_t st = e->stream;
     if (cell_off > 0) {
         CK(cudaMemcpyAsync(e->morton, mort.data(), sizeof(int) * cell_off, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(e->nbr, nbr.data(), sizeof(int) * (size_t)cell_off * e->nb,
-                           cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(e->cell_xyz, cxyz.data(), sizeof(int) * cell_off,
                            cudaMemcpyHostToDevice, st));
     }
@@ -508,11 +499,11 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
     int blk = e->tune.block_size;
     {
         ProfScope ps(e, SPH_PASS_DENSITY, st);
-        launch_density(v, e->precision, e->group.kernel, s, blk, e->tune.sweep, st);
+        launch_density(v, e->precision, e->group.kernel, s, blk, st);
     }
     if (e->group.heat_flux) {
         ProfScope ps(e, SPH_PASS_HEAT, st);
-        launch_heat(v, e->precision, e->group.kernel, blk, e->tune.sweep, st);
+        launch_heat(v, e->precision, e->group.kernel, blk, st);
     }
     if (mode == 1 && s == e->nstage - 1 && e->any_thermostat) {
         ProfScope ps(e, SPH_PASS_TSUM, st);
@@ -521,7 +512,7 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
     {
         ProfScope ps(e, SPH_PASS_FORCE, st);
         launch_force(v, e->precision, e->group.kernel, e->group.viscosity, e->group.heat_flux,
-                     e->group.integrator, s, mode, blk, e->tune.sweep, st);
+                     e->group.integrator, s, mode, blk, st);
     }
 }
 
@@ -717,7 +708,7 @@ void free_all(sph_engine *e) {
     free_graph(e);
     void *ptrs[] = {e->a_u, e->a_m, e->a_id, e->a_sim, e->b_u, e->b_m, e->b_id, e->b_sim,
                     e->cell_of, e->rank, e->order_tmp, e->order, e->cell_b, e->cell_count,
-                    e->cell_start, e->nbr, e->morton, e->scan_tmp, e->pk_pos[0], e->pk_pos[1],
+                    e->cell_start, e->morton, e->scan_tmp, e->pk_pos[0], e->pk_pos[1],
                     e->pk_vel[0], e->pk_vel[1], e->pk_f, e->pk_q, e->ue, e->rho, e->rho_l,
                     e->temp, e->pres, e->pco, e->rho0, e->pres0, e->pco0, e->udot, e->f0u,
                     e->acc_u, e->stage_buf, e->sims_d, e->t_scale, e->tsum_part, e->steps_d,
@@ -800,8 +791,8 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->cap_p = max_particles;
     e->cap_s = max_sims;
     e->tune.block_size = 128;
-    e->tune.sweep = 0;
-    e->tune.cell_ratio = 1.0;
+    e->tune.reserved = 0;
+    e->tune.cell_ratio = 0.5;
     e->tune.use_graph = 1;
     e->tune.steps_per_graph = 1;
     if (stream) {
@@ -1043,7 +1034,7 @@ int sph_sim_pair_count(sph_engine *e, int32_t id, int64_t *nip) {
     enqueue_prepare(e, st);
     View v = make_view(e);
     stage_view(e, v, 0);
-    launch_density(v, e->precision, e->group.kernel, 0, e->tune.block_size, e->tune.sweep, st);
+    launch_density(v, e->precision, e->group.kernel, 0, e->tune.block_size, st);
     unsigned long long c = 0;
     CK(cudaMemcpyAsync(&c, e->pair_count + id, sizeof(c), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1172,8 +1163,9 @@ int sph_get_tuning(sph_engine *e, sph_tuning *t) {
 
 int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
     if (!e || !t) return SPH_EINVAL;
-    if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) || !(t->cell_ratio >= 1.0) ||
-        t->sweep < 0 || t->sweep > 1)
+    if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) ||
+        !(t->cell_ratio >= 0.3 && t->cell_ratio <= 4.0) || t->reserved != 0 ||
+        t->steps_per_graph < 1)
         return SPH_EINVAL;
     bool regrid = t->cell_ratio != e->tune.cell_ratio;
     e->tune = *t;

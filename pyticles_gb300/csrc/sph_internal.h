@@ -9,8 +9,9 @@
 //    (float4 in mixed mode, double4 in FP64 mode), FP64 raw evaluation
 //    positions xe (exact pair test), ue, ve; densities, EOS outputs, packed
 //    force factors, heat flux, rates and integrator accumulators.
-//  * cell table: per simulation a Morton-ordered cell range; cell_start[C+1]
-//    and a neighbour table nbr[C][3^dim] of global cell ids (-1: none).
+//  * cell table: per simulation a Morton-ordered cell range; cell_start[C+1],
+//    the packed integer coordinates of every cell and, per simulation, the
+//    linear-cell -> Morton-rank map used to find neighbour cells.
 #pragma once
 
 #include <cstdint>
@@ -28,11 +29,11 @@ struct SimDev {
     double edge[3], inv_edge[3];
     double slack_half[3];   // max displacement per axis between binning and an evaluation
     int nc[3];
+    int win[3];             // neighbour window: +-win cells per axis (0 on single-cell axes)
     int small_mask;         // bit a set: axis a has one cell (minimum image in the pair pass)
     int active;
     int cell_off, ncells;
     int part_off, n;        // range in B (sorted) order
-    int nbr_count;          // 3^dim, neighbour slots per cell
     int thermostat;
     double thr;             // cutoff^2 + tolerance^2 (FP64, the reference's value)
     double hs, hl;          // smoothing lengths
@@ -63,7 +64,7 @@ struct View {
     int *rank;              // A order: arrival rank within cell
     int *order_tmp, *order; // B slot -> A index
     int *cell_count, *cell_start, *cell_b;  // cell_b: B order cell id
-    int *nbr, *morton;
+    int *morton;            // per simulation: linear cell -> Morton rank
     int *cell_xyz;          // global cell -> packed cell coordinates (11/11/10 bits)
     double *org[3];         // B order: FP64 origin of the particle's cell-local frame
     // evaluation (stage s reads *_in, its force pass writes stage s+1's *_out)
@@ -109,11 +110,11 @@ void launch_iota_sim(int *id, int *sim, int sim_id, int n, cudaStream_t s);
 // ---- launch wrappers (sph_pairs.cu) ----
 // stage: evaluation index within the step; nstage: evaluations per step;
 // mode: 0 derivative only, 1 advance.
-void launch_density(const View &v, int precision, int kernel, int stage, int block, int sweep,
+void launch_density(const View &v, int precision, int kernel, int stage, int block,
                     cudaStream_t s);
-void launch_heat(const View &v, int precision, int kernel, int block, int sweep, cudaStream_t s);
+void launch_heat(const View &v, int precision, int kernel, int block, cudaStream_t s);
 void launch_force(const View &v, int precision, int kernel, int viscosity, int heat,
-                  int integrator, int stage, int mode, int block, int sweep, cudaStream_t s);
+                  int integrator, int stage, int mode, int block, cudaStream_t s);
 void launch_tsum(const View &v, int precision, int nsims, cudaStream_t s);
 void launch_pair_rows(const View &v, int precision, int sim_off, int n, long long *row_count,
                       cudaStream_t s);

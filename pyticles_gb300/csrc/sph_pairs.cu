@@ -39,6 +39,7 @@ template <typename R, int D>
 struct PairFrame {
     R thr_lo, thr_hi;
     R edge[3], L[3], hL[3];
+    R ext[3];       // half extent of a cell including the allowed drift
     int small_mask;
     __device__ __forceinline__ void init(const SimDev &S) {
         thr_lo = (R)(S.thr * (1.0 - Margin<R>::rel));
@@ -48,14 +49,12 @@ struct PairFrame {
             edge[a] = (R)S.edge[a];
             L[a] = (R)S.L[a];
             hL[a] = (R)S.half_L[a];
+            // conservative: rounded up so no reachable cell is culled; a
+            // single-cell axis is never culled
+            ext[a] = S.nc[a] >= 3 ? (R)((0.5 * S.edge[a] + S.slack_half[a]) * 1.0001)
+                                  : (R)1e30;
         }
         small_mask = S.small_mask;
-    }
-    // neighbour-cell displacement for neighbour slot t (t = ox+1 + 3(oy+1) + 9(oz+1))
-    __device__ __forceinline__ void shift(int t, R *sh) const {
-        sh[0] = (R)((t % 3) - 1) * edge[0];
-        sh[1] = (R)(((t / 3) % 3) - 1) * edge[1];
-        sh[2] = (D == 3) ? (R)((t / 9) - 1) * edge[2] : (R)0;
     }
     __device__ __forceinline__ void min_image(R *d) const {
         if (small_mask) {
@@ -71,231 +70,76 @@ struct PairFrame {
 
 template <int D> struct NbrCount { static constexpr int value = D == 2 ? 9 : 27; };
 
-// Iterates the pair set of particle i.  body(j, d[3], rsq) is called for
-// every j != i with the exact pair test passed.
+// max(|c| - ext, 0): distance along one axis from particle i to a cell whose
+// centre sits at c relative to i
+template <typename R> __device__ __forceinline__ R fmaxf_(R c, R ext) {
+    R a = (c < (R)0 ? -c : c) - ext;
+    return a > (R)0 ? a : (R)0;
+}
+
+// Iterates the pair set of particle i.  body(j, pj, d[3], rsq) is called for
+// every j != i that passes the exact pair test, in a fixed order: neighbour
+// cells in raster order (z, y, x) of their offset from i's cell, particles in
+// cell order.  The order depends only on i's cell, never on which particles
+// share a warp or a launch, so every particle sums its pairs identically
+// whether its simulation runs alone or in a batch.
+//
+// Cells are (cutoff + skin)/W wide and the window spans +-W cells per axis;
+// a cell whose box (grown by the allowed drift) lies beyond the cutoff from
+// particle i is skipped before any of its particles is loaded.
 template <typename R, int D, typename T4, typename F>
 __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                                           const PairFrame<R, D> &fr, const T4 *__restrict__ P,
                                           int i, const T4 &pi, F body) {
-    constexpr int NB = NbrCount<D>::value;
-    const int *nb = v.nbr + (size_t)v.cell_b[i] * NB;
-    for (int t = 0; t < NB; ++t) {
-        int cj = nb[t];
-        if (cj < 0) continue;
-        R sh[3];
-        fr.shift(t, sh);
-        R ox = sh[0] - pi.x, oy = sh[1] - pi.y, oz = sh[2] - pi.z;
-        int jb = v.cell_start[cj], je = v.cell_start[cj + 1];
-        for (int j = jb; j < je; ++j) {
-            if (j == i) continue;
-            T4 pj = P[j];
-            R d[3];
-            d[0] = pj.x + ox;
-            d[1] = pj.y + oy;
-            d[2] = (D == 3) ? pj.z + oz : (R)0;
-            fr.min_image(d);
-            R rsq = d[0] * d[0] + d[1] * d[1];
-            if (D == 3) rsq += d[2] * d[2];
-            if (rsq > fr.thr_hi) continue;
-            if (rsq >= fr.thr_lo && !exact_in_set<D>(v.xe_in, &S, i, j)) continue;
-            body(j, pj, d, rsq);
+    const int cp = v.cell_xyz[v.cell_b[i]];
+    const int c0 = cp & 2047, c1 = (cp >> 11) & 2047, c2 = (cp >> 22) & 1023;
+    const int w0 = S.win[0], w1 = S.win[1], w2 = D == 3 ? S.win[2] : 0;
+    const int n0 = S.nc[0], n1 = S.nc[1], n2 = S.nc[2];
+    const int *mort = v.morton + S.cell_off;
+    for (int oz = -w2; oz <= w2; ++oz) {
+        R dz = (R)0;
+        int z = 0;
+        if (D == 3) {
+            dz = fmaxf_((R)oz * fr.edge[2] - pi.z, fr.ext[2]);
+            z = c2 + oz;
+            z += (z < 0) ? n2 : 0;
+            z -= (z >= n2) ? n2 : 0;
         }
-    }
-}
-
-// ---- tiled sweep: warp-uniform candidate loops + per-lane compacted lists ----
-//
-// A warp holds 32 consecutive cell-sorted particles, usually from one or two
-// Morton-adjacent cells.  Looping every lane over its own 3^d neighbour
-// cells serialises the warp whenever its lanes sit in different cells, and
-// evaluating the pair body right after the distance test leaves most lanes
-// idle (about a third of the candidates are in range).  Here the warp
-// iterates the union box of its lanes' neighbourhoods with one shared loop
-// (every lane tests the same candidate j against its own particle), appends
-// the in-range neighbours to a per-lane list in shared memory as
-// (neighbour slot t, index within that cell), and evaluates the pair body
-// over the lists with all lanes busy.  Box cells are visited in raster order
-// (z, y, x), which for every lane is the raster order of its own 3^d
-// neighbourhood: each particle sums its pairs in the same order as the
-// per-lane loop, so results do not depend on which particles share a warp.
-constexpr int kTileWarps = 4;
-constexpr int kTileThreads = 32 * kTileWarps;
-template <int D> struct TileCap { static constexpr int value = D == 2 ? 128 : 96; };
-
-template <typename R, int D>
-struct TileShared {
-    unsigned short list[TileCap<D>::value][32];
-    int nstart[NbrCount<D>::value][32];     // per lane: start of its neighbour cell t
-    R shx[NbrCount<D>::value], shy[NbrCount<D>::value], shz[NbrCount<D>::value];
-    int box_start[64], box_len[64];
-};
-
-// Per-lane loop over its own neighbour cells (fallback for wide boxes).
-template <typename R, int D, typename T4, typename F>
-__device__ __forceinline__ void for_pairs_direct(const View &v, const SimDev &S,
-                                                 const PairFrame<R, D> &fr,
-                                                 const T4 *__restrict__ P, int i, const T4 &pi,
-                                                 F body) {
-    for_pairs<R, D>(v, S, fr, P, i, pi, body);
-}
-
-template <typename R, int D, typename T4, typename F>
-__device__ __forceinline__ void for_pairs_tiled(const View &v, const T4 *__restrict__ P, int i,
-                                                bool active, F body) {
-    constexpr int NB = NbrCount<D>::value;
-    constexpr int CAP = TileCap<D>::value;
-    __shared__ TileShared<R, D> tsh[kTileWarps];
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    TileShared<R, D> &ts = tsh[threadIdx.x >> 5];
-    const int s_me = active ? v.b_sim[i] : -1;
-    unsigned todo = __ballot_sync(FULL, active);
-    while (todo) {
-        const int leader = __ffs(todo) - 1;
-        const int s_lead = __shfl_sync(FULL, s_me, leader);
-        const unsigned grp = __ballot_sync(FULL, active && s_me == s_lead);
-        todo &= ~grp;
-        const bool mine = (grp >> lane) & 1u;
-        const SimDev &S = v.sims[s_lead];
-        PairFrame<R, D> fr;
-        fr.init(S);
-        const T4 pi = P[mine ? i : v.np - 1];
-        // cell coordinates relative to the leader's cell, unwrapped
-        const int cp = v.cell_xyz[v.cell_b[mine ? i : v.np - 1]];
-        const int cref = __shfl_sync(FULL, cp, leader);
-        int dc[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, w[3] = {1, 1, 1}, cr[3];
-        bool ok = true;
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-            const int sh = a == 0 ? 0 : (a == 1 ? 11 : 22);
-            const int mask = a == 2 ? 1023 : 2047;
-            cr[a] = (cref >> sh) & mask;
-            const int nc = S.nc[a];
-            if (nc >= 3) {
-                int d = ((cp >> sh) & mask) - cr[a];
-                if (2 * d >= nc) d -= nc;
-                if (2 * d < -nc) d += nc;
-                dc[a] = d;
-                const int mn = __reduce_min_sync(FULL, mine ? d : 0x7fffffff);
-                const int mx = __reduce_max_sync(FULL, mine ? d : -0x7fffffff);
-                lo[a] = mn - 1;
-                w[a] = mx - mn + 3;
-                if (w[a] > 4 || w[a] > nc) ok = false;
-            }
-        }
-        if (!ok) {
-            if (mine) for_pairs_direct<R, D>(v, S, fr, P, i, pi, body);
-            __syncwarp();
-            continue;
-        }
-        const int nbox = w[0] * w[1] * w[2];
-        // box table: start and length of every box cell (raster order, x fastest)
-        int maxlen = 0;
-        for (int b = lane; b < nbox; b += 32) {
-            int o[3] = {b % w[0], (b / w[0]) % w[1], b / (w[0] * w[1])};
-            int lin = 0, mul = 1;
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-                int x = cr[a] + lo[a] + o[a];
-                const int nc = S.nc[a];
-                if (x < 0) x += nc;
-                if (x >= nc) x -= nc;
-                lin += x * mul;
-                mul *= nc;
-            }
-            const int gc = S.cell_off + v.morton[S.cell_off + lin];
-            const int st = v.cell_start[gc];
-            ts.box_start[b] = st;
-            ts.box_len[b] = v.cell_start[gc + 1] - st;
-            maxlen = max(maxlen, ts.box_len[b]);
-        }
-        if (__reduce_max_sync(FULL, maxlen) > 2047) {
-            // index within a cell does not fit the 11-bit list code
-            __syncwarp();
-            if (mine) for_pairs_direct<R, D>(v, S, fr, P, i, pi, body);
-            __syncwarp();
-            continue;
-        }
-        if (lane < NB) {
-            R sh[3];
-            fr.shift(lane, sh);
-            ts.shx[lane] = sh[0];
-            ts.shy[lane] = sh[1];
-            ts.shz[lane] = sh[2];
-        }
-        __syncwarp();
-        int cnt = 0;
-        auto flush = [&]() {
-            const int mc = __reduce_max_sync(FULL, cnt);
-            for (int e = 0; e < mc; ++e) {
-                if (e < cnt) {
-                    const unsigned code = ts.list[e][lane];
-                    const int t = code >> 11;
-                    const int j = ts.nstart[t][lane] + (int)(code & 2047u);
+        for (int oy = -w1; oy <= w1; ++oy) {
+            R dy = fmaxf_((R)oy * fr.edge[1] - pi.y, fr.ext[1]);
+            R dyz = dy * dy + dz * dz;
+            if (dyz > fr.thr_hi) continue;
+            int y = c1 + oy;
+            y += (y < 0) ? n1 : 0;
+            y -= (y >= n1) ? n1 : 0;
+            const int row = (z * n1 + y) * n0;
+            for (int ox = -w0; ox <= w0; ++ox) {
+                R dx = fmaxf_((R)ox * fr.edge[0] - pi.x, fr.ext[0]);
+                if (dx * dx + dyz > fr.thr_hi) continue;
+                int x = c0 + ox;
+                x += (x < 0) ? n0 : 0;
+                x -= (x >= n0) ? n0 : 0;
+                const int gc = S.cell_off + mort[row + x];
+                const R ox_ = (R)ox * fr.edge[0] - pi.x;
+                const R oy_ = (R)oy * fr.edge[1] - pi.y;
+                const R oz_ = (D == 3) ? (R)oz * fr.edge[2] - pi.z : (R)0;
+                const int jb = v.cell_start[gc], je = v.cell_start[gc + 1];
+                for (int j = jb; j < je; ++j) {
+                    if (j == i) continue;
                     const T4 pj = P[j];
                     R d[3];
-                    d[0] = pj.x + (ts.shx[t] - pi.x);
-                    d[1] = pj.y + (ts.shy[t] - pi.y);
-                    d[2] = (D == 3) ? pj.z + (ts.shz[t] - pi.z) : (R)0;
+                    d[0] = pj.x + ox_;
+                    d[1] = pj.y + oy_;
+                    d[2] = (D == 3) ? pj.z + oz_ : (R)0;
                     fr.min_image(d);
                     R rsq = d[0] * d[0] + d[1] * d[1];
                     if (D == 3) rsq += d[2] * d[2];
+                    if (rsq > fr.thr_hi) continue;
+                    if (rsq >= fr.thr_lo && !exact_in_set<D>(v.xe_in, &S, i, j)) continue;
                     body(j, pj, d, rsq);
                 }
             }
-            cnt = 0;
-        };
-        for (int b = 0; b < nbox; ++b) {
-            const int st = ts.box_start[b], len = ts.box_len[b];
-            if (len == 0) continue;
-            // this box cell relative to the lane's own cell
-            int t = 0, mul = 1;
-            bool nbh = mine;
-            int o[3] = {b % w[0], (b / w[0]) % w[1], b / (w[0] * w[1])};
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-                const int rel = lo[a] + o[a] - dc[a];
-                nbh = nbh && rel >= -1 && rel <= 1;
-                t += (rel + 1) * mul;
-                mul *= 3;
-            }
-            if (nbh) ts.nstart[t][lane] = st;
-            const R ox = nbh ? ts.shx[t] - pi.x : (R)0;
-            const R oy = nbh ? ts.shy[t] - pi.y : (R)0;
-            const R oz = (nbh && D == 3) ? ts.shz[t] - pi.z : (R)0;
-            // chunks that fit the lists; flush when the fullest list is full
-            for (int k0 = 0; k0 < len;) {
-                int room = CAP - __reduce_max_sync(FULL, cnt);
-                if (room == 0) {
-                    __syncwarp();
-                    flush();
-                    room = CAP;
-                }
-                const int k1 = min(len, k0 + room);
-                for (int k = k0; k < k1; ++k) {
-                    const int j = st + k;
-                    const T4 pj = P[j];
-                    if (nbh && j != i) {
-                        R d[3];
-                        d[0] = pj.x + ox;
-                        d[1] = pj.y + oy;
-                        d[2] = (D == 3) ? pj.z + oz : (R)0;
-                        fr.min_image(d);
-                        R rsq = d[0] * d[0] + d[1] * d[1];
-                        if (D == 3) rsq += d[2] * d[2];
-                        if (rsq <= fr.thr_hi &&
-                            (rsq < fr.thr_lo || exact_in_set<D>(v.xe_in, &S, i, j))) {
-                            ts.list[cnt][lane] = (unsigned short)((t << 11) | k);
-                            ++cnt;
-                        }
-                    }
-                }
-                k0 = k1;
-            }
         }
-        __syncwarp();
-        flush();
-        __syncwarp();
     }
 }
 
@@ -314,8 +158,8 @@ __device__ __forceinline__ void add_pair_count(unsigned long long *cnt, int s, u
     if ((threadIdx.x & 31) == leader) atomicAdd(&cnt[s], tot);
 }
 
-template <typename R, int D, int K, bool TILED>
-__global__ void __launch_bounds__(kTileThreads) k_density(View v, int stage) {
+template <typename R, int D, int K>
+__global__ void __launch_bounds__(256) k_density(View v, int stage) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
@@ -338,14 +182,12 @@ __global__ void __launch_bounds__(kTileThreads) k_density(View v, int stage) {
         rl.add(pj.w * w);
         ++cnt;
     };
-    if (TILED) {
-        for_pairs_tiled<R, D>(v, P, i, active, body);
-    } else if (active) {
+    if (!active) return;
+    {
         PairFrame<R, D> fr;
         fr.init(S);
         for_pairs<R, D>(v, S, fr, P, i, P[i], body);
     }
-    if (!active) return;
     // EOS in FP64 from the compensated sums plus the FP64 self term
     // (properties.py:77-78): the temperature T = (u + a rho)/k_B cancels
     // strongly, so rho enters it with the bits the FP32 sum carried in its
@@ -378,8 +220,8 @@ __global__ void __launch_bounds__(kTileThreads) k_density(View v, int stage) {
     add_pair_count(v.pair_count, s, cnt);
 }
 
-template <typename R, int D, int K, bool TILED>
-__global__ void __launch_bounds__(kTileThreads) k_heat(View v) {
+template <typename R, int D, int K>
+__global__ void __launch_bounds__(256) k_heat(View v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
@@ -404,14 +246,12 @@ __global__ void __launch_bounds__(kTileThreads) k_heat(View v) {
         q[1].add(f * d[1]);
         if (D == 3) q[2].add(f * d[2]);
     };
-    if (TILED) {
-        for_pairs_tiled<R, D>(v, P, i, active, body);
-    } else if (active) {
+    if (!active) return;
+    {
         PairFrame<R, D> fr;
         fr.init(S);
         for_pairs<R, D>(v, S, fr, P, i, P[i], body);
     }
-    if (!active) return;
     R kap = (R)S.kappa;
     R qq[3] = {kap * q[0].get(), kap * q[1].get(), kap * q[2].get()};
     R ir2 = (R)1 / (fi.y * fi.y);
@@ -460,8 +300,8 @@ __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S
     v.a_sim[i] = v.b_sim[i];
 }
 
-template <typename R, int D, int K, bool TILED>
-__global__ void __launch_bounds__(kTileThreads) k_force(View v, int stage, int mode, int integ,
+template <typename R, int D, int K>
+__global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int integ,
                                                         int visc, int heat) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < v.np;
@@ -510,14 +350,12 @@ __global__ void __launch_bounds__(kTileThreads) k_force(View v, int stage, int m
         }
         ud.add(du);
     };
-    if (TILED) {
-        for_pairs_tiled<R, D>(v, P, i, active, body);
-    } else if (active) {
+    if (!active) return;
+    {
         PairFrame<R, D> fr;
         fr.init(S);
         for_pairs<R, D>(v, S, fr, P, i, P[i], body);
     }
-    if (!active) return;
     R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
     R udr = ud.get();
     for (int a = 0; a < D; ++a) ((R *)v.vdot[a])[i] = vdr[a];
@@ -635,49 +473,26 @@ __global__ void __launch_bounds__(kTileThreads) k_force(View v, int stage, int m
         default: { constexpr int K = SPH_KERNEL_CUBIC; CALL; break; }                     \
     }
 
-// sweep: 0 tiled warp sweep (block of kTileThreads), 1 per-lane loop (block
-// of `block` threads).
-void launch_density(const View &v, int precision, int kernel, int stage, int block, int sweep,
+void launch_density(const View &v, int precision, int kernel, int stage, int block,
                     cudaStream_t s) {
     if (v.np <= 0) return;
-    if (sweep == 0) {
-        int nb = (v.np + kTileThreads - 1) / kTileThreads;
-        SPH_DISPATCH(precision, v.dim, kernel,
-                     (k_density<R, D, K, true><<<nb, kTileThreads, 0, s>>>(v, stage)));
-    } else {
-        int nb = (v.np + block - 1) / block;
-        SPH_DISPATCH(precision, v.dim, kernel,
-                     (k_density<R, D, K, false><<<nb, block, 0, s>>>(v, stage)));
-    }
+    int nb = (v.np + block - 1) / block;
+    SPH_DISPATCH(precision, v.dim, kernel, (k_density<R, D, K><<<nb, block, 0, s>>>(v, stage)));
 }
 
-void launch_heat(const View &v, int precision, int kernel, int block, int sweep,
-                 cudaStream_t s) {
+void launch_heat(const View &v, int precision, int kernel, int block, cudaStream_t s) {
     if (v.np <= 0) return;
-    if (sweep == 0) {
-        int nb = (v.np + kTileThreads - 1) / kTileThreads;
-        SPH_DISPATCH(precision, v.dim, kernel,
-                     (k_heat<R, D, K, true><<<nb, kTileThreads, 0, s>>>(v)));
-    } else {
-        int nb = (v.np + block - 1) / block;
-        SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K, false><<<nb, block, 0, s>>>(v)));
-    }
+    int nb = (v.np + block - 1) / block;
+    SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K><<<nb, block, 0, s>>>(v)));
 }
 
 void launch_force(const View &v, int precision, int kernel, int viscosity, int heat,
-                  int integrator, int stage, int mode, int block, int sweep, cudaStream_t s) {
+                  int integrator, int stage, int mode, int block, cudaStream_t s) {
     if (v.np <= 0) return;
-    if (sweep == 0) {
-        int nb = (v.np + kTileThreads - 1) / kTileThreads;
-        SPH_DISPATCH(precision, v.dim, kernel,
-                     (k_force<R, D, K, true><<<nb, kTileThreads, 0, s>>>(
-                         v, stage, mode, integrator, viscosity, heat)));
-    } else {
-        int nb = (v.np + block - 1) / block;
-        SPH_DISPATCH(precision, v.dim, kernel,
-                     (k_force<R, D, K, false><<<nb, block, 0, s>>>(v, stage, mode, integrator,
-                                                                  viscosity, heat)));
-    }
+    int nb = (v.np + block - 1) / block;
+    SPH_DISPATCH(precision, v.dim, kernel,
+                 (k_force<R, D, K><<<nb, block, 0, s>>>(v, stage, mode, integrator, viscosity,
+                                                       heat)));
 }
 
 // ---- thermostat: per-chunk FP64 partial sums of T, then one thread per
@@ -728,94 +543,98 @@ void launch_tsum(const View &v, int precision, int nsims, cudaStream_t s) {
 }
 
 // ---- pair-set export (VerletList.build + NeighbourList.separations
-// attributes); exact FP64 test on every candidate, not on the hot path ----
-template <int D>
+// attributes): the same pair iteration, rows keyed by original index ----
+template <typename R, int D>
 __global__ void k_pair_rows(View v, int off, int n, long long *row_count) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int i = off + k;
     const SimDev &S = v.sims[v.b_sim[i]];
-    constexpr int NB = NbrCount<D>::value;
-    const int *nb = v.nbr + (size_t)v.cell_b[i] * NB;
-    int idi = v.b_id[i];
+    using T4 = typename V4<R>::T;
+    const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
+    PairFrame<R, D> fr;
+    fr.init(S);
+    const int idi = v.b_id[i];
     long long c = 0;
-    for (int t = 0; t < NB; ++t) {
-        int cj = nb[t];
-        if (cj < 0) continue;
-        for (int j = v.cell_start[cj]; j < v.cell_start[cj + 1]; ++j) {
-            if (j == i || v.b_id[j] < idi) continue;
-            if (exact_rsq<D>(v.xe_in, S, i, j) < S.thr) ++c;
-        }
-    }
+    for_pairs<R, D>(v, S, fr, P, i, P[i], [&](int j, const T4 &, const R *, R) {
+        if (v.b_id[j] > idi) ++c;
+    });
     row_count[idi] = c;
 }
 
-template <int D>
+template <typename R, int D>
 __global__ void k_pair_write(View v, int off, int n, const long long *row_start, long long *iap,
                              double *drij, double *rsq, double *dv) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int i = off + k;
     const SimDev &S = v.sims[v.b_sim[i]];
-    constexpr int NB = NbrCount<D>::value;
-    const int *nb = v.nbr + (size_t)v.cell_b[i] * NB;
-    int idi = v.b_id[i];
-    long long base = row_start[idi];
+    using T4 = typename V4<R>::T;
+    const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
+    PairFrame<R, D> fr;
+    fr.init(S);
+    const int idi = v.b_id[i];
+    const long long base = row_start[idi];
     long long m = 0;
-    for (int t = 0; t < NB; ++t) {
-        int cj = nb[t];
-        if (cj < 0) continue;
-        for (int j = v.cell_start[cj]; j < v.cell_start[cj + 1]; ++j) {
-            if (j == i || v.b_id[j] < idi) continue;
-            double r2 = exact_rsq<D>(v.xe_in, S, i, j);
-            if (!(r2 < S.thr)) continue;
-            // insertion into the row, ordered by j's original index
-            int idj = v.b_id[j];
-            long long p = base + m;
-            while (p > base && iap[2 * (p - 1) + 1] > idj) {
-                iap[2 * p] = iap[2 * (p - 1)];
-                iap[2 * p + 1] = iap[2 * (p - 1) + 1];
-                if (rsq) rsq[p] = rsq[p - 1];
-                if (drij)
-                    for (int a = 0; a < D; ++a) drij[p * D + a] = drij[(p - 1) * D + a];
-                if (dv)
-                    for (int a = 0; a < D; ++a) dv[p * D + a] = dv[(p - 1) * D + a];
-                --p;
-            }
-            iap[2 * p] = idi;
-            iap[2 * p + 1] = idj;
-            if (rsq) rsq[p] = r2;
-            for (int a = 0; a < D; ++a) {
-                double d = __dsub_rn(v.xe_in[a][j], v.xe_in[a][i]);
-                if (d > S.half_L[a]) d = __dsub_rn(d, S.L[a]);
-                if (d < -S.half_L[a]) d = __dadd_rn(d, S.L[a]);
-                if (drij) drij[p * D + a] = d;
-                if (dv) dv[p * D + a] = __dsub_rn(v.ve_in[a][j], v.ve_in[a][i]);
-            }
-            ++m;
+    for_pairs<R, D>(v, S, fr, P, i, P[i], [&](int j, const T4 &, const R *, R) {
+        const int idj = v.b_id[j];
+        if (idj < idi) return;
+        // insertion into the row, ordered by j's original index
+        long long p = base + m;
+        while (p > base && iap[2 * (p - 1) + 1] > idj) {
+            iap[2 * p] = iap[2 * (p - 1)];
+            iap[2 * p + 1] = iap[2 * (p - 1) + 1];
+            if (rsq) rsq[p] = rsq[p - 1];
+            if (drij)
+                for (int a = 0; a < D; ++a) drij[p * D + a] = drij[(p - 1) * D + a];
+            if (dv)
+                for (int a = 0; a < D; ++a) dv[p * D + a] = dv[(p - 1) * D + a];
+            --p;
         }
-    }
+        iap[2 * p] = idi;
+        iap[2 * p + 1] = idj;
+        double r2 = 0.0;
+        for (int a = 0; a < D; ++a) {
+            double d = __dsub_rn(v.xe_in[a][j], v.xe_in[a][i]);
+            if (d > S.half_L[a]) d = __dsub_rn(d, S.L[a]);
+            if (d < -S.half_L[a]) d = __dadd_rn(d, S.L[a]);
+            r2 = (a == 0) ? __dmul_rn(d, d) : __dadd_rn(r2, __dmul_rn(d, d));
+            if (drij) drij[p * D + a] = d;
+            if (dv) dv[p * D + a] = __dsub_rn(v.ve_in[a][j], v.ve_in[a][i]);
+        }
+        if (rsq) rsq[p] = r2;
+        ++m;
+    });
 }
 
 void launch_pair_rows(const View &v, int precision, int sim_off, int n, long long *row_count,
                       cudaStream_t s) {
-    (void)precision;
     if (n <= 0) return;
     int nb = (n + 127) / 128;
-    if (v.dim == 2) k_pair_rows<2><<<nb, 128, 0, s>>>(v, sim_off, n, row_count);
-    else k_pair_rows<3><<<nb, 128, 0, s>>>(v, sim_off, n, row_count);
+    if (precision == SPH_MIXED) {
+        if (v.dim == 2) k_pair_rows<float, 2><<<nb, 128, 0, s>>>(v, sim_off, n, row_count);
+        else k_pair_rows<float, 3><<<nb, 128, 0, s>>>(v, sim_off, n, row_count);
+    } else {
+        if (v.dim == 2) k_pair_rows<double, 2><<<nb, 128, 0, s>>>(v, sim_off, n, row_count);
+        else k_pair_rows<double, 3><<<nb, 128, 0, s>>>(v, sim_off, n, row_count);
+    }
 }
 
 void launch_pair_write(const View &v, int precision, int sim_off, int n,
                        const long long *row_start, long long *iap, double *drij, double *rsq,
                        double *dv, cudaStream_t s) {
-    (void)precision;
     if (n <= 0) return;
     int nb = (n + 127) / 128;
-    if (v.dim == 2)
-        k_pair_write<2><<<nb, 128, 0, s>>>(v, sim_off, n, row_start, iap, drij, rsq, dv);
-    else
-        k_pair_write<3><<<nb, 128, 0, s>>>(v, sim_off, n, row_start, iap, drij, rsq, dv);
+#define SPH_PW(R_, D_) \
+    k_pair_write<R_, D_><<<nb, 128, 0, s>>>(v, sim_off, n, row_start, iap, drij, rsq, dv)
+    if (precision == SPH_MIXED) {
+        if (v.dim == 2) SPH_PW(float, 2);
+        else SPH_PW(float, 3);
+    } else {
+        if (v.dim == 2) SPH_PW(double, 2);
+        else SPH_PW(double, 3);
+    }
+#undef SPH_PW
 }
 
 // exclusive scan of n+1 int64 entries in place (export path only)

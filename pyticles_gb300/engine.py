@@ -186,16 +186,15 @@ class Engine:
     def tuning(self):
         t = SphTuning()
         check(self._lib.sph_get_tuning(self._h, ctypes.byref(t)), "sph_get_tuning")
-        return {"block_size": t.block_size, "sweep": t.sweep,
-                "cell_ratio": t.cell_ratio, "use_graph": t.use_graph,
-                "steps_per_graph": t.steps_per_graph}
+        return {"block_size": t.block_size, "use_graph": t.use_graph,
+                "steps_per_graph": t.steps_per_graph, "cell_ratio": t.cell_ratio}
 
     def set_tuning(self, **kw):
         cur = self.tuning
         cur.update(kw)
-        t = SphTuning(int(cur["block_size"]), int(cur["sweep"]),
-                      float(cur["cell_ratio"]), int(cur["use_graph"]),
-                      int(cur["steps_per_graph"]))
+        t = SphTuning(block_size=int(cur["block_size"]), use_graph=int(cur["use_graph"]),
+                      steps_per_graph=int(cur["steps_per_graph"]), reserved=0,
+                      cell_ratio=float(cur["cell_ratio"]))
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), "sph_set_tuning")
 
     # -- launch-ready graphs and per-pass timing --
