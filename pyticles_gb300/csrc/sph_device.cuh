@@ -109,19 +109,26 @@ template <typename R> struct KConst {
     R h, inv_h, inv_h_lo, sig, g0;  // g0: Lucy -12 sig/h^2, Gaussian -2/h^2, cubic sig/h^2
 };
 
+template <typename R> __device__ __forceinline__ const SimConst<R> &sconst(const SimDev &S);
+template <> __device__ __forceinline__ const SimConst<float> &sconst<float>(const SimDev &S) {
+    return S.cf;
+}
+template <> __device__ __forceinline__ const SimConst<double> &sconst<double>(const SimDev &S) {
+    return S.cd;
+}
+
+// Kernel constants of smoothing length `which` (0 short, 1 long).  1/h is a
+// hi/lo pair: q = fma(r, hi, r*lo) is unbiased to ~0.5 ulp instead of
+// carrying the rounding of 1/h into every term alike.
 template <typename R>
-__device__ __forceinline__ KConst<R> make_kconst(int K, double h, double sig) {
+__device__ __forceinline__ KConst<R> make_kconst(const SimDev &S, int which) {
+    const SimConst<R> &c = sconst<R>(S);
     KConst<R> k;
-    k.h = (R)h;
-    k.inv_h = (R)(1.0 / h);
-    // 1/h as a hi/lo pair: q = fma(r, hi, r*lo) is then unbiased to ~0.5 ulp
-    // instead of carrying the rounding of 1/h into every term alike
-    k.inv_h_lo = (R)(1.0 / h - (double)k.inv_h);
-    k.sig = (R)sig;
-    if (K == SPH_KERNEL_LUCY) k.g0 = (R)(-12.0 * sig / (h * h));
-    else if (K == SPH_KERNEL_GAUSSIAN) k.g0 = (R)(-2.0 / (h * h));  // times sig in kernel_wg
-    else if (K == SPH_KERNEL_CUBIC) k.g0 = (R)(sig / (h * h));
-    else k.g0 = (R)(-3.0 * sig);
+    k.h = c.h[which];
+    k.inv_h = c.inv_h[which];
+    k.inv_h_lo = c.inv_h_lo[which];
+    k.sig = c.sig[which];
+    k.g0 = c.g0[which];
     return k;
 }
 
@@ -142,6 +149,11 @@ template <> __device__ __forceinline__ double qof<double>(const KConst<double> &
 
 // *w receives W/sigma (the normalisation is applied once per particle in
 // FP64, which keeps its rounding out of every term); *g the full (dW/dr)/r.
+// correctly rounded reciprocal (cheaper than a division)
+template <typename R> __device__ __forceinline__ R rrcp(R x);
+template <> __device__ __forceinline__ float rrcp<float>(float x) { return __frcp_rn(x); }
+template <> __device__ __forceinline__ double rrcp<double>(double x) { return 1.0 / x; }
+
 template <int K, typename R>
 __device__ __forceinline__ void kernel_wg(const KConst<R> &k, R r, R *w, R *g) {
     if (K == SPH_KERNEL_LUCY) {
@@ -164,24 +176,23 @@ __device__ __forceinline__ void kernel_wg(const KConst<R> &k, R r, R *w, R *g) {
         if (r < k.h) {
             R s = k.h - r;
             *w = s * s * s;
-            *g = (r > (R)0) ? k.g0 * s * s / r : (R)0;
+            *g = (r > (R)0) ? k.g0 * s * s * rrcp<R>(r) : (R)0;
         } else {
             *w = (R)0;
             *g = (R)0;
         }
-    } else {  // cubic spline
+    } else {  // cubic spline, evaluated without branches (selects)
         R q = qof<R>(k, r);
-        if (q < (R)1) {
-            *w = (R)1 - (R)1.5 * q * q + (R)0.75 * q * q * q;
-            *g = k.g0 * ((R)-3 + (R)2.25 * q);
-        } else if (q < (R)2) {
-            R s = (R)2 - q;
-            *w = (R)0.25 * s * s * s;
-            *g = (R)-0.75 * k.sig * s * s * k.inv_h / r;
-        } else {
-            *w = (R)0;
-            *g = (R)0;
-        }
+        R s = (R)2 - q;
+        s = s > (R)0 ? s : (R)0;
+        R w_in = (R)1 - (R)1.5 * q * q + (R)0.75 * q * q * q;
+        R g_in = k.g0 * ((R)-3 + (R)2.25 * q);
+        R w_out = (R)0.25 * s * s * s;
+        // -0.75 sig s^2 / (h r) = g0 * (-0.75 s^2 h / r) with g0 = sig/h^2
+        R g_out = k.g0 * ((R)-0.75 * s * s * k.h) * rrcp<R>(r);
+        bool inner = q < (R)1;
+        *w = inner ? w_in : w_out;
+        *g = inner ? g_in : g_out;
     }
 }
 

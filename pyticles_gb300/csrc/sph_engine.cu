@@ -71,7 +71,7 @@ int dalloc(T **p, size_t n) {
 struct sph_engine {
     sph_params group;
     int precision = SPH_MIXED;
-    int dim = 2, nb = 9, nstage = 2;
+    int dim = 2, nstage = 2;
     size_t rsize = 4, v4size = 16;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -235,6 +235,42 @@ void make_grid(Sim &S, int dim, double ratio) {
     }
 }
 
+template <typename R>
+void fill_const(SimConst<R> &c, const sph_engine *e, const Sim &S, const SimDev &d,
+                double margin) {
+    const sph_params &p = S.prm;
+    c.thr_lo = (R)(d.thr * (1.0 - margin));
+    c.thr_hi = (R)(d.thr * (1.0 + margin));
+    for (int a = 0; a < 3; ++a) {
+        c.edge[a] = (R)S.edge[a];
+        c.L[a] = (R)p.box[a];
+        c.hL[a] = (R)d.half_L[a];
+        // rounded up so no reachable cell is culled; single-cell axes never are
+        c.ext[a] = (a < e->dim && S.win[a] > 0) ? (R)((0.5 * S.edge[a] + d.slack_half[a]) * 1.0001)
+                                               : (R)1e30;
+    }
+    const double hh[2] = {p.h_short, p.h_long}, sg[2] = {d.sig_s, d.sig_l};
+    for (int k = 0; k < 2; ++k) {
+        double h = hh[k], sig = sg[k];
+        c.h[k] = (R)h;
+        c.inv_h[k] = (R)(1.0 / h);
+        c.inv_h_lo[k] = (R)(1.0 / h - (double)c.inv_h[k]);
+        c.sig[k] = (R)sig;
+        switch (p.kernel) {
+            case SPH_KERNEL_LUCY: c.g0[k] = (R)(-12.0 * sig / (h * h)); break;
+            case SPH_KERNEL_GAUSSIAN: c.g0[k] = (R)(-2.0 / (h * h)); break;  // times sig later
+            case SPH_KERNEL_CUBIC: c.g0[k] = (R)(sig / (h * h)); break;
+            default: c.g0[k] = (R)(-3.0 * sig); break;
+        }
+    }
+    c.hs = (R)p.h_short;
+    c.eps_h2 = (R)(p.visc_eps * p.h_short * p.h_short);
+    c.alpha_c = (R)(p.visc_alpha * p.sound_speed);
+    c.beta = (R)p.visc_beta;
+    c.pl2 = (R)(-2.0 * p.adash);
+    c.kappa = (R)p.thermalk;
+}
+
 SimDev make_simdev(const sph_engine *e, const Sim &S) {
     SimDev d;
     memset(&d, 0, sizeof(d));
@@ -278,6 +314,10 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
     d.T0 = p.thermostat_temp;
     d.T1 = p.thermostat_temp_end;
     d.ramp = p.thermostat_ramp_steps;
+    // fast-test guard band: 2^-12 relative in FP32 (cell-local coordinates
+    // keep the FP32 squared distance within 5e-6 of the FP64 one), 1e-9 in FP64
+    fill_const<float>(d.cf, e, S, d, 1.0 / 4096.0);
+    fill_const<double>(d.cd, e, S, d, 1e-9);
     return d;
 }
 
@@ -784,7 +824,6 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->group = *group;
     e->precision = precision;
     e->dim = group->dim;
-    e->nb = group->dim == 2 ? 9 : 27;
     e->nstage = nstage_of(group->integrator);
     e->rsize = precision == SPH_MIXED ? 4 : 8;
     e->v4size = precision == SPH_MIXED ? 16 : 32;
@@ -792,7 +831,8 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->cap_s = max_sims;
     e->tune.block_size = 128;
     e->tune.reserved = 0;
-    e->tune.cell_ratio = 0.5;
+    // measured on GB300: 1/3-cutoff cells in 2D, 1/2 in 3D (autotune.py re-tunes)
+    e->tune.cell_ratio = group->dim == 2 ? 1.0 / 3.0 : 0.5;
     e->tune.use_graph = 1;
     e->tune.steps_per_graph = 1;
     if (stream) {

@@ -23,6 +23,17 @@ namespace sph {
 
 constexpr int kMaxNbr = 27;
 
+// Pair-pass constants of one simulation in the arithmetic type of the
+// passes, precomputed on the host so that no thread spends FP64 work (or a
+// division) deriving them.  Index 0 = short smoothing length, 1 = long.
+template <typename R> struct SimConst {
+    R thr_lo, thr_hi;            // fast-test band around cutoff^2 + tolerance^2
+    R edge[3], L[3], hL[3];
+    R ext[3];                    // half cell extent + allowed drift (culling)
+    R h[2], inv_h[2], inv_h_lo[2], sig[2], g0[2];
+    R hs, eps_h2, alpha_c, beta, pl2, kappa;
+};
+
 // Per-simulation constants on the device.
 struct SimDev {
     double L[3], half_L[3], inv_L[3];
@@ -46,6 +57,8 @@ struct SimDev {
     double inv_kb;
     double T0, T1;          // thermostat ramp ends
     long long ramp;
+    SimConst<float> cf;
+    SimConst<double> cd;
 };
 
 // Pointers of the engine buffers (device addresses), passed by value.

@@ -42,17 +42,15 @@ struct PairFrame {
     R ext[3];       // half extent of a cell including the allowed drift
     int small_mask;
     __device__ __forceinline__ void init(const SimDev &S) {
-        thr_lo = (R)(S.thr * (1.0 - Margin<R>::rel));
-        thr_hi = (R)(S.thr * (1.0 + Margin<R>::rel));
+        const SimConst<R> &c = sconst<R>(S);
+        thr_lo = c.thr_lo;
+        thr_hi = c.thr_hi;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            edge[a] = (R)S.edge[a];
-            L[a] = (R)S.L[a];
-            hL[a] = (R)S.half_L[a];
-            // conservative: rounded up so no reachable cell is culled; a
-            // single-cell axis is never culled
-            ext[a] = S.nc[a] >= 3 ? (R)((0.5 * S.edge[a] + S.slack_half[a]) * 1.0001)
-                                  : (R)1e30;
+            edge[a] = c.edge[a];
+            L[a] = c.L[a];
+            hL[a] = c.hL[a];
+            ext[a] = c.ext[a];
         }
         small_mask = S.small_mask;
     }
@@ -167,8 +165,8 @@ __global__ void __launch_bounds__(256) k_density(View v, int stage) {
     const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
     const int s = v.b_sim[ii];
     const SimDev &S = v.sims[s];
-    KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
-    KConst<R> kl = make_kconst<R>(K, S.hl, S.sig_l);
+    KConst<R> ks = make_kconst<R>(S, 0);
+    KConst<R> kl = make_kconst<R>(S, 1);
     Acc<R> rs, rl;
     rs.init((R)0);
     rl.init((R)0);
@@ -230,7 +228,7 @@ __global__ void __launch_bounds__(256) k_heat(View v) {
     const T4 *__restrict__ F = (const T4 *)v.pk_f;
     const int s = v.b_sim[ii];
     const SimDev &S = v.sims[s];
-    KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
+    KConst<R> ks = make_kconst<R>(S, 0);
     const T4 fi = F[ii];
     Acc<R> q[3];
     q[0].init(0);
@@ -241,7 +239,7 @@ __global__ void __launch_bounds__(256) k_heat(View v) {
         R g = kernel_g<K, R>(ks, r);
         T4 fj = F[j];
         R dT = (fj.z - fi.z) + (fj.w - fi.w);
-        R f = (pj.w / fj.y) * dT * g;
+        R f = pj.w * rrcp<R>(fj.y) * dT * g;
         q[0].add(f * d[0]);
         q[1].add(f * d[1]);
         if (D == 3) q[2].add(f * d[2]);
@@ -252,7 +250,7 @@ __global__ void __launch_bounds__(256) k_heat(View v) {
         fr.init(S);
         for_pairs<R, D>(v, S, fr, P, i, P[i], body);
     }
-    R kap = (R)S.kappa;
+    R kap = sconst<R>(S).kappa;
     R qq[3] = {kap * q[0].get(), kap * q[1].get(), kap * q[2].get()};
     R ir2 = (R)1 / (fi.y * fi.y);
     for (int a = 0; a < D; ++a) ((R *)v.q[a])[i] = qq[a];
@@ -313,11 +311,12 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
     const T4 *__restrict__ Q = (const T4 *)v.pk_q;
     const int s = v.b_sim[ii];
     const SimDev &S = v.sims[s];
-    KConst<R> ks = make_kconst<R>(K, S.hs, S.sig_s);
-    KConst<R> kl = make_kconst<R>(K, S.hl, S.sig_l);
-    const R hs = (R)S.hs, eps_h2 = (R)(S.eps * S.hs * S.hs);
-    const R alpha_c = (R)(S.alpha * S.c), beta = (R)S.beta;
-    const R pl2 = (R)(-2.0 * S.a);  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
+    KConst<R> ks = make_kconst<R>(S, 0);
+    KConst<R> kl = make_kconst<R>(S, 1);
+    const SimConst<R> &sc = sconst<R>(S);
+    const R hs = sc.hs, eps_h2 = sc.eps_h2;
+    const R alpha_c = sc.alpha_c, beta = sc.beta;
+    const R pl2 = sc.pl2;  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
     const T4 vi = V[ii], fi = F[ii];
     const T4 qi = heat ? Q[ii] : make_v4<R>(0, 0, 0, 0);
     Acc<R> ax[3], ud;
@@ -334,6 +333,7 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
         if (D == 3) dvdx += (vj.z - vi.z) * d[2];
         R ps = fi.x + fj.x;
         if (visc && dvdx < (R)0) {
+            // Monaghan viscosity on approaching pairs
             R mu = hs * dvdx / (rsq + eps_h2);
             ps += (-alpha_c * mu + beta * mu * mu) / ((R)0.5 * (fi.y + fj.y));
         }

@@ -153,11 +153,16 @@ def test_full_physics_vs_oracle(case, precision):
     with e:
         d = e.derivatives(s)
         e.sync()
-        tol = EVAL_TOL if precision == "fp64" else MIXED_TOL
         keys = KEYS + (("jq",) if prm.heat_flux else ())
         errs = {k: rel_l2(d[k], ref[k]) for k in keys}
         print(case, precision, errs)
         for k, err in errs.items():
+            if precision == "fp64":
+                tol = EVAL_TOL
+            else:
+                # jq sums temperature differences T_j - T_i, each carrying the
+                # density error times a/k_B: held to the pressure-only bound
+                tol = PRESSURE_ONLY_TOL if k == "jq" else MIXED_TOL
             assert err < tol, (k, err)
         assert e.pair_count(s) == ref["nip"]
         e.advance(5)
