@@ -203,6 +203,34 @@ int sph_sync(sph_engine *e);
 /* Per-simulation device error word (0 = ok). */
 int sph_sim_status(sph_engine *e, int32_t sim_id, int32_t *status);
 
+/* ---- allocation-free evaluation (no counterpart in the reference) ------
+ * One derivative evaluation of one simulation -- the passes of
+ * sph_sim_derivatives -- for callers that cannot let a library allocate
+ * device memory: a host application or framework that budgets the whole
+ * device up front and hands out memory only from its own pool, or a
+ * latency-critical loop that may not block in the allocator.  All pointers
+ * are device pointers owned by the caller: r, v (n x dim), m, u (n) in;
+ * rho, rho_lr, t, p, pco, udot (n) and vdot, jq (n x dim) out, in the
+ * caller's particle order (any output may be NULL).  stream is a
+ * cudaStream_t (NULL: the legacy default stream); the call returns after the
+ * work has finished, with the device error word (SPH_ENAN) as its status.
+ * It calls no cudaMalloc / cudaFree: all intermediate arrays live in one
+ * file-scope static device array of SPH_NOALLOC_SCRATCH_BYTES, which every
+ * GPU that loads the library holds until the process exits.  Limits:
+ * n <= SPH_NOALLOC_MAX_PARTICLES (SPH_EINVAL beyond), at most
+ * SPH_NOALLOC_MAX_CELLS cells (coarser cells are chosen when the box needs
+ * more; SPH_ECAPACITY if even those exceed it).  The first call on a device
+ * looks up the array's device address; make that first call before any
+ * stream capture.  All calls share the array: calls whose work overlaps on
+ * the GPU (two threads, or unordered streams) race on it. */
+#define SPH_NOALLOC_MAX_PARTICLES 16384
+#define SPH_NOALLOC_MAX_CELLS 16384
+#define SPH_NOALLOC_SCRATCH_BYTES (16384u * 512u + 16384u * 32u + (256u << 10))
+int sph_derivatives_noalloc(const sph_params *p, int32_t precision, int64_t n, const double *r,
+                            const double *v, const double *m, const double *u, double *rho,
+                            double *rho_lr, double *t, double *pres, double *pco, double *vdot,
+                            double *udot, double *jq, void *stream);
+
 const char *sph_status_string(int status);
 int sph_version(void);
 

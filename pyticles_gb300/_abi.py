@@ -23,6 +23,7 @@ SPH_ESKIN = 7
 SPH_ECAPACITY = 8
 SPH_ENOTFOUND = 9
 PASSES = ("sort", "density", "heat", "tsum", "force")
+NOALLOC_MAX_PARTICLES = 16384
 
 STATUS_NAMES = {
     0: "SPH_OK", 1: "SPH_EINVAL", 2: "SPH_ENOMEM", 3: "SPH_ECELL_OVERFLOW",
@@ -172,6 +173,7 @@ def _declare(lib):
         "sph_kernels_per_step": [vp, P(c_i64)],
         "sph_sync": [vp],
         "sph_sim_status": [vp, c_i32, P(c_i32)],
+        "sph_derivatives_noalloc": [P(SphParams), c_i32, c_i64] + [vp] * 13,
         "sph_status_string": [ctypes.c_int],
         "sph_version": [],
     }
@@ -191,7 +193,7 @@ def exported_symbols():
             "sph_sim_export_pairs", "sph_last_pair_total", "sph_sim_diagnostics",
             "sph_get_tuning", "sph_set_tuning", "sph_prepare", "sph_profile",
             "sph_profile_read", "sph_kernels_per_step", "sph_sync", "sph_sim_status",
-            "sph_status_string", "sph_version"]
+            "sph_derivatives_noalloc", "sph_status_string", "sph_version"]
 
 
 def lib():

@@ -1284,3 +1284,38 @@ int sph_sim_status(sph_engine *e, int32_t id, int32_t *status) {
 }
 
 }  // extern "C"
+
+namespace sph {
+
+// Host-side tables of one simulation laid out on its own (cell offset 0,
+// particle offset 0): device constants, linear-cell -> Morton map and packed
+// cell coordinates, for callers that provide all device memory themselves.
+// cell_ratio as in sph_tuning; vmax bounds |v| for the cell slack.
+int single_sim_tables(const sph_params *p, int64_t n, double cell_ratio, double vmax,
+                      SimDev *dev, std::vector<int> *morton, std::vector<int> *cell_xyz) {
+    if (!p || !dev || !morton || !cell_xyz || n <= 0) return SPH_EINVAL;
+    sph_engine cfg;
+    cfg.group = *p;
+    cfg.dim = p->dim;
+    int st = validate_params(&cfg, p);
+    if (st != SPH_OK) return st;
+    Sim S;
+    S.prm = *p;
+    S.n = n;
+    S.vmax = vmax;
+    S.active = true;
+    make_grid(S, p->dim, cell_ratio);
+    S.cell_off = 0;
+    S.part_off = 0;
+    *dev = make_simdev(&cfg, S);
+    *morton = S.morton;
+    cell_xyz->assign(S.ncells, 0);
+    for (int r = 0; r < S.ncells; ++r) {
+        int lin = S.rank_lin[r];
+        int c0 = lin % S.nc[0], c1 = (lin / S.nc[0]) % S.nc[1], c2 = lin / (S.nc[0] * S.nc[1]);
+        (*cell_xyz)[r] = c0 | (c1 << 11) | (c2 << 22);
+    }
+    return SPH_OK;
+}
+
+}  // namespace sph
