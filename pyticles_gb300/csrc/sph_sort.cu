@@ -3,8 +3,8 @@
 //
 // Per step: k_bin (cell id + arrival rank, one atomic per particle) ->
 // exclusive scan of the cell counts -> k_scatter -> k_cellsort (within each
-// cell, order members by their previous slot, which makes the sort stable
-// and the whole step deterministic) -> k_permute (gather the FP64 state into
+// cell, order members by original particle index, which makes the layout and
+// every sum order a function of the state alone) -> k_permute (gather the FP64 state into
 // B and write the packed cell-local FP32/FP64 copies of the first evaluation).
 #include "sph_device.cuh"
 
@@ -141,8 +141,11 @@ void launch_scatter(const View &v, int np_a, cudaStream_t s) {
 }
 
 // One warp per cell: the rank of each member is the number of members with a
-// smaller previous slot, so the within-cell order no longer depends on the
-// order in which the atomics of k_bin arrived.
+// smaller original particle index (unique within a cell: a cell belongs to
+// one simulation).  The order inside a cell is therefore canonical -- it
+// depends neither on the order in which the atomics of k_bin arrived nor on
+// the layout the state had before -- so every pass sums its pairs in an order
+// that is a function of the positions alone.
 __global__ void k_cellsort(View v, int ncells) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -151,8 +154,9 @@ __global__ void k_cellsort(View v, int ncells) {
     int m = e - b;
     for (int x = lane; x < m; x += 32) {
         int val = v.order_tmp[b + x];
+        int key = v.a_id[val];
         int r = 0;
-        for (int t = 0; t < m; ++t) r += (v.order_tmp[b + t] < val) ? 1 : 0;
+        for (int t = 0; t < m; ++t) r += (v.a_id[v.order_tmp[b + t]] < key) ? 1 : 0;
         v.order[b + r] = val;
         v.cell_b[b + r] = warp;
     }

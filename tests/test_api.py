@@ -1,0 +1,184 @@
+"""The reference-facing API (pyticles_gb300 mirrors of particles.py,
+neighbour_list.py, forces.py, spam_complete_force.py, box.py), with the
+reference's own unit tests re-expressed (test/neighbour_list_test.py,
+test/force_test.py) and a driver in the shape of run_scripts/bspana_profile.py.
+Host-side logic runs on CPU; anything that evaluates runs on the GPU."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from pyticles_gb300 import (CohesiveSpamForce, MirrorBox, NeighbourList, ParticleSystem,
+                            PeriodicBox, SmoothParticleSystem, SortedVerletList, SpamComplete,
+                            SpamForce, VerletList, workloads)
+from pyticles_gb300.box import wrap_teleport
+from tests.golden_cases import load, params_of, rel_l2, sort_pairs
+
+
+# ---- host logic (CPU) ----
+
+def test_minimum_image_matches_reference_rule():
+    dr = np.array([3.0, -3.0, 0.4])
+    NeighbourList.minimum_image(dr, 5.0, 5.0, 1.0)
+    assert np.allclose(dr, [-2.0, 2.0, 0.4])
+    dr = np.array([2.5, -2.5, 0.5])   # exactly L/2: strict comparisons keep it
+    NeighbourList.minimum_image(dr, 5.0, 5.0, 1.0)
+    assert np.allclose(dr, [2.5, -2.5, 0.5])
+
+
+def test_ponder_rebuild_host_logic():
+    """test/neighbour_list_test.py:48-53: False after build, True once a
+    particle moved further than the tolerance."""
+    p = ParticleSystem(3, d=3, maxn=3)
+    nl = VerletList(p, cutoff=10, tolerance=2)
+    nl.r_old[:, :] = p.r[:, :]
+    nl.ponder_rebuild()
+    assert nl.rebuild_list is False
+    p.r[0, :] = (100.0, 100.0, 100.0)
+    nl.ponder_rebuild()
+    assert nl.rebuild_list is True
+
+
+def test_periodic_box_teleports():
+    r = np.array([[5.5, -0.1], [0.0, 5.0], [-2.0, 7.0]])
+    wrap_teleport(r, (5.0, 5.0))
+    assert np.array_equal(r, [[0.0, 5.0], [0.0, 5.0], [5.0, 0.0]])
+
+
+def test_mirror_box_is_refused_by_the_engine():
+    p = SmoothParticleSystem(4, d=2, maxn=4)
+    nl = VerletList(p, cutoff=1.0, tolerance=0.0)
+    p.nlists.append(nl)
+    p.forces.append(SpamComplete(p, nl))
+    assert isinstance(p.box, MirrorBox)
+    with pytest.raises(NotImplementedError):
+        p.engine_params(1e-3)
+
+
+def test_engine_params_from_reference_objects():
+    box = PeriodicBox(xmax=20, ymax=20, zmax=1)
+    p = SmoothParticleSystem(400, d=2, maxn=400, hshort=3.0, hlong=6.0, simbox=box,
+                             integrator="ieuler", thermostat=True, thermostat_temp=0.4)
+    nl = VerletList(p, cutoff=6.0, tolerance=0.5)
+    p.nlists.append(nl)
+    p.nl_default = nl
+    p.forces.append(SpamComplete(p, nl, eta=0.8, zeta=0.2))
+    prm = p.engine_params(2e-3)
+    assert (prm.dim, prm.kernel, prm.viscosity, prm.thermostat) == (2, 2, 1, 1)
+    assert (prm.visc_alpha, prm.visc_beta, prm.cutoff, prm.tolerance) == (0.8, 0.2, 6.0, 0.5)
+    assert (prm.h_short, prm.h_long, prm.dt, prm.thermostat_temp) == (3.0, 6.0, 2e-3, 0.4)
+    p.forces = [SpamForce(p, nl), CohesiveSpamForce(p, nl)]
+    assert p.engine_params(1e-3).viscosity == 0
+
+
+# ---- evaluation (GPU) ----
+
+@pytest.mark.gpu
+def test_reference_nlist_tests():
+    """test/neighbour_list_test.py:8-53 through the GPU pair export."""
+    p = ParticleSystem(3, d=3, maxn=3)
+    p.r[0, :] = (0.0, 0.0, 0.0)
+    p.r[1, :] = (1.0, 0.0, 0.0)
+    p.r[2, :] = (0.0, 0.0, 1.0)
+    nl = NeighbourList(p)
+    nl.build()
+    nl.separations()
+    k = nl.find_pair(0, 1)
+    assert nl.rij[k] == 1.0
+    nl2 = VerletList(p, cutoff=10, tolerance=2)
+    nl2.build()
+    nl2.compress()
+    nl2.separations()
+    assert nl2.rij[0] == 1.0
+    nl2.ponder_rebuild()
+    assert nl2.rebuild_list is False
+    p.r[0, :] = (100.0, 100.0, 100.0)
+    nl2.ponder_rebuild()
+    assert nl2.rebuild_list is True
+    nl.close()
+    nl2.close()
+
+
+@pytest.mark.gpu
+def test_sorted_verlet_list_matches_reference_pairs():
+    g = load("lucy2d_400")
+    box = PeriodicBox(xmax=20, ymax=20, zmax=1)
+    p = SmoothParticleSystem(400, d=2, maxn=400, simbox=box)
+    p.r[:] = g["r0"]
+    p.v[:] = g["v0"]
+    nl = SortedVerletList(p, cutoff=6.0, tolerance=0.0)
+    nl.build()
+    got, _ = sort_pairs(nl.iap)
+    ref, _ = sort_pairs(g["iap"])
+    assert np.array_equal(got, ref)
+    assert np.all(np.diff(nl.rsq) <= 0)   # descending separation
+    nl.close()
+
+
+def bspana_like(g, precision, steps):
+    """run_scripts/bspana_profile.py:39-61 with the periodic box."""
+    box = PeriodicBox(xmax=float(g["box"][0]), ymax=float(g["box"][1]), zmax=1)
+    n = len(g["r0"])
+    p = SmoothParticleSystem(n, d=2, maxn=n, hshort=float(g["h_short"]),
+                             hlong=float(g["h_long"]), simbox=box, integrator="ieuler",
+                             precision=precision)
+    p.r[:] = g["r0"]
+    p.v[:] = g["v0"]
+    p.m[:] = g["m"]
+    p.u[:] = g["u0"]
+    nl = VerletList(p, cutoff=float(g["cutoff"]), tolerance=0.0)
+    p.nlists.append(nl)
+    p.nl_default = nl
+    p.forces.append(SpamComplete(p, nl, eta=0.0, zeta=0.0))
+    for _ in range(steps):
+        p.update(float(g["dt"]))
+    return p
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 5e-6)])
+def test_update_matches_reference_trajectory(precision, tol):
+    g = load("lucy2d_400")
+    p = bspana_like(g, precision, int(g["steps"]))
+    assert rel_l2(p.r, g["r_final"]) < tol
+    assert rel_l2(p.v, g["v_final"]) < tol
+    assert rel_l2(p.u, g["u_final"]) < tol
+    for k in ("rho", "rho_lr", "t", "p", "pco", "vdot", "udot"):
+        assert rel_l2(getattr(p, k), g["after_" + k]) < tol, k
+    assert p.steps == int(g["steps"])
+    p.close()
+
+
+@pytest.mark.gpu
+def test_force_apply_writes_reference_arrays():
+    """SpamComplete.apply / p.derivatives() fill rho, p, pco, t, vdot, udot
+    (spam_complete_force.py:171-183) with one evaluation."""
+    g = load("lucy2d_1024")
+    p = bspana_like(g, "fp64", 0)
+    p.forces[0].apply()
+    for k in ("rho", "rho_lr", "t", "p", "pco", "vdot", "udot"):
+        assert rel_l2(getattr(p, k), g["ev_" + k]) < 1e-12, k
+    p.close()
+
+
+@pytest.mark.gpu
+def test_run_many_steps_equals_update_loop():
+    prm, r, v, m, T0 = workloads.config_2d(24, 77, viscosity=True)
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    out = []
+    for mode in ("update", "run"):
+        box = PeriodicBox(xmax=24, ymax=24, zmax=1)
+        p = SmoothParticleSystem(len(r), d=2, maxn=len(r), hshort=3.0, hlong=6.0, simbox=box,
+                                 precision="mixed")
+        p.r[:], p.v[:], p.m[:], p.u[:] = r, v, m, u
+        nl = VerletList(p, cutoff=6.0, tolerance=0.0)
+        p.nlists.append(nl)
+        p.forces.append(SpamComplete(p, nl))
+        if mode == "update":
+            for _ in range(4):
+                p.update(1e-3)
+        else:
+            p.run(1e-3, 4)
+        out.append((p.r.copy(), p.v.copy(), p.u.copy()))
+        p.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
