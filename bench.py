@@ -156,12 +156,20 @@ def gpu_initial_energy(prm, r, v, m, T0, stream):
     return T0 * prm.kbdash - prm.adash * rho
 
 
-def run_timed(prm, r, v, m, u, precision, steps, warmup, torch, stream, profile=True):
+def run_timed(prm, r, v, m, u, precision, steps, warmup, torch, stream, profile=True,
+              knobs=None, sims=None):
     """Device time of `steps` steps captured in one graph, with per-pass
-    CUDA events recorded inside the graph."""
+    CUDA events recorded inside the graph.  `sims` [(params, r, v, m, u)]
+    replaces the single simulation for batched runs."""
     from pyticles_gb300 import Engine
-    e = Engine(prm, precision, max_particles=len(r), stream=stream.cuda_stream)
-    s = e.add(prm, r, v, m, u)
+    sims = sims or [(prm, r, v, m, u)]
+    total = sum(len(x[1]) for x in sims)
+    e = Engine(sims[0][0], precision, max_particles=total, max_sims=len(sims),
+               stream=stream.cuda_stream)
+    for sm in sims:
+        e.add(*sm)
+    if knobs:
+        e.set_tuning(**knobs)
     e.set_tuning(steps_per_graph=max(1, steps), use_graph=1)
     e.advance(max(1, warmup))
     e.sync()
@@ -183,6 +191,62 @@ def run_timed(prm, r, v, m, u, precision, steps, warmup, torch, stream, profile=
     e.profile(False)
     e.close()
     return ms, pairs, passes, kps
+
+
+def batched_workload(nsims, ramp_steps=500):
+    """512 independent 2D simulations: N log-uniform in [256, 65536], T in
+    [0.2, 1.2], areal density in [0.4, 0.9], thermostat quench T -> T/2 over
+    500 steps; u0 = k_B T0 - a n (n the number density)."""
+    from pyticles_gb300 import workloads
+    sims = []
+    for prm, r, v, m, T0 in workloads.batched_2d(nsims, seed_base=4000,
+                                                  ramp_steps=ramp_steps):
+        dens = 1.0 / (prm.box[0] / math.sqrt(len(r))) ** 2
+        u = workloads.vdw_energy(np.full(len(r), dens), T0)
+        sims.append((prm, r, v, m, u))
+    return sims
+
+
+def fluid3d_workload(side):
+    """3D fluid at number density 0.7 (side^3 particles), cubic spline with
+    support radii 2.735 / 5.148 (about 60 / 400 neighbours), viscosity, heat
+    flux."""
+    from pyticles_gb300 import workloads
+    prm, r, v, m, T0 = workloads.config_3d(side, 3000)
+    u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
+    return [(prm, r, v, m, u)]
+
+
+def timed_workload(sims, steps, warmup, torch, stream, tune=True):
+    """Autotunes on a sample, then times `steps` graph-captured steps."""
+    knobs = None
+    if tune:
+        from pyticles_gb300 import autotune
+        knobs, _ = autotune.tune(sims[0][0], "mixed",
+                                 autotune.sample_sims(sims, 1 << 20), steps=3, warmup=2)
+    ms, pairs, passes, kps = run_timed(None, None, None, None, None, "mixed", steps, warmup,
+                                       torch, stream, knobs=knobs, sims=sims)
+    n = sum(len(x[1]) for x in sims)
+    return {"sims": len(sims), "n": n, "steps": steps, "ms_per_step": ms / steps,
+            "pairs_per_eval": pairs, "value": pairs * 2 * steps / (ms * 1e-3),
+            "unit": UNIT, "tuning": knobs,
+            "pass_ms_per_step": {k: p["ms"] / steps for k, p in passes.items()}}
+
+
+def serve_window(njobs, time_limit, seed=5000):
+    """A fixed Poisson arrival window of the served workload (20 jobs/s, 70%
+    2D, N log-uniform in [1e3, 1e6], steps uniform in [100, 5000]), served in
+    real time within an HBM budget; jobs still running at the time limit are
+    reported as unfinished."""
+    from pyticles_gb300 import serve
+    jobs = serve.poisson_jobs(njobs, seed=seed)
+    offered = sum(j.n * (56.5 if j.dim == 2 else 200.0) * 2 * j.steps for j in jobs)
+    srv = serve.Server(60e9, chunk=25, max_sims=256)
+    rep = srv.run(jobs, realtime=True, time_limit=time_limit)
+    srv.close()
+    rep["offered_pair_interactions_per_s"] = offered / max(rep["arrival_window_s"], 1e-9)
+    rep["time_limit_s"] = time_limit
+    return rep
 
 
 def run_e2e(prm, r, v, m, u, steps, torch, stream):
@@ -274,6 +338,14 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched, 3D and served sub-workloads")
+    ap.add_argument("--batched-sims", type=int, default=512)
+    ap.add_argument("--batched-steps", type=int, default=100)
+    ap.add_argument("--side3d", type=int, default=128)
+    ap.add_argument("--steps3d", type=int, default=20)
+    ap.add_argument("--serve-jobs", type=int, default=12)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -295,11 +367,13 @@ def main():
     n = len(r)
     hbm_peak, peak_kind, sm_max = measured_peaks()
 
+    from pyticles_gb300 import autotune
+    knobs, tune_table = autotune.tune(prm, "mixed", [(prm, r, v, m, u)], steps=3, warmup=2)
     if dist:
         dist.barrier()
     with ClockSampler(local) as clocks:
         ms, pairs, passes, kps = run_timed(prm, r, v, m, u, "mixed", args.steps, args.warmup,
-                                           torch, stream)
+                                           torch, stream, knobs=knobs)
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -313,7 +387,7 @@ def main():
 
     # plain FP64 GPU step on the same workload
     ms64, pairs64, _, _ = run_timed(prm, r, v, m, u, "fp64", args.fp64_steps, 3, torch, stream,
-                                    profile=False)
+                                    profile=False, knobs=knobs)
     fp64_value = pairs64 * 2 * args.fp64_steps / (ms64 * 1e-3)
 
     # end to end through the C ABI with pinned host buffers
@@ -330,6 +404,14 @@ def main():
     flops = FLOPS_FORCE[2] * pairs / (avg_ms * 1e-3) / 1e12
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
     total_pass_ms = sum(p["ms"] for p in passes.values())
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras["batched"] = timed_workload(batched_workload(args.batched_sims),
+                                           args.batched_steps, 3, torch, stream)
+        extras["fluid3d"] = timed_workload(fluid3d_workload(args.side3d), args.steps3d, 3,
+                                           torch, stream)
+        extras["serve"] = serve_window(args.serve_jobs, args.serve_seconds)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -358,6 +440,7 @@ def main():
             "l2": f"working set ~{working_set / 1e6:.0f} MB per step > 129 MB L2 (no flush)",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
             "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value,
+            "tuning": knobs,
             "pass_ms_per_step": {k: p["ms"] / args.steps for k, p in passes.items()},
         },
         "roofline": {
@@ -378,6 +461,11 @@ def main():
         "gpu_launches": kps * args.steps,
         "clocks": clocks.summary(),
     }
+    if extras:
+        sv = extras.get("serve", {})
+        line["latency"] = {"p50_s": sv.get("latency_p50_s"), "p99_s": sv.get("latency_p99_s"),
+                           "workload": "served Poisson window (see workloads.serve)"}
+        line["workloads"] = extras
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

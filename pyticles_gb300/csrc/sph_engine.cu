@@ -50,6 +50,7 @@ struct Sim {
     int cell_off = 0;
     int part_off = 0;          // B layout
     int a_off = 0;             // contiguous range in A
+    int chunk_first = 0, nchunk = 0;
     int64_t steps = 0;
     double vmax = 0.0;
 };
@@ -292,6 +293,8 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
     d.ncells = S.ncells;
     d.part_off = S.part_off;
     d.n = (int)S.n;
+    d.chunk_first = S.chunk_first;
+    d.nchunk = S.nchunk;
     d.thermostat = p.thermostat;
     d.thr = p.cutoff * p.cutoff + p.tolerance * p.tolerance;
     d.hs = p.h_short;
@@ -454,6 +457,8 @@ int relayout(sph_engine *e) {
             int c[3] = {lin % S.nc[0], (lin / S.nc[0]) % S.nc[1], lin / (S.nc[0] * S.nc[1])};
             cxyz[S.cell_off + r] = c[0] | (c[1] << 11) | (c[2] << 22);
         }
+        S.chunk_first = (int)csim.size();
+        S.nchunk = (int)((S.n + 1023) / 1024);
         for (int64_t b = 0; b < S.n; b += 1024) {
             csim.push_back((int)(&S - &e->sims[0]));
             cstart.push_back(S.part_off + (int)b);

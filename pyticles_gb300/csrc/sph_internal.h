@@ -45,6 +45,7 @@ struct SimDev {
     int active;
     int cell_off, ncells;
     int part_off, n;        // range in B (sorted) order
+    int chunk_first, nchunk;  // this simulation's reduction chunks
     int thermostat;
     double thr;             // cutoff^2 + tolerance^2 (FP64, the reference's value)
     double hs, hl;          // smoothing lengths

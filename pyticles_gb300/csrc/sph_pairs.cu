@@ -522,8 +522,7 @@ __global__ void k_tsum_sims(View v, int nsims) {
     v.steps[s] = done;
     if (!S.thermostat) return;
     double sum = 0.0;
-    for (int c = 0; c < v.nchunks; ++c)
-        if (v.chunk_sim[c] == s) sum += v.tsum_part[c];
+    for (int c = S.chunk_first; c < S.chunk_first + S.nchunk; ++c) sum += v.tsum_part[c];
     double tav = sum / (double)S.n;
     double target = S.T0;
     if (S.ramp > 0) {

@@ -1,0 +1,261 @@
+"""Continuous-batching SPH job server.
+
+Jobs -- independent 2D or 3D simulations with their own size, parameters and
+step count -- arrive over time.  Each dimension group (2D: Lucy kernel,
+viscosity; 3D: cubic spline, viscosity, heat flux) owns one engine on its own
+CUDA stream, whose particle capacity is its share of an HBM budget.  A job is
+admitted into its group's engine as soon as a simulation slot and enough
+particle capacity are free (first fit over the waiting queue), joins the
+engine's next chunk of steps, and leaves -- state copied back, capacity
+released -- when its steps are done.  The 2D and 3D engines run their chunks
+concurrently.  Per job: queueing delay (admission - arrival), service time
+(completion - admission) and latency (completion - arrival).
+
+Failure handling: a job larger than its group's whole capacity is rejected at
+admission; a job whose state turns non-finite (or whose particles outrun the
+cell slack) is retired with that error after the chunk in which it happened,
+and the other jobs continue unaffected (their particles never interact).
+"""
+import collections
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .engine import Engine
+from .workloads import lattice_system, rng_for, vdw_energy
+
+# Bytes of engine state per particle (mirrors alloc_particles in
+# csrc/sph_engine.cu): FP64 state A/B, evaluation positions/velocities, cell
+# origins (3 axes x 8 arrays x 8 B), rates and factors in the pass precision,
+# ids and sort scratch, packed vectors, staging.
+def bytes_per_particle(precision="mixed", integrator="ieuler"):
+    rs = 4 if precision == "mixed" else 8
+    v4 = 4 * rs
+    b = 3 * 8 * 8 + 9 * rs + 5 * 8 + 9 * 4 + 6 * v4 + 10 * rs + 4 * 8
+    if integrator == "rk4":
+        b += 7 * 8
+    return b
+
+
+@dataclass
+class Job:
+    job_id: int
+    arrival: float            # seconds after the server starts
+    dim: int
+    steps: int
+    params: object            # SphParams
+    r: np.ndarray
+    v: np.ndarray
+    m: np.ndarray
+    u: np.ndarray
+    visible: float = None     # server time at which the job was seen
+    admitted: float = None
+    finished: float = None
+    result: tuple = None
+    error: str = None
+    sim: int = None
+    remaining: int = 0
+    work: float = 0.0         # pair-interactions done
+
+    @property
+    def n(self):
+        return len(self.r)
+
+
+def make_job(job_id, arrival, dim, n, steps, seed, precision_kw=None):
+    """A job of the served workload: 2D van der Waals fluid (spacing 1, Lucy
+    h = 3, 6, viscosity) or 3D fluid at density 0.7 (cubic spline, support
+    2.735 / 5.148, viscosity, heat flux), about n particles, T ~ U[0.4, 0.8]."""
+    rng = rng_for(seed)
+    temp = rng.uniform(0.4, 0.8)
+    if dim == 2:
+        side = max(16, int(round(math.sqrt(n))))
+        prm, r, v, m, T0 = lattice_system(side, 2, spacing=1.0, jitter=0.1, temperature=temp,
+                                          seed=seed, kernel="lucy", h_short=3.0, h_long=6.0,
+                                          viscosity=True, dt=1e-3)
+        rho0 = 1.0
+    else:
+        dens = 0.7
+        side = max(10, int(round(n ** (1.0 / 3.0))))
+        prm, r, v, m, T0 = lattice_system(side, 3, spacing=dens ** (-1.0 / 3.0), jitter=0.1,
+                                          temperature=temp, seed=seed, kernel="cubic",
+                                          h_short=2.735 / 2, h_long=5.148 / 2, viscosity=True,
+                                          heat_flux=True, dt=1e-3)
+        rho0 = dens
+    u = vdw_energy(np.full(len(r), rho0), T0)
+    return Job(job_id, arrival, dim, steps, prm, r, v, m, u)
+
+
+def poisson_jobs(njobs, rate=20.0, frac2d=0.7, n_lo=1e3, n_hi=1e6, steps_lo=100,
+                 steps_hi=5000, seed=5000):
+    """The served workload: Poisson arrivals at `rate` jobs/s, 2D with
+    probability frac2d, N log-uniform in [n_lo, n_hi], steps uniform in
+    [steps_lo, steps_hi]; seeded."""
+    rng = rng_for(seed)
+    t = 0.0
+    jobs = []
+    for k in range(njobs):
+        t += rng.exponential(1.0 / rate)
+        dim = 2 if rng.uniform() < frac2d else 3
+        n = int(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi))))
+        steps = int(rng.integers(steps_lo, steps_hi + 1))
+        jobs.append(make_job(k, t, dim, n, steps, seed + 1 + k))
+    return jobs
+
+
+class Group:
+    """One engine (one dimension group) and its jobs."""
+
+    def __init__(self, dim, params, capacity, max_sims, precision, chunk, engine_factory,
+                 stream):
+        self.dim = dim
+        self.capacity = int(capacity)
+        self.max_sims = max_sims
+        self.chunk = chunk
+        self.engine = engine_factory(params, precision, self.capacity, max_sims, stream)
+        self.engine.set_tuning(steps_per_graph=chunk, use_graph=1)
+        self.active = {}          # sim id -> job
+        self.live = 0
+
+    def fits(self, job):
+        return len(self.active) < self.max_sims and self.live + job.n <= self.capacity
+
+    def admit(self, job, now):
+        job.sim = self.engine.add(job.params, job.r, job.v, job.m, job.u)
+        job.admitted = now
+        job.remaining = job.steps
+        self.active[job.sim] = job
+        self.live += job.n
+
+    def launch(self):
+        """Enqueues one chunk (asynchronous); returns its step count."""
+        if not self.active:
+            return 0
+        steps = min(self.chunk, min(j.remaining for j in self.active.values()))
+        self.engine.advance(steps)
+        return steps
+
+    def finish(self, steps, now):
+        """Waits for the chunk, accounts work and retires finished or failed
+        jobs.  Returns the retired jobs."""
+        if steps == 0:
+            return []
+        failed = set()
+        try:
+            self.engine.sync()
+        except _abi.SphError:
+            for sim, job in self.active.items():
+                code = self.engine.status(sim)
+                if code:
+                    job.error = _abi.STATUS_NAMES.get(code, str(code))
+                    failed.add(sim)
+        pairs = self.engine.last_pair_total()
+        total = sum(j.n for j in self.active.values())
+        done = []
+        for sim, job in list(self.active.items()):
+            job.remaining -= steps
+            job.work += 2.0 * steps * pairs * (job.n / total)
+            if sim in failed or job.remaining <= 0:
+                if sim not in failed:
+                    job.result = self.engine.get_state(sim)
+                job.finished = now()
+                self.engine.remove(sim)
+                del self.active[sim]
+                self.live -= job.n
+                done.append(job)
+        return done
+
+    def close(self):
+        self.engine.close()
+
+
+def default_engine_factory(params, precision, capacity, max_sims, stream):
+    return Engine(params, precision, max_particles=capacity, max_sims=max_sims, stream=stream)
+
+
+class Server:
+    """Continuous batching over a 2D and a 3D engine within an HBM budget."""
+
+    def __init__(self, hbm_budget_bytes, precision="mixed", chunk=25, max_sims=256,
+                 share_2d=0.6, engine_factory=default_engine_factory, clock=time.perf_counter,
+                 streams=None, group_params=None):
+        self.precision = precision
+        self.chunk = chunk
+        self.clock = clock
+        bpp = bytes_per_particle(precision)
+        caps = {2: hbm_budget_bytes * share_2d / bpp, 3: hbm_budget_bytes * (1 - share_2d) / bpp}
+        if group_params is None:
+            group_params = {2: make_job(0, 0.0, 2, 256, 1, 1).params,
+                            3: make_job(0, 0.0, 3, 1000, 1, 2).params}
+        streams = streams or {2: None, 3: None}
+        self.groups = {d: Group(d, group_params[d], caps[d], max_sims, precision, chunk,
+                                engine_factory, streams[d]) for d in (2, 3)}
+        self.rejected = []
+
+    def run(self, jobs, realtime=True, time_limit=None):
+        """Serves `jobs`.  With realtime, a job becomes visible at its arrival
+        time on the server clock; otherwise all jobs are visible at once.
+        Latency and queueing delay are measured from when a job is visible."""
+        jobs = sorted(jobs, key=lambda j: j.arrival)
+        pending = collections.deque(jobs)
+        waiting = []
+        completed = []
+        t0 = self.clock()
+        now = lambda: self.clock() - t0
+        while pending or waiting or any(g.active for g in self.groups.values()):
+            t = now()
+            if time_limit is not None and t > time_limit:
+                break
+            while pending and (not realtime or pending[0].arrival <= t):
+                job = pending.popleft()
+                job.visible = t
+                waiting.append(job)
+            # admission: first fit in arrival order
+            still = []
+            for job in waiting:
+                g = self.groups[job.dim]
+                if job.n > g.capacity:
+                    job.error = "rejected: larger than the group's HBM budget"
+                    job.finished = t
+                    self.rejected.append(job)
+                elif g.fits(job):
+                    g.admit(job, t)
+                else:
+                    still.append(job)
+            waiting = still
+            if not any(g.active for g in self.groups.values()):
+                if pending:
+                    wait = pending[0].arrival - now()
+                    if realtime and wait > 0:
+                        time.sleep(min(wait, 0.05))
+                continue
+            launched = {d: g.launch() for d, g in self.groups.items()}
+            for d, g in self.groups.items():
+                completed.extend(g.finish(launched[d], now))
+        makespan = now()
+        return self.report(completed, makespan, jobs)
+
+    def report(self, completed, makespan, jobs):
+        ok = [j for j in completed if j.error is None]
+        lat = np.array([j.finished - j.visible for j in ok]) if ok else np.zeros(1)
+        queue = np.array([j.admitted - j.visible for j in ok]) if ok else np.zeros(1)
+        service = np.array([j.finished - j.admitted for j in ok]) if ok else np.zeros(1)
+        work = sum(j.work for j in completed)
+        window = max(j.arrival for j in jobs) if jobs else 0.0
+        return {
+            "jobs": len(jobs), "completed": len(ok),
+            "failed": len([j for j in completed if j.error]), "rejected": len(self.rejected),
+            "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99)),
+            "queue_p50_s": float(np.percentile(queue, 50)),
+            "service_p50_s": float(np.percentile(service, 50)),
+            "makespan_s": makespan, "arrival_window_s": window,
+            "achieved_pair_interactions_per_s": work / makespan if makespan > 0 else 0.0,
+        }
+
+    def close(self):
+        for g in self.groups.values():
+            g.close()

@@ -1,0 +1,189 @@
+"""Continuous-batching server: admission, retirement, failure isolation and
+latency accounting on CPU with a fake engine; a real 2D + 3D run on the GPU
+where each job's result equals the same job run alone."""
+import numpy as np
+import pytest
+
+from pyticles_gb300 import _abi, serve
+from pyticles_gb300.serve import Job, Server, make_job
+
+
+class FakeEngine:
+    """Records calls; a simulation's 'state' is the number of steps it ran."""
+
+    def __init__(self, params, precision, capacity, max_sims, stream):
+        self.capacity = capacity
+        self.sims = {}
+        self.next_id = 0
+        self.fail = set()
+        self.err = False
+        self.log = []
+
+    def set_tuning(self, **kw):
+        pass
+
+    def add(self, prm, r, v, m, u):
+        sid = self.next_id
+        self.next_id += 1
+        self.sims[sid] = {"n": len(r), "steps": 0, "nan": bool(np.isnan(u).any())}
+        self.log.append(("add", sid))
+        return sid
+
+    def remove(self, sid):
+        self.log.append(("remove", sid))
+        del self.sims[sid]
+
+    def advance(self, k):
+        self.log.append(("advance", k, tuple(sorted(self.sims))))
+        for s in self.sims.values():
+            s["steps"] += k
+            if s["nan"]:
+                self.err = True
+
+    def sync(self):
+        if self.err:
+            self.err = False
+            raise _abi.SphError(_abi.SPH_ENAN, "device")
+
+    def status(self, sid):
+        return _abi.SPH_ENAN if self.sims[sid]["nan"] else 0
+
+    def get_state(self, sid):
+        return (self.sims[sid]["steps"],)
+
+    def last_pair_total(self):
+        return sum(s["n"] for s in self.sims.values()) * 10
+
+    def close(self):
+        pass
+
+
+def fake_job(k, arrival, dim, n, steps, nan=False):
+    u = np.zeros(n)
+    if nan:
+        u[0] = np.nan
+    return Job(k, arrival, dim, steps, None, np.zeros((n, dim)), np.zeros((n, dim)),
+               np.ones(n), u)
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        self.t += 0.001
+        return self.t
+
+
+def fake_server(budget_particles, chunk=10, max_sims=4):
+    bpp = serve.bytes_per_particle("mixed")
+    return Server(budget_particles * bpp / 0.5, chunk=chunk, max_sims=max_sims, share_2d=0.5,
+                  engine_factory=FakeEngine, clock=FakeClock(), group_params={2: None, 3: None})
+
+
+def test_jobs_run_exactly_their_steps_and_leave():
+    srv = fake_server(1000)
+    jobs = [fake_job(0, 0.0, 2, 100, 25), fake_job(1, 0.0, 2, 200, 40),
+            fake_job(2, 0.0, 3, 50, 7)]
+    rep = srv.run(jobs, realtime=False)
+    assert rep["completed"] == 3 and rep["failed"] == 0
+    assert [j.result[0] for j in jobs] == [25, 40, 7]
+    assert not srv.groups[2].active and srv.groups[2].live == 0
+
+
+def test_admission_waits_for_capacity_and_slots():
+    srv = fake_server(300, chunk=5, max_sims=2)
+    jobs = [fake_job(0, 0.0, 2, 200, 10), fake_job(1, 0.0, 2, 200, 10),
+            fake_job(2, 0.0, 2, 50, 10), fake_job(3, 0.0, 2, 50, 10)]
+    srv.run(jobs, realtime=False)
+    adv = [e for e in srv.groups[2].engine.log if e[0] == "advance"]
+    # capacity 300: job 1 (200) cannot join job 0 (200); first fit lets job 2 in
+    assert all(len(e[2]) <= 2 for e in adv)
+    assert jobs[1].admitted > jobs[2].admitted
+    assert all(j.result[0] == 10 for j in jobs)
+
+
+def test_oversized_job_is_rejected_not_run():
+    srv = fake_server(100)
+    jobs = [fake_job(0, 0.0, 2, 500, 10), fake_job(1, 0.0, 2, 20, 10)]
+    rep = srv.run(jobs, realtime=False)
+    assert rep["rejected"] == 1 and jobs[0].error.startswith("rejected")
+    assert jobs[1].result == (10,)
+
+
+def test_failed_job_is_retired_and_others_continue():
+    srv = fake_server(1000, chunk=5)
+    jobs = [fake_job(0, 0.0, 2, 100, 20), fake_job(1, 0.0, 2, 100, 20, nan=True),
+            fake_job(2, 0.0, 2, 100, 20)]
+    rep = srv.run(jobs, realtime=False)
+    assert jobs[1].error == "SPH_ENAN" and jobs[1].result is None
+    assert jobs[0].result == (20,) and jobs[2].result == (20,)
+    assert rep["failed"] == 1 and rep["completed"] == 2
+
+
+def test_latency_accounting_uses_arrival_times():
+    srv = fake_server(1000, chunk=10)
+    jobs = [fake_job(0, 0.0, 2, 10, 10), fake_job(1, 0.5, 2, 10, 10)]
+    rep = srv.run(jobs, realtime=False)
+    for j in jobs:
+        assert j.finished >= j.admitted >= j.visible
+    assert rep["arrival_window_s"] == 0.5
+    assert rep["latency_p99_s"] >= rep["latency_p50_s"] > 0
+
+
+def test_poisson_workload_shape():
+    jobs = serve.poisson_jobs(60, n_lo=1e3, n_hi=2e3, steps_lo=100, steps_hi=200, seed=9)
+    arr = np.array([j.arrival for j in jobs])
+    assert np.all(np.diff(arr) > 0)
+    assert 1.0 < arr[-1] < 6.0                      # ~3 s at 20 jobs/s
+    frac2d = np.mean([j.dim == 2 for j in jobs])
+    assert 0.5 < frac2d < 0.9
+    assert all(100 <= j.steps <= 200 for j in jobs)
+    assert all(j.params.dim == j.dim for j in jobs)
+
+
+# ---- on the GPU ----
+
+def small_jobs(seed=77):
+    specs = [(2, 900, 30), (3, 1000, 20), (2, 1600, 45), (2, 400, 15), (3, 1331, 25),
+             (2, 2500, 35)]
+    return [make_job(k, 0.01 * k, d, n, s, seed + k) for k, (d, n, s) in enumerate(specs)]
+
+
+def run_alone(job, precision="mixed"):
+    from pyticles_gb300 import Engine
+    with Engine(job.params, precision, max_particles=job.n) as e:
+        s = e.add(job.params, job.r, job.v, job.m, job.u)
+        e.advance(job.steps)
+        e.sync()
+        return e.get_state(s)
+
+
+@pytest.mark.gpu
+def test_served_results_equal_alone():
+    jobs = small_jobs()
+    srv = Server(2e9, chunk=10, max_sims=8)
+    rep = srv.run(jobs, realtime=False)
+    srv.close()
+    assert rep["completed"] == len(jobs) and rep["failed"] == 0
+    assert rep["latency_p99_s"] >= rep["latency_p50_s"] > 0
+    for job in jobs:
+        alone = run_alone(job)
+        for a, b in zip(alone, job.result):
+            assert np.array_equal(a, b), job.job_id
+
+
+@pytest.mark.gpu
+def test_nan_job_does_not_disturb_the_mix():
+    jobs = small_jobs(seed=91)
+    bad = make_job(99, 0.0, 2, 900, 30, 1234)
+    bad.u[5] = np.nan
+    srv = Server(2e9, chunk=10, max_sims=8)
+    srv.run(jobs + [bad], realtime=False)
+    srv.close()
+    assert bad.error == "SPH_ENAN"
+    for job in jobs:
+        assert job.error is None
+        alone = run_alone(job)
+        for a, b in zip(alone, job.result):
+            assert np.array_equal(a, b), job.job_id
