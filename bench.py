@@ -338,6 +338,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="use the engine's default knobs (stable launch counts for profilers)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched, 3D and served sub-workloads")
     ap.add_argument("--batched-sims", type=int, default=512)
@@ -368,7 +370,9 @@ def main():
     hbm_peak, peak_kind, sm_max = measured_peaks()
 
     from pyticles_gb300 import autotune
-    knobs, tune_table = autotune.tune(prm, "mixed", [(prm, r, v, m, u)], steps=3, warmup=2)
+    knobs = None
+    if not args.no_tune:
+        knobs, _ = autotune.tune(prm, "mixed", [(prm, r, v, m, u)], steps=3, warmup=2)
     if dist:
         dist.barrier()
     with ClockSampler(local) as clocks:
