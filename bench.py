@@ -378,15 +378,8 @@ def main():
     with ClockSampler(local) as clocks:
         ms, pairs, passes, kps = run_timed(prm, r, v, m, u, "mixed", args.steps, args.warmup,
                                            torch, stream, knobs=knobs)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        w = torch.tensor([float(pairs)], device="cuda")
-        dist.all_reduce(w, op=dist.ReduceOp.SUM)
-        pairs_all = float(w.item())
-    else:
-        pairs_all = float(pairs)
+    from pyticles_gb300 import replicas
+    ms, pairs_all = replicas.combine(ms, pairs, dist, device="cuda")
     value = pairs_all * 2 * args.steps / (ms * 1e-3)
 
     # plain FP64 GPU step on the same workload

@@ -128,6 +128,10 @@ int sph_sim_get_properties(sph_engine *e, int32_t sim_id, double *rho, double *r
                            double *t, double *p, double *pco, double *vdot, double *udot,
                            double *jq, int32_t mem);
 int sph_sim_count(sph_engine *e, int32_t sim_id, int64_t *n);
+/* Steps a simulation has taken (the thermostat ramp position); set it when
+ * resuming from a checkpoint (particles.py:110 `steps`). */
+int sph_sim_steps(sph_engine *e, int32_t sim_id, int64_t *steps);
+int sph_sim_set_steps(sph_engine *e, int32_t sim_id, int64_t steps);
 
 /* Advances every simulation by nsteps steps of its integrator, applying
  * the periodic box after each step and the thermostat when enabled. */
@@ -202,6 +206,21 @@ int sph_kernels_per_step(sph_engine *e, int64_t *n);
 int sph_sync(sph_engine *e);
 /* Per-simulation device error word (0 = ok). */
 int sph_sim_status(sph_engine *e, int32_t sim_id, int32_t *status);
+
+/* Headless splash rendering (interpolate.splash_map_2d / splash_map_3d,
+ * interpolate.py:39-149; replaces the GL path of
+ * SmoothParticleView.render_density, pview.py:483-519).  mode 2: particles
+ * of a 2D system onto the (x, y) grid; mode 3: particles of a 3D system onto
+ * the plane at height z.  r is n x r_cols row-major; m, rho, a, h have
+ * length n (a may be NULL: a = rho); x (nx) and y (ny) are the regular pixel
+ * coordinates; bounds = {xmin, xmax, ymin, ymax} is host memory in both
+ * modes; Z receives nx x ny values, Z[ix * ny + iy].  Each particle adds
+ * a m / rho W_lucy(s, h) to the pixels of its box whose minimum-imaged
+ * distance s is below the cutoff.  mem tags all other pointers. */
+int sph_splash_map(int32_t mode, int64_t n, const double *r, int32_t r_cols, const double *m,
+                   const double *rho, const double *a, const double *h, int32_t nx, int32_t ny,
+                   const double *x, const double *y, double z, const double *bounds,
+                   double cutoff, double *Z, int32_t mem, void *stream);
 
 /* ---- allocation-free evaluation (no counterpart in the reference) ------
  * One derivative evaluation of one simulation -- the passes of

@@ -159,6 +159,8 @@ def _declare(lib):
         "sph_sim_get_state": [vp, c_i32, vp, vp, vp, c_i32],
         "sph_sim_get_properties": [vp, c_i32, vp, vp, vp, vp, vp, vp, vp, vp, c_i32],
         "sph_sim_count": [vp, c_i32, P(c_i64)],
+        "sph_sim_steps": [vp, c_i32, P(c_i64)],
+        "sph_sim_set_steps": [vp, c_i32, c_i64],
         "sph_advance": [vp, c_i32],
         "sph_sim_derivatives": [vp, c_i32, vp, vp, vp, vp, vp, vp, vp, vp, c_i32],
         "sph_sim_pair_count": [vp, c_i32, P(c_i64)],
@@ -174,6 +176,8 @@ def _declare(lib):
         "sph_sync": [vp],
         "sph_sim_status": [vp, c_i32, P(c_i32)],
         "sph_derivatives_noalloc": [P(SphParams), c_i32, c_i64] + [vp] * 13,
+        "sph_splash_map": [c_i32, c_i64, vp, c_i32, vp, vp, vp, vp, c_i32, c_i32, vp, vp,
+                           ctypes.c_double, vp, ctypes.c_double, vp, c_i32, vp],
         "sph_status_string": [ctypes.c_int],
         "sph_version": [],
     }
@@ -189,11 +193,11 @@ def exported_symbols():
     """Names of every entry point declared in include/sph.h."""
     return ["sph_engine_create", "sph_engine_destroy", "sph_sim_add", "sph_sim_remove",
             "sph_sim_set_state", "sph_sim_get_state", "sph_sim_get_properties",
-            "sph_sim_count", "sph_advance", "sph_sim_derivatives", "sph_sim_pair_count",
+            "sph_sim_count", "sph_sim_steps", "sph_sim_set_steps", "sph_advance", "sph_sim_derivatives", "sph_sim_pair_count",
             "sph_sim_export_pairs", "sph_last_pair_total", "sph_sim_diagnostics",
             "sph_get_tuning", "sph_set_tuning", "sph_prepare", "sph_profile",
             "sph_profile_read", "sph_kernels_per_step", "sph_sync", "sph_sim_status",
-            "sph_derivatives_noalloc", "sph_status_string", "sph_version"]
+            "sph_splash_map", "sph_derivatives_noalloc", "sph_status_string", "sph_version"]
 
 
 def lib():

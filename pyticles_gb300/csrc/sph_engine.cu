@@ -989,6 +989,23 @@ int sph_sim_count(sph_engine *e, int32_t id, int64_t *n) {
     return SPH_OK;
 }
 
+int sph_sim_steps(sph_engine *e, int32_t id, int64_t *steps) {
+    TRY(check_sim(e, id));
+    if (!steps) return SPH_EINVAL;
+    *steps = e->sims[id].steps;
+    return SPH_OK;
+}
+
+int sph_sim_set_steps(sph_engine *e, int32_t id, int64_t steps) {
+    TRY(check_sim(e, id));
+    if (steps < 0) return SPH_EINVAL;
+    long long s = (long long)steps;
+    CK(cudaMemcpyAsync(e->steps_d + id, &s, sizeof(s), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    e->sims[id].steps = steps;
+    return SPH_OK;
+}
+
 int sph_advance(sph_engine *e, int32_t nsteps) {
     if (!e || nsteps < 0) return SPH_EINVAL;
     if (nsteps == 0) return SPH_OK;

@@ -60,6 +60,7 @@ class Engine:
               "sph_engine_create")
         self._h = h
         self.counts = {}
+        self.sim_params = {}
 
     # -- lifetime --
     def close(self):
@@ -88,11 +89,13 @@ class Engine:
         check(self._lib.sph_sim_add(self._h, ctypes.byref(params), n, ptr(r), ptr(v), ptr(m),
                                     ptr(u), mem, ctypes.byref(sid)), "sph_sim_add")
         self.counts[sid.value] = n
+        self.sim_params[sid.value] = params
         return sid.value
 
     def remove(self, sim):
         check(self._lib.sph_sim_remove(self._h, int(sim)), "sph_sim_remove")
         self.counts.pop(sim, None)
+        self.sim_params.pop(sim, None)
 
     def set_state(self, sim, r, v, m, u):
         r, v, m, u = _host(r), _host(v), _host(m), _host(u)
@@ -129,6 +132,14 @@ class Engine:
     def properties(self, sim, out=None):
         """Per-particle properties left by the last step (reference semantics)."""
         return self._props(self._lib.sph_sim_get_properties, sim, out)
+
+    def steps(self, sim):
+        n = ctypes.c_int64()
+        check(self._lib.sph_sim_steps(self._h, int(sim), ctypes.byref(n)), "sph_sim_steps")
+        return n.value
+
+    def set_steps(self, sim, steps):
+        check(self._lib.sph_sim_set_steps(self._h, int(sim), int(steps)), "sph_sim_set_steps")
 
     def advance(self, nsteps=1):
         check(self._lib.sph_advance(self._h, int(nsteps)), "sph_advance")

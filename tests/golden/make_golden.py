@@ -11,10 +11,15 @@ it needs into a temporary directory and applies only mechanical edits:
 
   * `print x` statements become `print(x)`;
   * neighbour_list.py:32 `/ 2` becomes `// 2` (an int array size in Py3);
+  * spkernel.lucy_w3d returns `w[0]` instead of the 1-element array `w`
+    (NumPy 2 no longer assigns it into a scalar slot, interpolate.py:147);
   * stub modules replace the absent compiled ones: pairsep (Cython),
-    fkernel, collision (Fortran), configuration, spam_nc (netCDF) and
-    f_properties (re-exports properties); eos.get_vdw_u is restated as the
-    reference's own properties.vdw_energy (properties.py:44-46).
+    fkernel, collision (Fortran), configuration, spam_nc (netCDF),
+    neighbours (vasp) and f_properties (re-exports properties);
+    eos.get_vdw_u is restated as the reference's own properties.vdw_energy
+    (properties.py:44-46), fkernel's 3D Lucy kernel as spkernel.lucy_kernel's
+    3D branch, neighbours.minimum_image as neighbour_list.py:105-123 on two
+    axes.
 
 The derivative evaluation composes reference functions in the order of
 SpamComplete.apply (spam_complete_force.py:63-183), whose Fortran is absent:
@@ -46,11 +51,25 @@ sys.path.insert(0, ROOT)
 from pyticles_gb300 import workloads  # noqa: E402  (seeded initial states only)
 
 MODULES = ["spkernel.py", "spdensity.py", "properties.py", "forces.py", "neighbour_list.py",
-           "integrator.py", "box.py", "controller.py", "particles.py"]
+           "integrator.py", "box.py", "controller.py", "particles.py", "interpolate.py"]
 
 STUBS = {
     "pairsep.py": "def pairsep(nl):\n    pass\n",
-    "fkernel.py": "kernel = None\n",
+    # lucy_w3d's Fortran kernel, restated as the 3D Lucy kernel (spkernel.py:86-118)
+    "fkernel.py": ("import math\n"
+                   "class _Kernel:\n"
+                   "    @staticmethod\n"
+                   "    def lucy_kernel(r, dr, h, w, dwdx):\n"
+                   "        q = 105. / (math.pi * 16. * (h ** 3))\n"
+                   "        w[0] = q * (1 + 3. * r / h) * ((1. - r / h)) ** 3 if r < h else 0.0\n"
+                   "kernel = _Kernel()\n"),
+    # the vasp `neighbours` module is absent: its minimum_image restated with
+    # the rule of neighbour_list.py:105-123 on the first two axes
+    "neighbours.py": ("def minimum_image(dr, xmax, ymax):\n"
+                      "    if dr[0] > xmax / 2.:\n        dr[0] = dr[0] - xmax\n"
+                      "    if dr[1] > ymax / 2.:\n        dr[1] = dr[1] - ymax\n"
+                      "    if dr[0] < -xmax / 2.:\n        dr[0] = dr[0] + xmax\n"
+                      "    if dr[1] < -ymax / 2.:\n        dr[1] = dr[1] + ymax\n"),
     "collision.py": "collision = None\n",
     "configuration.py": "",
     "spam_nc.py": "def read_step(*a, **k):\n    raise RuntimeError('netCDF4 absent')\n",
@@ -85,6 +104,11 @@ def shim(refdir):
     for name in MODULES:
         src = open(os.path.join(refdir, name)).read()
         src = py3(src)
+        if name == "spkernel.py":
+            # NumPy 2 no longer assigns a 1-element array to a scalar slot
+            # (interpolate.py:147 adds lucy_w3d's result into Z[x, y])
+            src = src.replace("    kfc(r,dr,h,w,dwdx)\n    return w\n",
+                              "    kfc(r,dr,h,w,dwdx)\n    return w[0]\n")
         if name == "neighbour_list.py":
             src = src.replace("(particle.maxn * particle.maxn) / 2 - 1",
                               "(particle.maxn * particle.maxn) // 2 - 1")
@@ -99,13 +123,14 @@ def load_reference(refdir):
     tmp = shim(refdir)
     import box
     import forces
+    import interpolate
     import integrator
     import neighbour_list
     import particles
     import properties
     import spdensity
     import spkernel
-    return tmp, dict(box=box, forces=forces, integrator=integrator,
+    return tmp, dict(box=box, forces=forces, integrator=integrator, interpolate=interpolate,
                      neighbour_list=neighbour_list, particles=particles,
                      properties=properties, spdensity=spdensity, spkernel=spkernel)
 
@@ -354,6 +379,27 @@ def pair_edge_cases(R):
     np.savez_compressed(os.path.join(HERE, "pairs_edge.npz"), **out)
 
 
+def splat_maps(R):
+    """interpolate.splash_map_2d / splash_map_3d on golden systems."""
+    ip = R["interpolate"]
+    g = dict(np.load(os.path.join(HERE, "lucy2d_400.npz")))
+    r, m, rho = g["r0"], g["m"], g["ev_rho"]
+    a = rho.copy()
+    h = np.full(len(r), 3.0)
+    x = np.arange(40) * 0.5
+    y = np.arange(40) * 0.5
+    Z2 = ip.splash_map_2d(x, y, r, m, rho, a, h, (0.0, 20.0, 0.0, 20.0), 5.0)
+    g3 = dict(np.load(os.path.join(HERE, "debrun3d_216.npz")))
+    r3, m3, rho3 = g3["r0"], g3["m"], g3["ev_rho"]
+    h3 = np.full(len(r3), 1.3)
+    x3 = np.arange(24) * 0.25
+    y3 = np.arange(24) * 0.25
+    Z3 = ip.splash_map_3d(x3, y3, 3.0, r3, m3, rho3, rho3.copy(), h3, (0.0, 6.0, 0.0, 6.0), 1.5)
+    np.savez_compressed(os.path.join(HERE, "splat.npz"), x=x, y=y, r=r, m=m, rho=rho, a=a, h=h,
+                        Z2=Z2, x3=x3, y3=y3, r3=r3, m3=m3, rho3=rho3, h3=h3, Z3=Z3)
+    print(f"splat: 2d {Z2.shape} sum={Z2.sum():.6f}  3d {Z3.shape} sum={Z3.sum():.6f}")
+
+
 def main():
     refdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     which = set(sys.argv[2:])
@@ -368,6 +414,8 @@ def main():
             kat_nlist(R)
         if want("pairs"):
             pair_edge_cases(R)
+        if want("splat"):
+            splat_maps(R)
         if want("lucy3d_27"):
             prm, r, v, m, T0 = workloads.lattice_system(3, 3, spacing=1.1, jitter=0.1,
                                                         temperature=0.6, seed=11)
