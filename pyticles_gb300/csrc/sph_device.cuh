@@ -94,6 +94,34 @@ template <> struct Acc<double> {
     __device__ __forceinline__ double get64() const { return s; }
 };
 
+// Blocked compensated sum: the terms of one neighbour cell (a handful) are
+// added plainly into `part`, which is folded into the compensated total once
+// per cell.  The per-cell partials carry a few ulp; the compensation keeps
+// the sum over cells from growing further.
+template <typename R> struct BAcc {
+    Acc<R> total;
+    R part;
+    __device__ __forceinline__ void init(R x) { total.init(x); part = (R)0; }
+    __device__ __forceinline__ void add(R x) { part += x; }
+    __device__ __forceinline__ void flush() { total.add(part); part = (R)0; }
+    __device__ __forceinline__ R get() { flush(); return total.get(); }
+    __device__ __forceinline__ double get64() { flush(); return total.get64(); }
+};
+
+// Approximate single-precision helpers for terms that do not enter a
+// cancelling sum (viscosity, force-pass distances): MUFU reciprocal and
+// reciprocal square root, about 2 ulp; exact operations in FP64 mode.
+template <typename R> __device__ __forceinline__ R fdiv(R a, R b);
+template <> __device__ __forceinline__ float fdiv<float>(float a, float b) {
+    return __fdividef(a, b);
+}
+template <> __device__ __forceinline__ double fdiv<double>(double a, double b) { return a / b; }
+template <typename R> __device__ __forceinline__ R fsqrt(R x);
+template <> __device__ __forceinline__ float fsqrt<float>(float x) {
+    return x > 0.0f ? x * rsqrtf(x) : 0.0f;
+}
+template <> __device__ __forceinline__ double fsqrt<double>(double x) { return sqrt(x); }
+
 // Fast-test bounds around the pair threshold.  In mixed mode the squared
 // distance comes from FP32 cell-local coordinates whose error is below
 // 5e-6 relative for cell edges up to twice the cutoff; pairs whose FP32

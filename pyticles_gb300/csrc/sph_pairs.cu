@@ -85,10 +85,10 @@ template <typename R> __device__ __forceinline__ R fmaxf_(R c, R ext) {
 // Cells are (cutoff + skin)/W wide and the window spans +-W cells per axis;
 // a cell whose box (grown by the allowed drift) lies beyond the cutoff from
 // particle i is skipped before any of its particles is loaded.
-template <typename R, int D, typename T4, typename F>
+template <typename R, int D, typename T4, typename F, typename G>
 __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                                           const PairFrame<R, D> &fr, const T4 *__restrict__ P,
-                                          int i, const T4 &pi, F body) {
+                                          int i, const T4 &pi, F body, G cell_done) {
     const int cp = v.cell_xyz[v.cell_b[i]];
     const int c0 = cp & 2047, c1 = (cp >> 11) & 2047, c2 = (cp >> 22) & 1023;
     const int w0 = S.win[0], w1 = S.win[1], w2 = D == 3 ? S.win[2] : 0;
@@ -136,6 +136,7 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                     if (rsq >= fr.thr_lo && !exact_in_set<D>(v.xe_in, &S, i, j)) continue;
                     body(j, pj, d, rsq);
                 }
+                cell_done();
             }
         }
     }
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(256) k_density(View v, int stage) {
     const SimDev &S = v.sims[s];
     KConst<R> ks = make_kconst<R>(S, 0);
     KConst<R> kl = make_kconst<R>(S, 1);
-    Acc<R> rs, rl;
+    BAcc<R> rs, rl;
     rs.init((R)0);
     rl.init((R)0);
     unsigned cnt = 0;
@@ -180,11 +181,15 @@ __global__ void __launch_bounds__(256) k_density(View v, int stage) {
         rl.add(pj.w * w);
         ++cnt;
     };
+    auto cell_done = [&]() {
+        rs.flush();
+        rl.flush();
+    };
     if (!active) return;
     {
         PairFrame<R, D> fr;
         fr.init(S);
-        for_pairs<R, D>(v, S, fr, P, i, P[i], body);
+        for_pairs<R, D>(v, S, fr, P, i, P[i], body, cell_done);
     }
     // EOS in FP64 from the compensated sums plus the FP64 self term
     // (properties.py:77-78): the temperature T = (u + a rho)/k_B cancels
@@ -230,12 +235,12 @@ __global__ void __launch_bounds__(256) k_heat(View v) {
     const SimDev &S = v.sims[s];
     KConst<R> ks = make_kconst<R>(S, 0);
     const T4 fi = F[ii];
-    Acc<R> q[3];
+    BAcc<R> q[3];
     q[0].init(0);
     q[1].init(0);
     q[2].init(0);
     auto body = [&](int j, const T4 &pj, const R *d, R rsq) {
-        R r = rsqrt_<R>(rsq);
+        R r = fsqrt<R>(rsq);
         R g = kernel_g<K, R>(ks, r);
         T4 fj = F[j];
         R dT = (fj.z - fi.z) + (fj.w - fi.w);
@@ -244,11 +249,16 @@ __global__ void __launch_bounds__(256) k_heat(View v) {
         q[1].add(f * d[1]);
         if (D == 3) q[2].add(f * d[2]);
     };
+    auto cell_done = [&]() {
+        q[0].flush();
+        q[1].flush();
+        if (D == 3) q[2].flush();
+    };
     if (!active) return;
     {
         PairFrame<R, D> fr;
         fr.init(S);
-        for_pairs<R, D>(v, S, fr, P, i, P[i], body);
+        for_pairs<R, D>(v, S, fr, P, i, P[i], body, cell_done);
     }
     R kap = sconst<R>(S).kappa;
     R qq[3] = {kap * q[0].get(), kap * q[1].get(), kap * q[2].get()};
@@ -319,13 +329,13 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
     const R pl2 = sc.pl2;  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
     const T4 vi = V[ii], fi = F[ii];
     const T4 qi = heat ? Q[ii] : make_v4<R>(0, 0, 0, 0);
-    Acc<R> ax[3], ud;
+    BAcc<R> ax[3], ud;
     ax[0].init(0);
     ax[1].init(0);
     ax[2].init(0);
     ud.init(0);
     auto body = [&](int j, const T4 &pj, const R *d, R rsq) {
-        R r = rsqrt_<R>(rsq);
+        R r = fsqrt<R>(rsq);
         R gs = kernel_g<K, R>(ks, r);
         R gl = kernel_g<K, R>(kl, r);
         T4 fj = F[j], vj = V[j];
@@ -334,8 +344,8 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
         R ps = fi.x + fj.x;
         if (visc && dvdx < (R)0) {
             // Monaghan viscosity on approaching pairs
-            R mu = hs * dvdx / (rsq + eps_h2);
-            ps += (-alpha_c * mu + beta * mu * mu) / ((R)0.5 * (fi.y + fj.y));
+            R mu = fdiv<R>(hs * dvdx, rsq + eps_h2);
+            ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), fi.y + fj.y);
         }
         R gsum = ps * gs + pl2 * gl;
         ax[0].add(gsum * d[0]);
@@ -350,11 +360,17 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
         }
         ud.add(du);
     };
+    auto cell_done = [&]() {
+        ax[0].flush();
+        ax[1].flush();
+        if (D == 3) ax[2].flush();
+        ud.flush();
+    };
     if (!active) return;
     {
         PairFrame<R, D> fr;
         fr.init(S);
-        for_pairs<R, D>(v, S, fr, P, i, P[i], body);
+        for_pairs<R, D>(v, S, fr, P, i, P[i], body, cell_done);
     }
     R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
     R udr = ud.get();
@@ -555,9 +571,11 @@ __global__ void k_pair_rows(View v, int off, int n, long long *row_count) {
     fr.init(S);
     const int idi = v.b_id[i];
     long long c = 0;
-    for_pairs<R, D>(v, S, fr, P, i, P[i], [&](int j, const T4 &, const R *, R) {
-        if (v.b_id[j] > idi) ++c;
-    });
+    for_pairs<R, D>(
+        v, S, fr, P, i, P[i], [&](int j, const T4 &, const R *, R) {
+            if (v.b_id[j] > idi) ++c;
+        },
+        [] {});
     row_count[idi] = c;
 }
 
@@ -603,7 +621,7 @@ __global__ void k_pair_write(View v, int off, int n, const long long *row_start,
         }
         if (rsq) rsq[p] = r2;
         ++m;
-    });
+    }, [] {});
 }
 
 void launch_pair_rows(const View &v, int precision, int sim_off, int n, long long *row_count,
