@@ -23,6 +23,9 @@
  *                                       properties.spam_properties       properties.py:63-120
  *                                       forces.SpamForce/CohesiveSpamForce forces.py:321-405
  *   sph_sim_pair_count / export_pairs   VerletList.build + separations   neighbour_list.py:160-189, 63-83
+ *   sph_collide_pairs                   CollisionForce / CollisionForce3d forces.py:87-243
+ *                                       FortranCollisionForce            forces.py:454-474
+ *                                       Force.apply (cutoff test)        forces.py:38-42
  */
 #ifndef PYTICLES_GB300_SPH_H
 #define PYTICLES_GB300_SPH_H
@@ -78,6 +81,9 @@ typedef struct sph_params {
     int32_t heat_flux;      /* 1: Fourier heat flux q and conduction energy rate    */
     int32_t thermostat;     /* 1: scaling thermostat after every step               */
     int32_t integrator;     /* enum sph_integrator                                   */
+    int32_t collision;      /* enum sph_collision: hard-sphere velocity exchange on
+                               pairs within collision_cutoff after every evaluation */
+    int32_t reserved;       /* 0                                                     */
     double box[3];          /* periodic extents xmax, ymax, zmax (box.py:18-22)     */
     double h_short;         /* repulsive smoothing length  (particles.py:286, p.h)  */
     double h_long;          /* cohesive smoothing length   (particles.py:287, p.hlr)*/
@@ -93,7 +99,17 @@ typedef struct sph_params {
     double thermostat_temp;      /* target temperature at step 0                    */
     double thermostat_temp_end;  /* target after thermostat_ramp_steps (linear)     */
     int64_t thermostat_ramp_steps;
+    double collision_cutoff;     /* pairs with rij^2 <= cutoff^2 collide (forces.py:38-42) */
 } sph_params;
+
+/* Hard collisions (forces.py:87-243, 454-474): after each derivative
+ * evaluation every pair (i<j in list order) with rij^2 <= collision_cutoff^2
+ * that is not separating exchanges the components of its velocities along
+ * the pair axis, scaled by the mass ratio, in the pair list's order.
+ * SPH_COLLIDE_EXCHANGE is CollisionForce (2D) / FortranCollisionForce
+ * (collide3d restated); SPH_COLLIDE_PUSHBACK adds CollisionForce3d's
+ * separation of the pair to cutoff + 0.01 (sph_collide_pairs only). */
+enum sph_collision { SPH_COLLIDE_OFF = 0, SPH_COLLIDE_EXCHANGE = 1, SPH_COLLIDE_PUSHBACK = 2 };
 
 typedef struct sph_engine sph_engine;
 
@@ -221,6 +237,20 @@ int sph_splash_map(int32_t mode, int64_t n, const double *r, int32_t r_cols, con
                    const double *rho, const double *a, const double *h, int32_t nx, int32_t ny,
                    const double *x, const double *y, double z, const double *bounds,
                    double cutoff, double *Z, int32_t mem, void *stream);
+
+/* Hard collisions over a given pair list: Force.apply of CollisionForce
+ * (mode SPH_COLLIDE_EXCHANGE, dim 2), FortranCollisionForce (EXCHANGE, the
+ * absent collide3d restated) and CollisionForce3d (SPH_COLLIDE_PUSHBACK).
+ * Pairs k = 0 .. nip-1 with rij[k]^2 <= cutoff^2 are applied in list order,
+ * as the reference's sequential loop does; pairs that share no particle run
+ * concurrently (dependency levels), with results identical to the
+ * sequential order.  r and v (n x dim) are updated in place; with PUSHBACK
+ * so are r, drij[k] (r_j - r_i, not minimum-imaged) and rij[k] of the pairs
+ * that were pushed apart.  iap is nip x 2 (int64, 0-based), drij nip x dim.
+ * mem tags every array pointer; returns after the work has finished. */
+int sph_collide_pairs(int32_t dim, int32_t mode, int64_t n, double *r, double *v,
+                      const double *m, int64_t nip, const int64_t *iap, double *drij,
+                      double *rij, double cutoff, int32_t mem, void *stream);
 
 /* ---- allocation-free evaluation (no counterpart in the reference) ------
  * One derivative evaluation of one simulation -- the passes of

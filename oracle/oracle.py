@@ -53,6 +53,9 @@ def lib():
         L.orc_kernel.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                  P(ctypes.c_double), P(ctypes.c_double)]
         L.orc_kernel.restype = None
+        L.orc_collide_pairs.argtypes = [ctypes.c_int32, ctypes.c_int32, i64, vp, vp, vp, i64,
+                                        vp, vp, vp, ctypes.c_double]
+        L.orc_collide_pairs.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_set_threads.restype = None
         L.orc_get_threads.restype = ctypes.c_int
@@ -139,3 +142,17 @@ def initial_energy(params, r, v, m, temperature):
     (properties.py:44-46, 116-119)."""
     d = derivatives(params, r, v, m, np.zeros(r.shape[0]))
     return temperature * params.kbdash - params.adash * d["rho"]
+
+
+def collide_pairs(mode, r, v, m, iap, drij, rij, cutoff):
+    """Force.apply of a collision force over a pair list, sequentially
+    (forces.py:38-42, 87-243).  Returns updated copies (r, v, drij, rij)."""
+    r, v, m = _c(r).copy(), _c(v).copy(), _c(m)
+    iap = _c(iap, np.int64)
+    drij, rij = _c(drij).copy(), _c(rij).copy()
+    n, d = v.shape
+    st = lib().orc_collide_pairs(d, int(mode), n, r.ctypes.data, v.ctypes.data,
+                                 m.ctypes.data, len(iap), iap.ctypes.data, drij.ctypes.data,
+                                 rij.ctypes.data, float(cutoff))
+    assert st == 0, st
+    return r, v, drij, rij

@@ -46,6 +46,17 @@
  *  integrator imp_euler / euler / rk4 on (r, v, u) with rates (v, vdot, udot)
  *             (integrator.py:14-103); c = f*dt, x = x0 + c, ...
  *  box        teleport wrap: r > L -> 0, r < 0 -> L per axis (box.py:33-47).
+ *  collisions after each evaluation (forces after SpamComplete in p.forces):
+ *             the pair list in (i, j) order, pairs with rij^2 <= cutoff^2
+ *             (forces.py:38-42) that are not separating trade the velocity
+ *             components along dr, scaled by the mass ratio, sequentially
+ *             (CollisionForce forces.py:87-156; FortranCollisionForce's absent
+ *             collide3d restated the same way, forces.py:454-474);
+ *             CollisionForce3d also pushes the pair apart to cutoff + 0.01
+ *             (forces.py:158-243).  In a step, the extra first evaluation of
+ *             update() (particles.py:480) leaves its collisions behind and the
+ *             first evaluation's collided velocities are x_start's
+ *             (integrator.py:44-59).
  *  thermostat T <- T_last * target/mean(T_last); u <- k_B T - a rho, with
  *             T_last the temperature of the step's last evaluation and rho
  *             the start-of-step density (particles.py:450-457, 513-526;
@@ -363,6 +374,88 @@ int orc_pairs(const sph_params *p, int64_t n, const double *r, int64_t cap, int6
     return SPH_OK;
 }
 
+/* ---- hard collisions ---------------------------------------------------- */
+
+/* One pair of the sequential loop (forces.py:87-156 and 158-243). */
+static void collide_pair(int dim, int mode, double *r, double *v, const double *m, int64_t i,
+                         int64_t j, double *dr, double *rij, double cutoff) {
+    double *vi = &v[i * dim], *vj = &v[j * dim];
+    double drsq = dr[0] * dr[0];
+    double vidotr = vi[0] * dr[0], vjdotr = vj[0] * dr[0];
+    for (int a = 1; a < dim; ++a) {
+        drsq = drsq + dr[a] * dr[a];
+        vidotr = vidotr + vi[a] * dr[a];
+        vjdotr = vjdotr + vj[a] * dr[a];
+    }
+    if (vidotr < 0 && vjdotr > 0) return;
+    double vti[3], vni[3], vtj[3], vnj[3];
+    for (int a = 0; a < dim; ++a) {
+        vti[a] = (vidotr / drsq) * dr[a];
+        vni[a] = vi[a] - vti[a];
+        vtj[a] = (vjdotr / drsq) * dr[a];
+        vnj[a] = vj[a] - vtj[a];
+    }
+    for (int a = 0; a < dim; ++a) {
+        double tmp = vti[a];
+        vti[a] = vtj[a] * (m[j] / m[i]);
+        vtj[a] = tmp * (m[i] / m[j]);
+    }
+    for (int a = 0; a < dim; ++a) {
+        vi[a] = vti[a] + vni[a];
+        vj[a] = vtj[a] + vnj[a];
+    }
+    if (mode == SPH_COLLIDE_PUSHBACK && drsq < cutoff * cutoff) {
+        double ro = (cutoff + 0.01 - *rij) / 2.0, nsq = 0.0;
+        for (int a = 0; a < dim; ++a) {
+            double dro = (dr[a] / *rij) * ro;
+            r[i * dim + a] -= dro;
+            r[j * dim + a] += dro;
+        }
+        for (int a = 0; a < dim; ++a) {
+            dr[a] = r[j * dim + a] - r[i * dim + a];
+            nsq = a == 0 ? dr[a] * dr[a] : nsq + dr[a] * dr[a];
+        }
+        *rij = sqrt(nsq);
+    }
+}
+
+/* Force.apply of a collision force over a pair list (forces.py:38-42). */
+int orc_collide_pairs(int32_t dim, int32_t mode, int64_t n, double *r, double *v,
+                      const double *m, int64_t nip, const int64_t *iap, double *drij,
+                      double *rij, double cutoff) {
+    double c2 = cutoff * cutoff;
+    for (int64_t k = 0; k < nip; ++k) {
+        int64_t i = iap[2 * k], j = iap[2 * k + 1];
+        if (i < 0 || j < 0 || i >= n || j >= n || i == j) return SPH_EINVAL;
+        if (rij[k] * rij[k] <= c2)
+            collide_pair(dim, mode, r, v, m, i, j, &drij[k * dim], &rij[k], cutoff);
+    }
+    return SPH_OK;
+}
+
+/* Collisions of one evaluation: the pair set at r in (i, j) order. */
+static int collide_state(const sph_params *p, int64_t n, double *r, double *v,
+                         const double *m) {
+    int64_t nip = 0;
+    int st = orc_pairs(p, n, r, 0, NULL, NULL, &nip);
+    if (st != SPH_OK && st != SPH_ECAPACITY) return st;
+    int64_t *iap = malloc(sizeof(int64_t) * 2 * (size_t)(nip + 1));
+    double *rsq = malloc(sizeof(double) * (size_t)(nip + 1));
+    st = orc_pairs(p, n, r, nip, iap, rsq, &nip);
+    double c2 = p->collision_cutoff * p->collision_cutoff;
+    for (int64_t k = 0; st == SPH_OK && k < nip; ++k) {
+        double rij = sqrt(rsq[k]);
+        if (!(rij * rij <= c2)) continue;
+        double dr[3];
+        pair_rsq(p, &r[iap[2 * k] * p->dim], &r[iap[2 * k + 1] * p->dim], dr);
+        collide_pair(p->dim, SPH_COLLIDE_EXCHANGE, r, v, m, iap[2 * k], iap[2 * k + 1], dr,
+                     &rij, p->collision_cutoff);
+    }
+    free(iap);
+    free(rsq);
+    return st;
+}
+
 /* ---- one derivative evaluation (gather form, OpenMP over particles) ----- */
 
 typedef struct {
@@ -523,7 +616,13 @@ int orc_advance(const sph_params *p, int64_t n, double *r, double *v, const doub
     double *ojq = jq ? jq : calloc(nd + 1, sizeof(double));
     int st = SPH_OK;
     int nstage = p->integrator == SPH_EULER ? 1 : (p->integrator == SPH_RK4 ? 4 : 2);
+    const int coll = p->collision == SPH_COLLIDE_EXCHANGE;
     for (int32_t s = 0; s < nsteps && st == SPH_OK; ++s) {
+        if (coll) {
+            /* update()'s extra first evaluation: only its collisions remain */
+            st = collide_state(p, n, r, v, m);
+            if (st) break;
+        }
         memcpy(r0, r, sizeof(double) * nd);
         memcpy(v0, v, sizeof(double) * nd);
         memcpy(u0, u, sizeof(double) * n1);
@@ -531,6 +630,11 @@ int orc_advance(const sph_params *p, int64_t n, double *r, double *v, const doub
             orc_out o = {rho, rho_lr, t, pres, pco, vdot, udot, ojq};
             st = derivatives(p, n, r, v, m, u, &o, NULL);
             if (st) break;
+            if (coll) {
+                st = collide_state(p, n, r, v, m);
+                if (st) break;
+                if (k == 0) memcpy(v0, v, sizeof(double) * nd);  /* x_start */
+            }
             if (k == 0) {
                 memcpy(rho0, rho, sizeof(double) * n1);
                 memcpy(p0, pres, sizeof(double) * n1);

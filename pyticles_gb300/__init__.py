@@ -7,14 +7,15 @@ Reference-facing API (same names as andrewcharles/pyticles):
     SmoothParticleSystem, ParticleSystem      particles.py
     NeighbourList, VerletList, SortedVerletList neighbour_list.py
     Force, SpamForce, CohesiveSpamForce, SpamConduction, SpamComplete
+    CollisionForce, CollisionForce3d, FortranCollisionForce
     PeriodicBox
 Engine-level API: Engine (many simulations per engine), workloads, serve.
 """
 from ._abi import KERNELS, SphError, SphParams, make_params  # noqa: F401
 from .box import Box, MirrorBox, PeriodicBox  # noqa: F401
 from .engine import Engine  # noqa: F401
-from .forces import (CohesiveSpamForce, Force, SpamComplete, SpamConduction,  # noqa: F401
-                     SpamForce)
+from .forces import (CohesiveSpamForce, CollisionForce, CollisionForce3d,  # noqa: F401
+                     Force, FortranCollisionForce, SpamComplete, SpamConduction, SpamForce)
 from .neighbour_list import NeighbourList, SortedVerletList, VerletList  # noqa: F401
 from .particles import ParticleSystem, SmoothParticleSystem  # noqa: F401
 

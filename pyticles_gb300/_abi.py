@@ -38,6 +38,10 @@ SPH_MIXED = 1
 INTEGRATORS = {"euler": 0, "ieuler": 1, "rk4": 2}
 SPH_DEVICE = 0
 SPH_HOST = 1
+# enum sph_collision
+SPH_COLLIDE_OFF = 0
+SPH_COLLIDE_EXCHANGE = 1
+SPH_COLLIDE_PUSHBACK = 2
 
 
 class SphParams(ctypes.Structure):
@@ -49,6 +53,8 @@ class SphParams(ctypes.Structure):
         ("heat_flux", ctypes.c_int32),
         ("thermostat", ctypes.c_int32),
         ("integrator", ctypes.c_int32),
+        ("collision", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
         ("box", ctypes.c_double * 3),
         ("h_short", ctypes.c_double),
         ("h_long", ctypes.c_double),
@@ -66,6 +72,7 @@ class SphParams(ctypes.Structure):
         ("thermostat_temp", ctypes.c_double),
         ("thermostat_temp_end", ctypes.c_double),
         ("thermostat_ramp_steps", ctypes.c_int64),
+        ("collision_cutoff", ctypes.c_double),
     ]
 
 
@@ -85,10 +92,12 @@ def make_params(dim=2, kernel="lucy", box=(32.0, 32.0, 1.0), h_short=3.0, h_long
                 viscosity=False, visc_alpha=1.0, visc_beta=0.1, visc_eps=0.01,
                 sound_speed=1.0, heat_flux=False, thermalk=1.0, dt=1e-3,
                 integrator="ieuler", thermostat=False, thermostat_temp=1.0,
-                thermostat_temp_end=None, thermostat_ramp_steps=0):
+                thermostat_temp_end=None, thermostat_ramp_steps=0, collision_cutoff=0.0):
     """Builds an SphParams.  Defaults follow the reference: a=2, b=0.5,
     k_B=1 (properties.py:18-20), eta=1, zeta=0.1, c=1
-    (spam_complete_force.py:36-46,142), thermalk=1 (f_properties.py:14)."""
+    (spam_complete_force.py:36-46,142), thermalk=1 (f_properties.py:14).
+    collision_cutoff > 0 turns on hard collisions (the velocity exchange of
+    CollisionForce / FortranCollisionForce) after every evaluation."""
     p = SphParams()
     p.dim = int(dim)
     p.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
@@ -115,6 +124,9 @@ def make_params(dim=2, kernel="lucy", box=(32.0, 32.0, 1.0), h_short=3.0, h_long
     p.thermostat_temp_end = float(thermostat_temp if thermostat_temp_end is None
                                   else thermostat_temp_end)
     p.thermostat_ramp_steps = int(thermostat_ramp_steps)
+    p.collision = SPH_COLLIDE_EXCHANGE if collision_cutoff > 0 else SPH_COLLIDE_OFF
+    p.reserved = 0
+    p.collision_cutoff = float(collision_cutoff)
     return p
 
 
@@ -133,7 +145,7 @@ def params_from_dict(d):
         if name == "box":
             for a in range(3):
                 p.box[a] = float(d["box"][a])
-        else:
+        elif name in d:
             setattr(p, name, d[name])
     return p
 
@@ -178,6 +190,8 @@ def _declare(lib):
         "sph_derivatives_noalloc": [P(SphParams), c_i32, c_i64] + [vp] * 13,
         "sph_splash_map": [c_i32, c_i64, vp, c_i32, vp, vp, vp, vp, c_i32, c_i32, vp, vp,
                            ctypes.c_double, vp, ctypes.c_double, vp, c_i32, vp],
+        "sph_collide_pairs": [c_i32, c_i32, c_i64, vp, vp, vp, c_i64, vp, vp, vp,
+                              ctypes.c_double, c_i32, vp],
         "sph_status_string": [ctypes.c_int],
         "sph_version": [],
     }
@@ -197,7 +211,7 @@ def exported_symbols():
             "sph_sim_export_pairs", "sph_last_pair_total", "sph_sim_diagnostics",
             "sph_get_tuning", "sph_set_tuning", "sph_prepare", "sph_profile",
             "sph_profile_read", "sph_kernels_per_step", "sph_sync", "sph_sim_status",
-            "sph_splash_map", "sph_derivatives_noalloc", "sph_status_string", "sph_version"]
+            "sph_splash_map", "sph_collide_pairs", "sph_derivatives_noalloc", "sph_status_string", "sph_version"]
 
 
 def lib():

@@ -114,6 +114,7 @@ struct sph_engine {
     unsigned long long *pair_count = nullptr;
     int *err = nullptr, *err_any = nullptr;
     int *chunk_sim = nullptr, *chunk_start = nullptr, *chunk_len = nullptr;
+    CollideSet coll = {};          // hard-collision candidates (group.collision)
 
     // profiling: event pairs recorded around each pass
     bool prof_on = false;
@@ -178,8 +179,17 @@ uint64_t part1by2(uint64_t x) {
 
 int validate_params(const sph_engine *e, const sph_params *p) {
     if (p->dim != e->dim || p->kernel != e->group.kernel || p->viscosity != e->group.viscosity ||
-        p->heat_flux != e->group.heat_flux || p->integrator != e->group.integrator)
+        p->heat_flux != e->group.heat_flux || p->integrator != e->group.integrator ||
+        p->collision != e->group.collision)
         return SPH_EINVAL;
+    if (p->collision != SPH_COLLIDE_OFF) {
+        // the engine runs the velocity exchange; a collision range beyond the
+        // pair set would need pairs the cell list does not visit
+        if (p->collision != SPH_COLLIDE_EXCHANGE || !(p->collision_cutoff > 0) ||
+            p->collision_cutoff * p->collision_cutoff >
+                p->cutoff * p->cutoff + p->tolerance * p->tolerance)
+            return SPH_EINVAL;
+    }
     for (int a = 0; a < p->dim; ++a)
         if (!(p->box[a] > 0.0) || !std::isfinite(p->box[a])) return SPH_EINVAL;
     if (!(p->h_short > 0) || !(p->h_long > 0) || !(p->cutoff > 0) || p->tolerance < 0)
@@ -317,6 +327,17 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
     d.T0 = p.thermostat_temp;
     d.T1 = p.thermostat_temp_end;
     d.ramp = p.thermostat_ramp_steps;
+    d.coll_on = p.collision == SPH_COLLIDE_EXCHANGE ? 1 : 0;
+    d.coll_c2 = p.collision_cutoff * p.collision_cutoff;
+    for (int a = 0; a < 3; ++a) {
+        // two particles within the collision range sit at most this many
+        // cells apart (each may have drifted by slack_half since binning)
+        int w = 0;
+        if (d.coll_on && a < e->dim && S.nc[a] > 1)
+            w = std::min(S.win[a], (int)std::ceil((p.collision_cutoff + 2.0 * d.slack_half[a]) /
+                                                  S.edge[a]));
+        d.coll_win[a] = w;
+    }
     // fast-test guard band: 2^-12 relative in FP32 (cell-local coordinates
     // keep the FP32 squared distance within 5e-6 of the FP64 one), 1e-9 in FP64
     fill_const<float>(d.cf, e, S, d, 1.0 / 4096.0);
@@ -538,10 +559,41 @@ void enqueue_prepare(sph_engine *e, cudaStream_t st) {
     launch_permute(v, e->precision, st);
 }
 
+// Collision candidates at the evaluation positions of v and their levels.
+void enqueue_collide_find(sph_engine *e, const View &v, cudaStream_t st) {
+    CollideSet c = e->coll;
+    c.np = e->np_b;
+    cudaMemsetAsync(c.info, 0, sizeof(int) * 4, st);
+    launch_collide_find(v, c, st);
+    launch_collide_levels(c, st);
+}
+
+// Collisions on the velocities of evaluation s (stage 0: the start state).
+void enqueue_collide_apply(sph_engine *e, int s, bool packed, cudaStream_t st) {
+    CollideSet c = e->coll;
+    c.np = e->np_b;
+    double *const *vel = s == 0 ? e->b_vel : e->ve;
+    Vec3Ref vr{{vel[0], vel[1], vel[2]}, 1};
+    launch_collide_apply(c, e->dim, vr, vr, e->b_m, 0.0, packed ? e->pk_vel[0] : nullptr,
+                         e->precision, e->err, e->err_any, (int)e->sims.size(), st);
+}
+
+// One evaluation of the step.  With hard collisions the reference's
+// derivatives() mutates the velocities after the rates are computed
+// (forces after SpamComplete in p.forces), before the integrator reads
+// them as rdot and, on the first evaluation, as x_start; the step's extra
+// first evaluation (particles.py:480) leaves its collisions behind too.  The
+// force pass then stops at the rates and a separate pass integrates.
 void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
     View v = make_view(e);
     stage_view(e, v, s);
     int blk = e->tune.block_size;
+    const bool coll = mode == 1 && e->group.collision != SPH_COLLIDE_OFF;
+    if (coll && s == 0) {
+        ProfScope ps(e, SPH_PASS_FORCE, st);
+        enqueue_collide_find(e, v, st);
+        enqueue_collide_apply(e, 0, true, st);
+    }
     {
         ProfScope ps(e, SPH_PASS_DENSITY, st);
         launch_density(v, e->precision, e->group.kernel, s, blk, st);
@@ -557,7 +609,12 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
     {
         ProfScope ps(e, SPH_PASS_FORCE, st);
         launch_force(v, e->precision, e->group.kernel, e->group.viscosity, e->group.heat_flux,
-                     e->group.integrator, s, mode, blk, st);
+                     e->group.integrator, s, coll ? 0 : mode, blk, st);
+        if (coll) {
+            if (s > 0) enqueue_collide_find(e, v, st);
+            enqueue_collide_apply(e, s, false, st);
+            launch_integrate(v, e->precision, e->group.integrator, s, st);
+        }
     }
 }
 
@@ -570,6 +627,9 @@ int64_t kernels_per_step(const sph_engine *e) {
     int64_t k = kSortKernels;
     k += (int64_t)e->nstage * (2 + (e->group.heat_flux ? 1 : 0));
     if (e->any_thermostat) k += 2;
+    // collisions: per find 5 kernels + 7 for the levels, one apply per
+    // evaluation plus the extra first one, one integrator pass per stage
+    if (e->group.collision != SPH_COLLIDE_OFF) k += (int64_t)e->nstage * 14 + 1;
     return k;
 }
 
@@ -726,6 +786,26 @@ int alloc_particles(sph_engine *e) {
     for (void **p : rs) TRY(dalloc((char **)p, P * e->rsize));
     if (e->group.integrator == SPH_RK4) TRY(dalloc(&e->acc_u, P));
     TRY(dalloc(&e->stage_buf, P * 4));
+    if (e->group.collision != SPH_COLLIDE_OFF) {
+        // up to one colliding pair per particle per evaluation (SPH_ECAPACITY beyond)
+        CollideSet &c = e->coll;
+        c.cap = (int)P;
+        TRY(dalloc(&c.row_count, P + 1));
+        TRY(dalloc(&c.row_start, P + 1));
+        TRY(dalloc(&c.scan_tmp, P / 4096 + 2));
+        TRY(dalloc(&c.ci, P));
+        TRY(dalloc(&c.cj, P));
+        for (int a = 0; a < 3; ++a) TRY(dalloc(&c.dr[a], P));
+        TRY(dalloc(&c.rij, P));
+        TRY(dalloc(&c.src, P));
+        TRY(dalloc(&c.touch_count, P + 1));
+        TRY(dalloc(&c.touch_start, P + 1));
+        TRY(dalloc(&c.touch_fill, P + 1));
+        TRY(dalloc(&c.touch, 2 * P));
+        TRY(dalloc(&c.pred, 2 * P));
+        TRY(dalloc(&c.level, P));
+        TRY(dalloc(&c.info, 4));
+    }
     // pk_q must read as zero when heat flux is off
     CK(cudaMemset(e->pk_q, 0, P * e->v4size));
     CK(cudaMemset(e->a_sim, 0xff, P * sizeof(int)));
@@ -760,6 +840,12 @@ void free_all(sph_engine *e) {
                     e->pair_count, e->err, e->err_any, e->chunk_sim, e->chunk_start,
                     e->chunk_len, e->cell_xyz};
     for (void *p : ptrs)
+        if (p) cudaFree(p);
+    const CollideSet &c = e->coll;
+    void *cp[] = {c.row_count, c.row_start, c.scan_tmp, c.ci,   c.cj,    c.dr[0],
+                  c.dr[1],     c.dr[2],     c.rij,      c.src,  c.touch_count,
+                  c.touch_start, c.touch_fill, c.touch, c.pred, c.level, c.info};
+    for (void *p : cp)
         if (p) cudaFree(p);
     for (int a = 0; a < 3; ++a) {
         void *pa[] = {e->org[a], e->a_pos[a], e->a_vel[a], e->b_pos[a], e->b_vel[a], e->xe[0][a],
@@ -822,6 +908,8 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     if (group->dim != 2 && group->dim != 3) return SPH_EINVAL;
     if (group->kernel < 1 || group->kernel > 4) return SPH_EINVAL;
     if (group->integrator < 0 || group->integrator > 2) return SPH_EINVAL;
+    if (group->collision != SPH_COLLIDE_OFF && group->collision != SPH_COLLIDE_EXCHANGE)
+        return SPH_EINVAL;
     if (precision != SPH_FP64 && precision != SPH_MIXED) return SPH_EINVAL;
     if (max_particles <= 0 || max_particles > (int64_t)0x7fffffff / 2 || max_sims <= 0)
         return SPH_EINVAL;

@@ -58,6 +58,9 @@ struct SimDev {
     double inv_kb;
     double T0, T1;          // thermostat ramp ends
     long long ramp;
+    int coll_on;            // hard collisions after each evaluation
+    int coll_win[3];        // +-cells searched for collision partners
+    double coll_c2;         // collision_cutoff^2 (Force.cutoffsq, forces.py:33)
     SimConst<float> cf;
     SimConst<double> cd;
 };
@@ -104,6 +107,49 @@ struct View {
     int *err;               // per sim error word
     int *err_any;
 };
+
+// Strided view of an n x 3 (SoA, stride 1) or n x dim (row-major, stride
+// dim) FP64 array: element (slot, axis a) is p[a][slot * stride].
+struct Vec3Ref {
+    double *p[3];
+    int stride;
+};
+
+// Colliding pairs of one evaluation in the order the reference applies
+// them, and the dependency levels that let pairs without a shared particle
+// run concurrently (sph_collide.cu).
+struct CollideSet {
+    int cap;                        // candidate capacity
+    int np;                         // particle slots
+    int *row_count, *row_start;     // [np + 1] per row (sequence order)
+    int *scan_tmp;                  // scan blocks
+    int *ci, *cj;                   // [cap] particle slots of i (first) and j
+    double *dr[3];                  // [cap] r_j - r_i, minimum-imaged
+    double *rij;                    // [cap] |dr| as listed
+    int *src;                       // [cap] index in the caller's pair list
+    int *touch_count, *touch_start, *touch_fill;  // [np + 1]
+    int *touch;                     // [2 cap] candidates of each particle
+    int *pred;                      // [2 cap] previous candidate on side i / j
+    int *level;                     // [cap]
+    int *info;                      // [4]: count, overflow, max level, solver status
+};
+
+// ---- launch wrappers (sph_collide.cu) ----
+// Engine path: candidates of every simulation with collisions on, found
+// with the cell list at the evaluation positions v.xe_in.
+void launch_collide_find(const View &v, const CollideSet &c, cudaStream_t s);
+// Touch lists, predecessors and dependency levels of the current set.
+void launch_collide_levels(const CollideSet &c, cudaStream_t s);
+// Applies the set level by level to velocities vel (and positions pos with
+// push_cut > 0: CollisionForce3d's pushback).  m is indexed by slot.  With
+// pk_vel non-null the packed evaluation velocities are refreshed too.
+// err/err_any (may be null) receive SPH_ECAPACITY for nsims simulations on
+// overflow.
+void launch_collide_apply(const CollideSet &c, int dim, Vec3Ref vel, Vec3Ref pos,
+                          const double *m, double push_cut, void *pk_vel, int precision,
+                          int *err, int *err_any, int nsims, cudaStream_t s);
+// Engine path: the integrator stage from the stored rates (collisions on).
+void launch_integrate(const View &v, int precision, int integrator, int stage, cudaStream_t s);
 
 // ---- launch wrappers (sph_sort.cu) ----
 void launch_bin(const View &v, int np_a, cudaStream_t s);

@@ -308,78 +308,12 @@ __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S
     v.a_sim[i] = v.b_sim[i];
 }
 
-template <typename R, int D, int K>
-__global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int integ,
-                                                        int visc, int heat) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < v.np;
-    const int ii = active ? i : v.np - 1;
-    using T4 = typename V4<R>::T;
-    const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
-    const T4 *__restrict__ V = (const T4 *)v.pk_vel_in;
-    const T4 *__restrict__ F = (const T4 *)v.pk_f;
-    const T4 *__restrict__ Q = (const T4 *)v.pk_q;
-    const int s = v.b_sim[ii];
-    const SimDev &S = v.sims[s];
-    KConst<R> ks = make_kconst<R>(S, 0);
-    KConst<R> kl = make_kconst<R>(S, 1);
-    const SimConst<R> &sc = sconst<R>(S);
-    const R hs = sc.hs, eps_h2 = sc.eps_h2;
-    const R alpha_c = sc.alpha_c, beta = sc.beta;
-    const R pl2 = sc.pl2;  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
-    const T4 vi = V[ii], fi = F[ii];
-    const T4 qi = heat ? Q[ii] : make_v4<R>(0, 0, 0, 0);
-    BAcc<R> ax[3], ud;
-    ax[0].init(0);
-    ax[1].init(0);
-    ax[2].init(0);
-    ud.init(0);
-    auto body = [&](int j, const T4 &pj, const R *d, R rsq) {
-        R r = fsqrt<R>(rsq);
-        R gs = kernel_g<K, R>(ks, r);
-        R gl = kernel_g<K, R>(kl, r);
-        T4 fj = F[j], vj = V[j];
-        R dvdx = (vj.x - vi.x) * d[0] + (vj.y - vi.y) * d[1];
-        if (D == 3) dvdx += (vj.z - vi.z) * d[2];
-        R ps = fi.x + fj.x;
-        if (visc && dvdx < (R)0) {
-            // Monaghan viscosity on approaching pairs
-            R mu = fdiv<R>(hs * dvdx, rsq + eps_h2);
-            ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), fi.y + fj.y);
-        }
-        R gsum = ps * gs + pl2 * gl;
-        ax[0].add(gsum * d[0]);
-        ax[1].add(gsum * d[1]);
-        if (D == 3) ax[2].add(gsum * d[2]);
-        R du = (R)0.5 * gsum * dvdx * pj.w;
-        if (heat) {
-            T4 qj = Q[j];
-            R dq = (qi.x + qj.x) * d[0] + (qi.y + qj.y) * d[1];
-            if (D == 3) dq += (qi.z + qj.z) * d[2];
-            du -= dq * gs * pj.w;
-        }
-        ud.add(du);
-    };
-    auto cell_done = [&]() {
-        ax[0].flush();
-        ax[1].flush();
-        if (D == 3) ax[2].flush();
-        ud.flush();
-    };
-    if (!active) return;
-    {
-        PairFrame<R, D> fr;
-        fr.init(S);
-        for_pairs<R, D>(v, S, fr, P, i, P[i], body, cell_done);
-    }
-    R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
-    R udr = ud.get();
-    for (int a = 0; a < D; ++a) ((R *)v.vdot[a])[i] = vdr[a];
-    ((R *)v.udot)[i] = udr;
-    if (!isfinite(vdr[0]) || !isfinite(udr)) set_err(v.err, v.err_any, s, SPH_ENAN);
-    if (mode == 0) return;
-
-    // ---- integrator stage (c = xdot * dt as in integrator.py) ----
+// Integrator stage of particle i (c = xdot dt as in integrator.py:14-103)
+// from its rates vdr, udr, followed on the last stage by the teleport wrap
+// and the thermostat.
+template <typename R, int D>
+__device__ __forceinline__ void integrate_stage(const View &v, const SimDev &S, int i, int s,
+                                                int stage, int integ, const R *vdr, R udr) {
     const double dt = S.dt;
     double x0[3] = {0, 0, 0}, v0[3] = {0, 0, 0}, rd[3] = {0, 0, 0}, vd[3] = {0, 0, 0};
 #pragma unroll
@@ -468,6 +402,95 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
     }
 }
 
+template <typename R, int D, int K>
+__global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int integ,
+                                                        int visc, int heat) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < v.np;
+    const int ii = active ? i : v.np - 1;
+    using T4 = typename V4<R>::T;
+    const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
+    const T4 *__restrict__ V = (const T4 *)v.pk_vel_in;
+    const T4 *__restrict__ F = (const T4 *)v.pk_f;
+    const T4 *__restrict__ Q = (const T4 *)v.pk_q;
+    const int s = v.b_sim[ii];
+    const SimDev &S = v.sims[s];
+    KConst<R> ks = make_kconst<R>(S, 0);
+    KConst<R> kl = make_kconst<R>(S, 1);
+    const SimConst<R> &sc = sconst<R>(S);
+    const R hs = sc.hs, eps_h2 = sc.eps_h2;
+    const R alpha_c = sc.alpha_c, beta = sc.beta;
+    const R pl2 = sc.pl2;  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
+    const T4 vi = V[ii], fi = F[ii];
+    const T4 qi = heat ? Q[ii] : make_v4<R>(0, 0, 0, 0);
+    BAcc<R> ax[3], ud;
+    ax[0].init(0);
+    ax[1].init(0);
+    ax[2].init(0);
+    ud.init(0);
+    auto body = [&](int j, const T4 &pj, const R *d, R rsq) {
+        R r = fsqrt<R>(rsq);
+        R gs = kernel_g<K, R>(ks, r);
+        R gl = kernel_g<K, R>(kl, r);
+        T4 fj = F[j], vj = V[j];
+        R dvdx = (vj.x - vi.x) * d[0] + (vj.y - vi.y) * d[1];
+        if (D == 3) dvdx += (vj.z - vi.z) * d[2];
+        R ps = fi.x + fj.x;
+        if (visc && dvdx < (R)0) {
+            // Monaghan viscosity on approaching pairs
+            R mu = fdiv<R>(hs * dvdx, rsq + eps_h2);
+            ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), fi.y + fj.y);
+        }
+        R gsum = ps * gs + pl2 * gl;
+        ax[0].add(gsum * d[0]);
+        ax[1].add(gsum * d[1]);
+        if (D == 3) ax[2].add(gsum * d[2]);
+        R du = (R)0.5 * gsum * dvdx * pj.w;
+        if (heat) {
+            T4 qj = Q[j];
+            R dq = (qi.x + qj.x) * d[0] + (qi.y + qj.y) * d[1];
+            if (D == 3) dq += (qi.z + qj.z) * d[2];
+            du -= dq * gs * pj.w;
+        }
+        ud.add(du);
+    };
+    auto cell_done = [&]() {
+        ax[0].flush();
+        ax[1].flush();
+        if (D == 3) ax[2].flush();
+        ud.flush();
+    };
+    if (!active) return;
+    {
+        PairFrame<R, D> fr;
+        fr.init(S);
+        for_pairs<R, D>(v, S, fr, P, i, P[i], body, cell_done);
+    }
+    R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
+    R udr = ud.get();
+    for (int a = 0; a < D; ++a) ((R *)v.vdot[a])[i] = vdr[a];
+    ((R *)v.udot)[i] = udr;
+    if (!isfinite(vdr[0]) || !isfinite(udr)) set_err(v.err, v.err_any, s, SPH_ENAN);
+    if (mode == 0) return;
+
+    integrate_stage<R, D>(v, S, i, s, stage, integ, vdr, udr);
+}
+
+// Integrator stage from the stored rates: the epilogue of k_force as a pass
+// of its own, for steps whose velocities change between the force pass and
+// the update (hard collisions).
+template <typename R, int D>
+__global__ void __launch_bounds__(256) k_integrate(View v, int stage, int integ) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.np) return;
+    const int s = v.b_sim[i];
+    const SimDev &S = v.sims[s];
+    if (!S.active) return;
+    R vdr[3] = {0, 0, 0};
+    for (int a = 0; a < D; ++a) vdr[a] = ((const R *)v.vdot[a])[i];
+    integrate_stage<R, D>(v, S, i, s, stage, integ, vdr, ((const R *)v.udot)[i]);
+}
+
 // ---- dispatch ----
 #define SPH_DISPATCH(PREC, DIM, KERN, CALL)                                       \
     do {                                                                          \
@@ -509,6 +532,18 @@ void launch_force(const View &v, int precision, int kernel, int viscosity, int h
     SPH_DISPATCH(precision, v.dim, kernel,
                  (k_force<R, D, K><<<nb, block, 0, s>>>(v, stage, mode, integrator, viscosity,
                                                        heat)));
+}
+
+void launch_integrate(const View &v, int precision, int integrator, int stage, cudaStream_t s) {
+    if (v.np <= 0) return;
+    int nb = (v.np + 255) / 256;
+    if (precision == SPH_MIXED) {
+        if (v.dim == 2) k_integrate<float, 2><<<nb, 256, 0, s>>>(v, stage, integrator);
+        else k_integrate<float, 3><<<nb, 256, 0, s>>>(v, stage, integrator);
+    } else {
+        if (v.dim == 2) k_integrate<double, 2><<<nb, 256, 0, s>>>(v, stage, integrator);
+        else k_integrate<double, 3><<<nb, 256, 0, s>>>(v, stage, integrator);
+    }
 }
 
 // ---- thermostat: per-chunk FP64 partial sums of T, then one thread per

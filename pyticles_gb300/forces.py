@@ -13,7 +13,15 @@ computes; the arithmetic runs in libsph's force pass:
 Force.apply() runs one evaluation of the whole derivative for the
 particle system it belongs to and writes p.rho, p.rho_lr, p.t, p.p, p.pco,
 p.vdot, p.udot and p.jq, as SpamComplete.apply does (:171-183).
+
+Hard collisions (forces.py:87-243, 454-474) mutate p.v (and, for
+CollisionForce3d, p.r) over the neighbour list's pairs on the device
+(sph_collide_pairs); inside SmoothParticleSystem.update the engine applies
+CollisionForce / FortranCollisionForce after every evaluation itself.
 """
+import numpy as np
+
+from . import _abi
 
 
 class Force:
@@ -84,3 +92,62 @@ class SpamComplete(Force):
         self.thermalk = thermalk
         self.visc_eps = visc_eps
         self.sound_speed = sound_speed
+
+
+def collide(p, nl, cutoff, mode, dims=None):
+    """Force.apply of a collision force (forces.py:38-42): pairs of nl with
+    rij^2 <= cutoff^2, in list order, on the GPU.  dims: the velocity
+    components the force acts on (CollisionForce: x and y)."""
+    n, ni = p.n, nl.nip
+    if ni == 0 or n == 0:
+        return
+    dim = p.dim if dims is None else dims
+    v = np.ascontiguousarray(p.v[:n, :dim], dtype=np.float64)
+    r = np.ascontiguousarray(p.r[:n, :dim], dtype=np.float64)
+    m = np.ascontiguousarray(p.m[:n], dtype=np.float64)
+    iap = np.ascontiguousarray(nl.iap[:ni], dtype=np.int64)
+    drij = np.ascontiguousarray(nl.drij[:ni, :dim], dtype=np.float64)
+    rij = np.ascontiguousarray(nl.rij[:ni], dtype=np.float64)
+    _abi.check(_abi.lib().sph_collide_pairs(dim, mode, n, r.ctypes.data, v.ctypes.data,
+                                            m.ctypes.data, ni, iap.ctypes.data,
+                                            drij.ctypes.data, rij.ctypes.data, float(cutoff),
+                                            _abi.SPH_HOST, None), "sph_collide_pairs")
+    p.v[:n, :dim] = v
+    if mode == _abi.SPH_COLLIDE_PUSHBACK:
+        p.r[:n, :dim] = r
+        nl.drij[:ni, :dim] = drij
+        nl.rij[:ni] = rij
+
+
+class CollisionForce(Force):
+    """Hard 2D collisions (forces.py:87-156): a pair that is not separating
+    trades the x/y velocity components along its separation, scaled by the
+    mass ratio."""
+
+    mode = _abi.SPH_COLLIDE_EXCHANGE
+    dims = 2
+
+    def __init__(self, particles, neighbour_list, cutoff=5.0):
+        Force.__init__(self, particles, neighbour_list, cutoff=cutoff)
+
+    def apply(self):
+        collide(self.p, self.nl, self.cutoff, self.mode, min(self.dims, self.p.dim))
+
+
+class CollisionForce3d(CollisionForce):
+    """Hard 3D collisions with the pushback that separates the pair to
+    cutoff + 0.01 (forces.py:158-243)."""
+
+    mode = _abi.SPH_COLLIDE_PUSHBACK
+    dims = 3
+
+
+class FortranCollisionForce(CollisionForce):
+    """forces.py:454-474.  Its collide3d (Fortran) is absent from pyticles;
+    it is restated as CollisionForce3d's velocity exchange, without the
+    pushback (collide3d receives no positions)."""
+
+    dims = 3
+
+    def __init__(self, particles, neighbour_list, cutoff=1.0):
+        CollisionForce.__init__(self, particles, neighbour_list, cutoff=cutoff)

@@ -24,7 +24,8 @@ import numpy as np
 from . import _abi
 from .box import MirrorBox, PeriodicBox
 from .engine import Engine
-from .forces import CohesiveSpamForce, SpamComplete, SpamConduction, SpamForce
+from .forces import (CohesiveSpamForce, CollisionForce, CollisionForce3d, SpamComplete,
+                     SpamConduction, SpamForce)
 
 XMAX = 5
 YMAX = 5
@@ -161,7 +162,32 @@ class SmoothParticleSystem(ParticleSystem):
                                       "SpamForce + CohesiveSpamForce pair")
         if SpamConduction in kinds:
             kw["heat_flux"] = True
+        kw["collision_cutoff"] = self._collision_cutoff(cutoff, tol)
         return _abi.make_params(**kw)
+
+    def _collision_forces(self):
+        return [f for f in self.forces if isinstance(f, CollisionForce)]
+
+    def _collision_cutoff(self, cutoff, tol):
+        """The engine's collision range: CollisionForce / FortranCollisionForce
+        placed after the SPH forces (bspana.py:45-46, fspana.py:117-119)."""
+        coll = self._collision_forces()
+        if not coll:
+            return 0.0
+        f = coll[0]
+        if len(coll) > 1 or isinstance(f, CollisionForce3d):
+            raise NotImplementedError(
+                "the engine step runs one CollisionForce or FortranCollisionForce; "
+                "CollisionForce3d's pushback moves particles inside the step -- apply() it "
+                "between steps instead")
+        if self.forces.index(f) != len(self.forces) - 1:
+            raise NotImplementedError("a collision force must come after the SPH forces")
+        if self.dim == 3 and f.dims == 2:
+            raise NotImplementedError("CollisionForce (x/y only) in a 3D engine step")
+        fc, ft = f.nl._cutoff_tol()
+        if f.cutoff ** 2 > min(cutoff * cutoff + tol * tol, fc * fc + ft * ft):
+            raise NotImplementedError("collision range beyond the neighbour list's pairs")
+        return float(f.cutoff)
 
     def _ensure_engine(self, dt):
         prm = self.engine_params(dt)
@@ -213,6 +239,10 @@ class SmoothParticleSystem(ParticleSystem):
         self.vdot[:n] = out["vdot"]
         self.udot[:n] = out["udot"]
         self.jq[:n] = out["jq"]
+        # collision forces mutate v after the rates (particles.py:562-564)
+        for f in self._collision_forces():
+            f.nl.separations()
+            f.apply()
         self.rdot = self.v
         self.timing["force time"] = time.time() - t
 

@@ -287,6 +287,66 @@ def run_case(R, name, r, v, m, box_len, dim, hs, hl, cutoff, tol, kname, T0, ste
     print(f"{name}: n={n} nip={ni} steps={steps} {time.time() - t0:.1f}s -> {path}")
 
 
+def collision_case(R, name, r, v, m, box_len, dim, hs, hl, cutoff, kname, T0, steps, coll,
+                   dt=1e-3, integ="ieuler"):
+    """SmoothParticleSystem.update with p.forces = [SpamComplete's sequence,
+    forces.CollisionForce(p, nl, cutoff=coll)] -- the order of the drivers
+    (bspana.py:45-46, fspana.py:117-119)."""
+    t0 = time.time()
+    n = r.shape[0]
+    u = ref_initial_energy(R, r, v, m, box_len, dim, hs, hl, cutoff, 0.0, kname, T0)
+    p, nl, force = build_system(R, r, v, m, u, box_len, dim, hs, hl, cutoff, 0.0, kname, integ)
+    p.forces.append(R["forces"].CollisionForce(p, nl, cutoff=coll))
+    traj = []
+    for s in range(steps):
+        p.update(dt)
+        traj.append((p.r[:n, :dim].copy(), p.v[:n, :dim].copy(), p.u[:n].copy()))
+    out = dict(name=name, dim=dim, kernel=kname, box=np.array(list(box_len) + [1.0] * (3 - dim)),
+               h_short=hs, h_long=hl, cutoff=cutoff, collision_cutoff=coll, dt=dt,
+               integrator=integ, steps=steps, r0=r, v0=v, m=m, u0=u)
+    for k, (rr, vv, uu) in enumerate(traj):
+        out[f"r_step{k + 1}"], out[f"v_step{k + 1}"], out[f"u_step{k + 1}"] = rr, vv, uu
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(f"{name}: n={n} steps={steps} {time.time() - t0:.1f}s")
+
+
+def collision_lists(R):
+    """Force.apply of CollisionForce (2D) and CollisionForce3d (pushback) on
+    a VerletList built by the reference (neighbour_list.py:160-189)."""
+    particles, nlm, forces = R["particles"], R["neighbour_list"], R["forces"]
+    rng = np.random.Generator(np.random.PCG64(4242))
+    out = {}
+    for dim, n, L, cut, coll in ((2, 150, 10.0, 1.5, 0.9), (3, 200, 5.0, 1.2, 0.75)):
+        p = particles.SmoothParticleSystem(n, d=3, maxn=n, xmax=L, ymax=L, zmax=L)
+        p.r[:, :] = 0.0
+        p.v[:, :] = 0.0
+        p.r[:, :dim] = rng.uniform(0.0, L, size=(n, dim))
+        p.v[:, :dim] = rng.normal(0.0, 1.0, size=(n, dim))
+        p.m[:] = rng.uniform(0.5, 2.0, size=n)
+        nl = nlm.VerletList(p, cutoff=cut, tolerance=0.0)
+        nl.build()
+        # NeighbourList.separations (neighbour_list.py:63-83): VerletList's
+        # own leaves rij to the absent Cython pairsep
+        nlm.NeighbourList.separations(nl)
+        ni = nl.nip
+        tag = f"{dim}d"
+        out[f"r_{tag}"] = p.r[:n, :dim].copy()
+        out[f"v_{tag}"] = p.v[:n, :dim].copy()
+        out[f"m_{tag}"] = p.m[:n].copy()
+        out[f"iap_{tag}"] = nl.iap[:ni].astype(np.int64)
+        out[f"drij_{tag}"] = nl.drij[:ni, :dim].copy()
+        out[f"rij_{tag}"] = nl.rij[:ni].copy()
+        out[f"cutoff_{tag}"] = coll
+        f = (forces.CollisionForce if dim == 2 else forces.CollisionForce3d)(p, nl, cutoff=coll)
+        f.apply()
+        out[f"v_after_{tag}"] = p.v[:n, :dim].copy()
+        out[f"r_after_{tag}"] = p.r[:n, :dim].copy()
+        out[f"drij_after_{tag}"] = nl.drij[:ni, :dim].copy()
+        out[f"rij_after_{tag}"] = nl.rij[:ni].copy()
+    np.savez_compressed(os.path.join(HERE, "collide_lists.npz"), **out)
+    print("collide_lists:", {k: v.shape for k, v in out.items() if k.startswith("iap")})
+
+
 def kernel_table(R):
     spk = R["spkernel"]
     rows = []
@@ -416,6 +476,13 @@ def main():
             pair_edge_cases(R)
         if want("splat"):
             splat_maps(R)
+        if want("collide_lists"):
+            collision_lists(R)
+        if want("collide2d_144"):
+            prm, r, v, m, T0 = workloads.lattice_system(12, 2, spacing=1.0, jitter=0.1,
+                                                        temperature=0.6, seed=18)
+            collision_case(R, "collide2d_144", r, v, m, (12.0, 12.0), 2, 2.0, 3.0, 3.0, "lucy",
+                           T0, steps=3, coll=0.95)
         if want("lucy3d_27"):
             prm, r, v, m, T0 = workloads.lattice_system(3, 3, spacing=1.1, jitter=0.1,
                                                         temperature=0.6, seed=11)

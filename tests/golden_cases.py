@@ -39,3 +39,14 @@ def sort_pairs(iap):
     hi = np.maximum(iap[:, 0], iap[:, 1])
     idx = np.lexsort((hi, lo))
     return np.stack([lo[idx], hi[idx]], axis=1), idx
+
+
+def collide_params(g, **over):
+    """Engine parameters of a collision fixture (collision_case in make_golden.py)."""
+    kw = dict(dim=int(g["dim"]), kernel=str(g["kernel"]), box=[float(x) for x in g["box"]],
+              h_short=float(g["h_short"]), h_long=float(g["h_long"]),
+              cutoff=float(g["cutoff"]), tolerance=0.0, dt=float(g["dt"]),
+              integrator=str(g["integrator"]), viscosity=False, heat_flux=False,
+              collision_cutoff=float(g["collision_cutoff"]))
+    kw.update(over)
+    return make_params(**kw)

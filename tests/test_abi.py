@@ -3,6 +3,8 @@ point include/sph.h declares; host-side parameter handling.  CPU only."""
 import ctypes
 import os
 import re
+import shutil
+import subprocess
 
 import pytest
 
@@ -40,10 +42,28 @@ def test_library_loads_and_reports_status_strings(libpath):
         assert s.startswith(name)
 
 
-def test_struct_layout_matches_header():
-    # 6 int32 + 3 doubles box + 15 doubles + int64
-    assert ctypes.sizeof(_abi.SphParams) == 6 * 4 + 3 * 8 + 15 * 8 + 8
-    assert _abi.SphParams.box.offset == 24
+def test_struct_layout_matches_header(tmp_path):
+    # 8 int32 + 3 doubles box + 15 doubles + int64 + collision cutoff
+    assert ctypes.sizeof(_abi.SphParams) == 8 * 4 + 3 * 8 + 15 * 8 + 8 + 8
+    assert _abi.SphParams.box.offset == 32
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stddef.h>\n#include <stdio.h>\n#include "sph.h"\n'
+        'int main(void) { printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(sph_params),'
+        ' offsetof(sph_params, box), offsetof(sph_params, thermostat_ramp_steps),'
+        ' offsetof(sph_params, collision_cutoff), sizeof(sph_tuning),'
+        ' offsetof(sph_tuning, cell_ratio)); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    P, T = _abi.SphParams, _abi.SphTuning
+    assert got == [ctypes.sizeof(P), P.box.offset, P.thermostat_ramp_steps.offset,
+                   P.collision_cutoff.offset, ctypes.sizeof(T), T.cell_ratio.offset]
 
 
 def test_make_params_defaults_follow_reference():

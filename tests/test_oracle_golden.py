@@ -99,3 +99,49 @@ def test_steps_match_reference(name):
     for k in ("rho", "rho_lr", "t", "p", "pco", "vdot", "udot"):
         err = rel_l2(props[k], g["after_" + k])
         assert err < STEP_TOL, (k, err)
+
+
+# Collisions: the reference squares with pow() (`dr[0]**2`), 1 ulp away from
+# dr*dr for ~0.3% of inputs, and rij after a pushback is np.linalg.norm; both
+# leave last-bit differences in chained updates.
+COLLIDE_ULP = 8
+
+
+def assert_ulp_close(a, b, ulp=COLLIDE_ULP):
+    a, b = np.asarray(a), np.asarray(b)
+    assert np.all(np.abs(a - b) <= ulp * np.spacing(np.maximum(np.abs(a), np.abs(b))))
+
+
+@pytest.mark.parametrize("tag, mode", [("2d", 1), ("3d", 2)])
+def test_collision_lists_match_reference(tag, mode):
+    """CollisionForce (2D) and CollisionForce3d (pushback) Force.apply on a
+    reference VerletList (forces.py:38-42, 87-243)."""
+    g = load("collide_lists")
+    r, v, drij, rij = oracle.collide_pairs(mode, g["r_" + tag], g["v_" + tag], g["m_" + tag],
+                                           g["iap_" + tag], g["drij_" + tag],
+                                           g["rij_" + tag], float(g["cutoff_" + tag]))
+    c = float(g["cutoff_" + tag])
+    assert np.count_nonzero(g["rij_" + tag] ** 2 <= c * c) > 100   # long chains of pairs
+    assert_ulp_close(v, g["v_after_" + tag])
+    assert_ulp_close(r, g["r_after_" + tag])
+    assert_ulp_close(drij, g["drij_after_" + tag])
+    assert_ulp_close(rij, g["rij_after_" + tag])
+
+
+def test_collision_steps_match_reference():
+    """SmoothParticleSystem.update with SpamForce + CohesiveSpamForce and a
+    CollisionForce after them: the extra first evaluation's collisions and
+    each stage's collided velocities (particles.py:459-494, integrator.py)."""
+    from tests.golden_cases import collide_params
+    g = load("collide2d_144")
+    prm = collide_params(g)
+    r, v, u = g["r0"], g["v0"], g["u0"]
+    for k in range(1, int(g["steps"]) + 1):
+        r, v, u, _ = oracle.advance(prm, r, v, g["m"], u, 1, step0=k - 1)
+        assert rel_l2(r, g[f"r_step{k}"]) < 1e-15
+        assert rel_l2(v, g[f"v_step{k}"]) < 1e-15
+        assert rel_l2(u, g[f"u_step{k}"]) < 1e-15
+    # the collisions matter: without them the velocities differ at O(1)
+    _, v_free, _, _ = oracle.advance(collide_params(g, collision_cutoff=0.0), g["r0"], g["v0"],
+                                     g["m"], g["u0"], int(g["steps"]))
+    assert rel_l2(v_free, g["v_step3"]) > 0.1
