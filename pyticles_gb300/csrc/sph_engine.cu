@@ -101,7 +101,7 @@ struct sph_engine {
     int *cell_xyz = nullptr;
     double *org[3] = {};
     int *scan_tmp = nullptr;
-    void *pk_pos[2] = {}, *pk_vel[2] = {}, *pk_f = nullptr, *pk_q = nullptr;
+    void *pk_pos[2] = {}, *pk_vel[2] = {}, *pk_f = nullptr, *pk_q = nullptr, *pk_fv = nullptr;
     double *xe[2][3] = {}, *ve[3] = {}, *ue = nullptr;
     void *rho = nullptr, *rho_l = nullptr, *temp = nullptr, *pres = nullptr, *pco = nullptr;
     void *rho0 = nullptr, *pres0 = nullptr, *pco0 = nullptr;
@@ -409,6 +409,7 @@ View make_view(const sph_engine *e) {
     for (int a = 0; a < 3; ++a) v.org[a] = e->org[a];
     v.pk_f = e->pk_f;
     v.pk_q = e->pk_q;
+    v.pk_fv = e->pk_fv;
     v.rho = e->rho;
     v.rho_l = e->rho_l;
     v.temp = e->temp;
@@ -781,6 +782,7 @@ int alloc_particles(sph_engine *e) {
     }
     TRY(dalloc((char **)&e->pk_f, P * e->v4size));
     TRY(dalloc((char **)&e->pk_q, P * e->v4size));
+    TRY(dalloc((char **)&e->pk_fv, P * e->v4size));
     void **rs[] = {&e->rho, &e->rho_l, &e->temp, &e->pres, &e->pco, &e->rho0, &e->pres0,
                    &e->pco0, &e->udot, &e->f0u};
     for (void **p : rs) TRY(dalloc((char **)p, P * e->rsize));
@@ -834,7 +836,7 @@ void free_all(sph_engine *e) {
     void *ptrs[] = {e->a_u, e->a_m, e->a_id, e->a_sim, e->b_u, e->b_m, e->b_id, e->b_sim,
                     e->cell_of, e->rank, e->order_tmp, e->order, e->cell_b, e->cell_count,
                     e->cell_start, e->morton, e->scan_tmp, e->pk_pos[0], e->pk_pos[1],
-                    e->pk_vel[0], e->pk_vel[1], e->pk_f, e->pk_q, e->ue, e->rho, e->rho_l,
+                    e->pk_vel[0], e->pk_vel[1], e->pk_f, e->pk_q, e->pk_fv, e->ue, e->rho, e->rho_l,
                     e->temp, e->pres, e->pco, e->rho0, e->pres0, e->pco0, e->udot, e->f0u,
                     e->acc_u, e->stage_buf, e->sims_d, e->t_scale, e->tsum_part, e->steps_d,
                     e->pair_count, e->err, e->err_any, e->chunk_sim, e->chunk_start,

@@ -171,6 +171,7 @@ extern "C" int sph_derivatives_noalloc(const sph_params *p, int32_t precision, i
     w.pk_vel_in = w.pk_vel_out = c.take<char>(N * v4);
     w.pk_f = c.take<char>(N * v4);
     w.pk_q = c.take<char>(N * v4);
+    w.pk_fv = c.take<char>(N * v4);
     void **scalars[] = {&w.rho, &w.rho_l, &w.temp, &w.pres, &w.pco, &w.rho0, &w.pres0, &w.pco0,
                         &w.udot};
     for (void **sp : scalars) *sp = c.take<char>(N * rs);

@@ -218,6 +218,10 @@ __global__ void __launch_bounds__(256) k_density(View v, int stage) {
     // {p/rho^2, rho, T_hi, T_lo}: T as a hi/lo pair so that T_j - T_i in the
     // heat pass does not lose the low bits
     ((T4 *)v.pk_f)[i] = make_v4<R>((R)fs, (R)rho, Th, (R)(T - (double)Th));
+    // what the force pass reads of a neighbour, in one 16-byte load in 2D
+    const T4 vi = ((const T4 *)v.pk_vel_in)[i];
+    ((T4 *)v.pk_fv)[i] = D == 2 ? make_v4<R>(vi.x, vi.y, (R)fs, (R)rho)
+                                : make_v4<R>(vi.x, vi.y, vi.z, (R)fs);
     if (!isfinite((R)p) || !isfinite((R)rho) || !isfinite((R)rhol))
         set_err(v.err, v.err_any, s, SPH_ENAN);
     add_pair_count(v.pair_count, s, cnt);
@@ -402,16 +406,21 @@ __device__ __forceinline__ void integrate_stage(const View &v, const SimDev &S, 
     }
 }
 
-template <typename R, int D, int K>
-__global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int integ,
-                                                        int visc, int heat) {
+// VH: bit 0 viscosity, bit 1 heat flux (compile-time, so a workload without
+// them carries neither their registers nor their branches)
+// At most 64 registers (4 blocks of 256 per SM): measured 17% faster than the
+// unconstrained 80-104 despite a few spilled words outside the pair loop.
+template <typename R, int D, int K, int VH>
+__global__ void __launch_bounds__(256, 4) k_force(View v, int stage, int mode, int integ) {
+    constexpr bool visc = (VH & 1) != 0;
+    constexpr bool heat = (VH & 2) != 0;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
     using T4 = typename V4<R>::T;
     const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
-    const T4 *__restrict__ V = (const T4 *)v.pk_vel_in;
-    const T4 *__restrict__ F = (const T4 *)v.pk_f;
+    const T4 *__restrict__ FV = (const T4 *)v.pk_fv;
+    const R *__restrict__ RHO = (const R *)v.rho;
     const T4 *__restrict__ Q = (const T4 *)v.pk_q;
     const int s = v.b_sim[ii];
     const SimDev &S = v.sims[s];
@@ -421,7 +430,11 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
     const R hs = sc.hs, eps_h2 = sc.eps_h2;
     const R alpha_c = sc.alpha_c, beta = sc.beta;
     const R pl2 = sc.pl2;  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
-    const T4 vi = V[ii], fi = F[ii];
+    // own velocity, p/rho^2 and rho
+    const T4 fvi = FV[ii];
+    const R vix = fvi.x, viy = fvi.y, viz = D == 3 ? fvi.z : (R)0;
+    const R fsi = D == 2 ? fvi.z : fvi.w;
+    const R rhoi = D == 2 ? fvi.w : RHO[ii];
     const T4 qi = heat ? Q[ii] : make_v4<R>(0, 0, 0, 0);
     BAcc<R> ax[3], ud;
     ax[0].init(0);
@@ -432,14 +445,15 @@ __global__ void __launch_bounds__(256) k_force(View v, int stage, int mode, int 
         R r = fsqrt<R>(rsq);
         R gs = kernel_g<K, R>(ks, r);
         R gl = kernel_g<K, R>(kl, r);
-        T4 fj = F[j], vj = V[j];
-        R dvdx = (vj.x - vi.x) * d[0] + (vj.y - vi.y) * d[1];
-        if (D == 3) dvdx += (vj.z - vi.z) * d[2];
-        R ps = fi.x + fj.x;
+        const T4 fvj = FV[j];
+        R dvdx = (fvj.x - vix) * d[0] + (fvj.y - viy) * d[1];
+        if (D == 3) dvdx += (fvj.z - viz) * d[2];
+        R ps = fsi + (D == 2 ? fvj.z : fvj.w);
         if (visc && dvdx < (R)0) {
             // Monaghan viscosity on approaching pairs
+            const R rhoj = D == 2 ? fvj.w : RHO[j];
             R mu = fdiv<R>(hs * dvdx, rsq + eps_h2);
-            ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), fi.y + fj.y);
+            ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), rhoi + rhoj);
         }
         R gsum = ps * gs + pl2 * gl;
         ax[0].add(gsum * d[0]);
@@ -529,9 +543,17 @@ void launch_force(const View &v, int precision, int kernel, int viscosity, int h
                   int integrator, int stage, int mode, int block, cudaStream_t s) {
     if (v.np <= 0) return;
     int nb = (v.np + block - 1) / block;
-    SPH_DISPATCH(precision, v.dim, kernel,
-                 (k_force<R, D, K><<<nb, block, 0, s>>>(v, stage, mode, integrator, viscosity,
-                                                       heat)));
+    const int vh = (viscosity ? 1 : 0) | (heat ? 2 : 0);
+#define SPH_FORCE(VH_) k_force<R, D, K, VH_><<<nb, block, 0, s>>>(v, stage, mode, integrator)
+    SPH_DISPATCH(precision, v.dim, kernel, ({
+                     switch (vh) {
+                         case 0: SPH_FORCE(0); break;
+                         case 1: SPH_FORCE(1); break;
+                         case 2: SPH_FORCE(2); break;
+                         default: SPH_FORCE(3); break;
+                     }
+                 }));
+#undef SPH_FORCE
 }
 
 void launch_integrate(const View &v, int precision, int integrator, int stage, cudaStream_t s) {
