@@ -187,8 +187,9 @@ typedef struct sph_tuning {
     int32_t reserved;         /* must be 0                                      */
     double cell_ratio;        /* cell edge / (cutoff + skin): 1 -> cells of the
                                  cutoff and a 3^d window, 1/2 -> half-size cells
-                                 and a 5^d window, 1/3 -> 7^d; cells beyond the
-                                 cutoff from a particle are skipped            */
+                                 and a 5^d window, 1/3 -> 7^d (down to 1/5);
+                                 cells beyond the cutoff from a particle are
+                                 skipped                                       */
 } sph_tuning;
 int sph_get_tuning(sph_engine *e, sph_tuning *t);
 int sph_set_tuning(sph_engine *e, const sph_tuning *t);

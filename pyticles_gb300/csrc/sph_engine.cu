@@ -252,6 +252,12 @@ void fill_const(SimConst<R> &c, const sph_engine *e, const Sim &S, const SimDev 
     const sph_params &p = S.prm;
     c.thr_lo = (R)(d.thr * (1.0 - margin));
     c.thr_hi = (R)(d.thr * (1.0 + margin));
+    // compact short kernels vanish beyond h (Lucy, Debrun) or 2h (cubic); the
+    // margin keeps every pair the FP32 kernel could still see as q < 1
+    double supp = p.kernel == SPH_KERNEL_CUBIC ? 2.0 * p.h_short : p.h_short;
+    c.thr_s = c.thr_hi;
+    if (p.kernel != SPH_KERNEL_GAUSSIAN && supp * supp * (1.0 + 1.0 / 1024.0) < d.thr)
+        c.thr_s = (R)(supp * supp * (1.0 + 1.0 / 1024.0));
     for (int a = 0; a < 3; ++a) {
         c.edge[a] = (R)S.edge[a];
         c.L[a] = (R)p.box[a];
@@ -926,8 +932,8 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->cap_s = max_sims;
     e->tune.block_size = 128;
     e->tune.reserved = 0;
-    // measured on GB300: 1/3-cutoff cells in 2D, 1/2 in 3D (autotune.py re-tunes)
-    e->tune.cell_ratio = group->dim == 2 ? 1.0 / 3.0 : 0.5;
+    // measured on GB300: half-cutoff cells in 2D and 3D (autotune.py re-tunes)
+    e->tune.cell_ratio = 0.5;
     e->tune.use_graph = 1;
     e->tune.steps_per_graph = 1;
     if (stream) {
@@ -1316,7 +1322,7 @@ int sph_get_tuning(sph_engine *e, sph_tuning *t) {
 int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
     if (!e || !t) return SPH_EINVAL;
     if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) ||
-        !(t->cell_ratio >= 0.3 && t->cell_ratio <= 4.0) || t->reserved != 0 ||
+        !(t->cell_ratio >= 0.2 && t->cell_ratio <= 4.0) || t->reserved != 0 ||
         t->steps_per_graph < 1)
         return SPH_EINVAL;
     bool regrid = t->cell_ratio != e->tune.cell_ratio;

@@ -28,6 +28,8 @@ constexpr int kMaxNbr = 27;
 // division) deriving them.  Index 0 = short smoothing length, 1 = long.
 template <typename R> struct SimConst {
     R thr_lo, thr_hi;            // fast-test band around cutoff^2 + tolerance^2
+    R thr_s;                     // short kernel's support^2 (grown by a margin, at
+                                 // most thr_hi): beyond it W_s = grad W_s = 0
     R edge[3], L[3], hL[3];
     R ext[3];                    // half cell extent + allowed drift (culling)
     R h[2], inv_h[2], inv_h_lo[2], sig[2], g0[2];
