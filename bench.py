@@ -217,13 +217,14 @@ def fluid3d_workload(side):
     return [(prm, r, v, m, u)]
 
 
-def timed_workload(sims, steps, warmup, torch, stream, tune=True):
+def timed_workload(sims, steps, warmup, torch, stream, tune=True, rebin=0):
     """Autotunes on a sample, then times `steps` graph-captured steps."""
     knobs = None
     if tune:
         from pyticles_gb300 import autotune
         knobs, _ = autotune.tune(sims[0][0], "mixed",
                                  autotune.sample_sims(sims, 1 << 20), steps=3, warmup=2)
+    knobs = dict(knobs or {}, rebin=rebin)
     ms, pairs, passes, kps = run_timed(None, None, None, None, None, "mixed", steps, warmup,
                                        torch, stream, knobs=knobs, sims=sims)
     n = sum(len(x[1]) for x in sims)
@@ -348,6 +349,9 @@ def main():
     ap.add_argument("--steps3d", type=int, default=20)
     ap.add_argument("--serve-jobs", type=int, default=12)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--rebin", type=int, default=1, choices=[0, 1],
+                    help="single-simulation workloads: 1 bins into cells on demand "
+                         "(tuning.rebin), 0 every step")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -373,6 +377,7 @@ def main():
     knobs = None
     if not args.no_tune:
         knobs, _ = autotune.tune(prm, "mixed", [(prm, r, v, m, u)], steps=3, warmup=2)
+    knobs = dict(knobs or {}, rebin=args.rebin)
     if dist:
         dist.barrier()
     with ClockSampler(local) as clocks:
@@ -407,7 +412,7 @@ def main():
         extras["batched"] = timed_workload(batched_workload(args.batched_sims),
                                            args.batched_steps, 3, torch, stream)
         extras["fluid3d"] = timed_workload(fluid3d_workload(args.side3d), args.steps3d, 3,
-                                           torch, stream)
+                                           torch, stream, rebin=args.rebin)
         extras["serve"] = serve_window(args.serve_jobs, args.serve_seconds)
 
     cpu = None

@@ -23,6 +23,7 @@
  *                                       properties.spam_properties       properties.py:63-120
  *                                       forces.SpamForce/CohesiveSpamForce forces.py:321-405
  *   sph_sim_pair_count / export_pairs   VerletList.build + separations   neighbour_list.py:160-189, 63-83
+ *   sph_tuning.rebin, sph_rebin_count   VerletList.compress/ponder_rebuild neighbour_list.py:191-234
  *   sph_collide_pairs                   CollisionForce / CollisionForce3d forces.py:87-243
  *                                       FortranCollisionForce            forces.py:454-474
  *                                       Force.apply (cutoff test)        forces.py:38-42
@@ -184,7 +185,16 @@ typedef struct sph_tuning {
     int32_t block_size;       /* threads per block of the pair passes          */
     int32_t use_graph;        /* capture each advance chunk as a CUDA graph     */
     int32_t steps_per_graph;  /* steps unrolled into one graph                  */
-    int32_t reserved;         /* must be 0                                      */
+    int32_t rebin;            /* 0: bin the particles into cells every step.
+                                 1: keep the cells of the last binning until a
+                                 particle has used half of the cell slack --
+                                 VerletList.compress / ponder_rebuild's skin
+                                 reuse (neighbour_list.py:191-234); the pair
+                                 set stays exact at every evaluation.  Improved
+                                 Euler and RK4 (Euler bins every step).  The
+                                 summation order then depends on when the
+                                 engine last binned, so a simulation equals
+                                 itself alone only to rounding             */
     double cell_ratio;        /* cell edge / (cutoff + skin): 1 -> cells of the
                                  cutoff and a 3^d window, 1/2 -> half-size cells
                                  and a 5^d window, 1/3 -> 7^d (down to 1/5);
@@ -193,6 +203,10 @@ typedef struct sph_tuning {
 } sph_tuning;
 int sph_get_tuning(sph_engine *e, sph_tuning *t);
 int sph_set_tuning(sph_engine *e, const sph_tuning *t);
+
+/* Binnings (counting sorts into cells) performed since the engine was
+ * created: one per step with tuning.rebin == 0. */
+int sph_rebin_count(sph_engine *e, int64_t *n);
 
 /* Instantiates (and caches) the CUDA graph of tuning.steps_per_graph steps
  * for the current layout without running it, so a later sph_advance starts

@@ -82,7 +82,7 @@ class SphTuning(ctypes.Structure):
         ("block_size", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
         ("steps_per_graph", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("rebin", ctypes.c_int32),
         ("cell_ratio", ctypes.c_double),
     ]
 
@@ -182,6 +182,7 @@ def _declare(lib):
         "sph_get_tuning": [vp, P(SphTuning)],
         "sph_set_tuning": [vp, P(SphTuning)],
         "sph_prepare": [vp],
+        "sph_rebin_count": [vp, P(c_i64)],
         "sph_profile": [vp, c_i32],
         "sph_profile_read": [vp, P(ctypes.c_double), P(c_i64)],
         "sph_kernels_per_step": [vp, P(c_i64)],
@@ -209,7 +210,7 @@ def exported_symbols():
             "sph_sim_set_state", "sph_sim_get_state", "sph_sim_get_properties",
             "sph_sim_count", "sph_sim_steps", "sph_sim_set_steps", "sph_advance", "sph_sim_derivatives", "sph_sim_pair_count",
             "sph_sim_export_pairs", "sph_last_pair_total", "sph_sim_diagnostics",
-            "sph_get_tuning", "sph_set_tuning", "sph_prepare", "sph_profile",
+            "sph_get_tuning", "sph_set_tuning", "sph_rebin_count", "sph_prepare", "sph_profile",
             "sph_profile_read", "sph_kernels_per_step", "sph_sync", "sph_sim_status",
             "sph_splash_map", "sph_collide_pairs", "sph_derivatives_noalloc", "sph_status_string", "sph_version"]
 

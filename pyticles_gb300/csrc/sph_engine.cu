@@ -115,6 +115,9 @@ struct sph_engine {
     int *err = nullptr, *err_any = nullptr;
     int *chunk_sim = nullptr, *chunk_start = nullptr, *chunk_len = nullptr;
     CollideSet coll = {};          // hard-collision candidates (group.collision)
+    int *rebin_gate = nullptr;     // tuning.rebin: bin before the next step
+    unsigned long long *bin_count = nullptr;
+    bool bins_valid = false;       // B, its packed copies and the cells match A
 
     // profiling: event pairs recorded around each pass
     bool prof_on = false;
@@ -302,6 +305,9 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
         d.nc[a] = S.nc[a];
         d.win[a] = S.win[a];
         d.slack_half[a] = (a < e->dim && S.win[a] > 0) ? 0.5 * (S.win[a] * S.edge[a] - rc) : 1e300;
+        d.box_half[a] = (a < e->dim && S.win[a] > 0) ? 0.5 * S.edge[a] + d.slack_half[a] : 1e300;
+        d.rebin_half[a] =
+            (a < e->dim && S.win[a] > 0) ? 0.5 * S.edge[a] + 0.5 * d.slack_half[a] : 1e300;
         if (a < e->dim && S.nc[a] == 1) d.small_mask |= (1 << a);
     }
     d.active = S.active ? 1 : 0;
@@ -437,8 +443,13 @@ View make_view(const sph_engine *e) {
     v.pair_count = e->pair_count;
     v.err = e->err;
     v.err_any = e->err_any;
+    v.bin_count = e->bin_count;
     return v;
 }
+
+// Binning on demand applies to multi-stage integrators: their last stage
+// writes packed buffer 0, which no evaluation of that stage reads.
+bool rebin_on_demand(const sph_engine *e) { return e->tune.rebin != 0 && e->nstage > 1; }
 
 // Evaluation buffers of stage s: stage 0 reads the permuted x0 (B) and
 // packed buffer 0; stage s >= 1 reads what stage s-1's force pass wrote.
@@ -461,6 +472,7 @@ void stage_view(const sph_engine *e, View &v, int s) {
 // Rebuilds the host-side layout: cell offsets, concatenated Morton and
 // neighbour tables, particle offsets and reduction chunks; uploads them.
 int relayout(sph_engine *e) {
+    e->bins_valid = false;
     int cell_off = 0, part_off = 0;
     e->any_thermostat = false;
     for (auto &S : e->sims) {
@@ -550,20 +562,28 @@ struct ProfScope {
 
 constexpr int kSortKernels = 7;  // bin, 3 scan, scatter, in-cell order, permute
 
-// Counting sort of A into B plus the packed first-evaluation copies.
-void enqueue_prepare(sph_engine *e, cudaStream_t st) {
+// Counting sort of A into B plus the packed first-evaluation copies.  Gated:
+// the kernels run only if the device gate is raised (binning on demand); the
+// close kernel then lowers it and counts the binning.
+void enqueue_prepare(sph_engine *e, cudaStream_t st, bool gated = false) {
     ProfScope ps(e, SPH_PASS_SORT, st);
     View v = make_view(e);
     stage_view(e, v, 0);
     v.pk_pos_out = e->pk_pos[0];
     v.pk_vel_out = e->pk_vel[0];
-    cudaMemsetAsync(e->cell_count, 0, sizeof(int) * std::max(e->ncells_total, 1), st);
+    const int *gate = gated ? e->rebin_gate : nullptr;
+    v.rebin_gate = gated ? e->rebin_gate : nullptr;
+    if (gated)
+        launch_fill_int(e->cell_count, 0, std::max(e->ncells_total, 1), st, gate);
+    else
+        cudaMemsetAsync(e->cell_count, 0, sizeof(int) * std::max(e->ncells_total, 1), st);
     cudaMemsetAsync(e->pair_count, 0, sizeof(unsigned long long) * e->cap_s, st);
     launch_bin(v, e->a_extent, st);
-    launch_scan(e->cell_count, e->cell_start, e->ncells_total, e->scan_tmp, st);
+    launch_scan(e->cell_count, e->cell_start, e->ncells_total, e->scan_tmp, st, gate);
     launch_scatter(v, e->a_extent, st);
     launch_cellsort(v, e->ncells_total, st);
     launch_permute(v, e->precision, st);
+    if (gated) launch_rebin_close(e->rebin_gate, e->bin_count, st);
 }
 
 // Collision candidates at the evaluation positions of v and their levels.
@@ -594,6 +614,10 @@ void enqueue_collide_apply(sph_engine *e, int s, bool packed, cudaStream_t st) {
 void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
     View v = make_view(e);
     stage_view(e, v, s);
+    if (mode == 1 && s == e->nstage - 1 && rebin_on_demand(e)) {
+        v.reuse = 1;
+        v.rebin_gate = e->rebin_gate;
+    }
     int blk = e->tune.block_size;
     const bool coll = mode == 1 && e->group.collision != SPH_COLLIDE_OFF;
     if (coll && s == 0) {
@@ -626,7 +650,7 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
 }
 
 void enqueue_step(sph_engine *e, cudaStream_t st) {
-    enqueue_prepare(e, st);
+    enqueue_prepare(e, st, rebin_on_demand(e));
     for (int s = 0; s < e->nstage; ++s) enqueue_stage(e, s, 1, st);
 }
 
@@ -637,6 +661,7 @@ int64_t kernels_per_step(const sph_engine *e) {
     // collisions: per find 5 kernels + 7 for the levels, one apply per
     // evaluation plus the extra first one, one integrator pass per stage
     if (e->group.collision != SPH_COLLIDE_OFF) k += (int64_t)e->nstage * 14 + 1;
+    if (rebin_on_demand(e)) k += 2;   // gated cell-count fill and close
     return k;
 }
 
@@ -828,6 +853,10 @@ int alloc_sims(sph_engine *e) {
     TRY(dalloc(&e->pair_count, S));
     TRY(dalloc(&e->err, S));
     TRY(dalloc(&e->err_any, 1));
+    TRY(dalloc(&e->rebin_gate, 1));
+    TRY(dalloc(&e->bin_count, 1));
+    CK(cudaMemset(e->rebin_gate, 0, sizeof(int)));
+    CK(cudaMemset(e->bin_count, 0, sizeof(unsigned long long)));
     CK(cudaMemset(e->err, 0, sizeof(int) * S));
     CK(cudaMemset(e->err_any, 0, sizeof(int)));
     CK(cudaMemset(e->steps_d, 0, sizeof(long long) * S));
@@ -845,7 +874,8 @@ void free_all(sph_engine *e) {
                     e->pk_vel[0], e->pk_vel[1], e->pk_f, e->pk_q, e->pk_fv, e->ue, e->rho, e->rho_l,
                     e->temp, e->pres, e->pco, e->rho0, e->pres0, e->pco0, e->udot, e->f0u,
                     e->acc_u, e->stage_buf, e->sims_d, e->t_scale, e->tsum_part, e->steps_d,
-                    e->pair_count, e->err, e->err_any, e->chunk_sim, e->chunk_start,
+                    e->pair_count, e->err, e->err_any, e->rebin_gate, e->bin_count,
+                    e->chunk_sim, e->chunk_start,
                     e->chunk_len, e->cell_xyz};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -931,7 +961,7 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->cap_p = max_particles;
     e->cap_s = max_sims;
     e->tune.block_size = 128;
-    e->tune.reserved = 0;
+    e->tune.rebin = 0;
     // measured on GB300: half-cutoff cells in 2D and 3D (autotune.py re-tunes)
     e->tune.cell_ratio = 0.5;
     e->tune.use_graph = 1;
@@ -1020,6 +1050,7 @@ int sph_sim_add(sph_engine *e, const sph_params *p, int64_t n, const double *r, 
     e->a_extent += (int)n;
     e->layout_dirty = true;
     e->props_valid = false;
+    e->bins_valid = false;
     *sim_id = id;
     return SPH_OK;
 }
@@ -1032,6 +1063,7 @@ int sph_sim_remove(sph_engine *e, int32_t id) {
     S.active = false;
     e->layout_dirty = true;
     e->props_valid = false;
+    e->bins_valid = false;
     return SPH_OK;
 }
 
@@ -1049,6 +1081,7 @@ int sph_sim_set_state(sph_engine *e, int32_t id, const double *r, const double *
     }
     CK(cudaStreamSynchronize(e->stream));
     e->props_valid = false;
+    e->bins_valid = false;
     return SPH_OK;
 }
 
@@ -1114,6 +1147,11 @@ int sph_advance(sph_engine *e, int32_t nsteps) {
     // left, A holds dropped or unsorted particles beyond the live count;
     // that first step runs eagerly, after which A is compact (extent == live).
     if (e->prof_on) TRY(ensure_prof_pool(e, e->prof_used + (size_t)nsteps * 2 * (1 + 4 * e->nstage) + 8));
+    if (rebin_on_demand(e) && !e->bins_valid) {
+        // the state or the layout changed since the last step: bin first
+        launch_fill_int(e->rebin_gate, 1, 1, st);
+        e->bins_valid = true;
+    }
     if (e->a_extent != e->np_b) {
         enqueue_step(e, st);
         after_advance(e, 1);
@@ -1322,7 +1360,7 @@ int sph_get_tuning(sph_engine *e, sph_tuning *t) {
 int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
     if (!e || !t) return SPH_EINVAL;
     if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) ||
-        !(t->cell_ratio >= 0.2 && t->cell_ratio <= 4.0) || t->reserved != 0 ||
+        !(t->cell_ratio >= 0.2 && t->cell_ratio <= 4.0) || (t->rebin != 0 && t->rebin != 1) ||
         t->steps_per_graph < 1)
         return SPH_EINVAL;
     bool regrid = t->cell_ratio != e->tune.cell_ratio;
@@ -1334,6 +1372,16 @@ int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
         e->layout_dirty = true;
         e->props_valid = false;
     }
+    e->bins_valid = false;
+    return SPH_OK;
+}
+
+int sph_rebin_count(sph_engine *e, int64_t *n) {
+    if (!e || !n) return SPH_EINVAL;
+    unsigned long long c = 0;
+    CK(cudaMemcpyAsync(&c, e->bin_count, sizeof(c), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    *n = (int64_t)c;
     return SPH_OK;
 }
 

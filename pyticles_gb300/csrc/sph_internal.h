@@ -41,6 +41,9 @@ struct SimDev {
     double L[3], half_L[3], inv_L[3];
     double edge[3], inv_edge[3];
     double slack_half[3];   // max displacement per axis between binning and an evaluation
+    double box_half[3];     // 0.5 edge + slack_half: a particle must stay this close
+                            // to its cell centre (SPH_ESKIN beyond)
+    double rebin_half[3];   // 0.5 edge + slack_half / 2: past it, bin again (rebin mode)
     int nc[3];
     int win[3];             // neighbour window: +-win cells per axis (0 on single-cell axes)
     int small_mask;         // bit a set: axis a has one cell (minimum image in the pair pass)
@@ -110,6 +113,13 @@ struct View {
     unsigned long long *pair_count;  // per sim (pairs x2 counted by gather)
     int *err;               // per sim error word
     int *err_any;
+    // binning on demand (tuning.rebin): the binning kernels run only while
+    // *rebin_gate != 0; with reuse set the last stage also writes B and the
+    // stage-0 packed arrays for the next step and raises *rebin_gate once a
+    // particle has used half of its cell slack
+    int *rebin_gate;
+    int reuse;
+    unsigned long long *bin_count;
 };
 
 // Strided view of an n x 3 (SoA, stride 1) or n x dim (row-major, stride
@@ -157,7 +167,8 @@ void launch_integrate(const View &v, int precision, int integrator, int stage, c
 
 // ---- launch wrappers (sph_sort.cu) ----
 void launch_bin(const View &v, int np_a, cudaStream_t s);
-void launch_scan(int *count, int *start, int n, int *block_tmp, cudaStream_t s);
+void launch_scan(int *count, int *start, int n, int *block_tmp, cudaStream_t s,
+                 const int *gate = nullptr);
 void launch_scatter(const View &v, int np_a, cudaStream_t s);
 void launch_cellsort(const View &v, int ncells, cudaStream_t s);
 void launch_permute(const View &v, int precision, cudaStream_t s);
@@ -168,7 +179,9 @@ void launch_store_scalar(double *dst, const double *src, const int *id, int off,
                          cudaStream_t s);
 void launch_store_R(double *dst, const void *src, int precision, const int *id, int off, int n,
                     cudaStream_t s);
-void launch_fill_int(int *dst, int val, int n, cudaStream_t s);
+void launch_fill_int(int *dst, int val, int n, cudaStream_t s, const int *gate = nullptr);
+// After a gated binning: clears the gate and counts the binning.
+void launch_rebin_close(int *gate, unsigned long long *bin_count, cudaStream_t s);
 void launch_iota_sim(int *id, int *sim, int sim_id, int n, cudaStream_t s);
 
 // ---- launch wrappers (sph_pairs.cu) ----

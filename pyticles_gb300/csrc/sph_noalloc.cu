@@ -112,10 +112,12 @@ extern "C" int sph_derivatives_noalloc(const sph_params *p, int32_t precision, i
     const int dim = p->dim;
     cudaStream_t st = (cudaStream_t)stream;
 
-    // host-side layout; coarser cells if the box needs more than the cell limit
+    // host-side layout (the engine's default cells of half the cutoff, so the
+    // summation order is the engine's); coarser cells if the box needs more
+    // than the cell limit
     SimDev sd;
     std::vector<int> morton, cxyz;
-    const double ratios[] = {dim == 2 ? 1.0 / 3.0 : 0.5, 0.5, 1.0, 2.0, 4.0};
+    const double ratios[] = {0.5, 1.0, 2.0, 4.0};
     int status = SPH_ECAPACITY;
     for (double ratio : ratios) {
         status = single_sim_tables(p, n, ratio, 0.0, &sd, &morton, &cxyz);

@@ -315,11 +315,18 @@ __device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S,
     bool skin = false;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-        xl[a] = (R)(x[a] - v.org[a][i]);
+        // relative to the cell the particle was binned in; with binning on
+        // demand the step may have started from a wrapped position
+        double d = x[a] - v.org[a][i];
+        if (d > S.half_L[a]) d -= S.L[a];
+        if (d < -S.half_L[a]) d += S.L[a];
+        xl[a] = (R)d;
         vv[a] = (R)vel[a];
         v.xe_out[a][i] = x[a];
         v.ve_out[a][i] = vel[a];
-        skin |= fabs(x[a] - v.b_pos[a][i]) > S.slack_half[a];
+        // the cell list finds every pair while each particle stays within its
+        // cell grown by the slack
+        skin |= fabs(d) > S.box_half[a];
     }
     if (skin) set_err(v.err, v.err_any, v.b_sim[i], SPH_ESKIN);
     v.ue_out[i] = u;
@@ -328,9 +335,16 @@ __device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S,
 }
 
 // Final state of the step into A (same slot as B), with the teleport wrap.
+// In rebin mode it is also the next step's start state in B and its packed
+// stage-0 copies, relative to the unchanged cells (the final stage writes
+// pk_*_out == buffer 0 for improved Euler and RK4); a particle past half of
+// its cell slack asks for a binning before the next step.
 template <typename R, int D>
 __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S, int i,
                                                   double *x, const double *vel, double u) {
+    using T4 = typename V4<R>::T;
+    R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
+    bool far = false;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
         double L = S.L[a];
@@ -338,11 +352,27 @@ __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S
         if (x[a] < 0) x[a] = L;
         v.a_pos[a][i] = x[a];
         v.a_vel[a][i] = vel[a];
+        if (v.reuse) {
+            double d = x[a] - v.org[a][i];
+            if (d > S.half_L[a]) d -= L;   // the wrap moved it across the box
+            if (d < -S.half_L[a]) d += L;
+            far |= fabs(d) > S.rebin_half[a];
+            xl[a] = (R)d;
+            vv[a] = (R)vel[a];
+            v.b_pos[a][i] = x[a];
+            v.b_vel[a][i] = vel[a];
+        }
     }
     v.a_u[i] = u;
     v.a_m[i] = v.b_m[i];
     v.a_id[i] = v.b_id[i];
     v.a_sim[i] = v.b_sim[i];
+    if (v.reuse) {
+        v.b_u[i] = u;
+        ((T4 *)v.pk_pos_out)[i] = make_v4<R>(xl[0], xl[1], xl[2], (R)v.b_m[i]);
+        ((T4 *)v.pk_vel_out)[i] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
+        if (far) *v.rebin_gate = 1;
+    }
 }
 
 // Integrator stage of particle i (c = xdot dt as in integrator.py:14-103)

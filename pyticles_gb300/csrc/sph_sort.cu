@@ -13,6 +13,7 @@ namespace sph {
 __global__ void k_bin(View v, int np_a) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= np_a) return;
+    if (v.rebin_gate && *v.rebin_gate == 0) return;
     int s = v.a_sim[k];
     int c = -1, rk = 0;
     if (s >= 0) {
@@ -73,7 +74,8 @@ __device__ __forceinline__ int block_excl_scan(int x, int *total) {
     return res;
 }
 
-__global__ void k_scan_reduce(const int *count, int n, int *block_tmp) {
+__global__ void k_scan_reduce(const int *count, int n, int *block_tmp, const int *gate) {
+    if (gate && *gate == 0) return;
     int base = blockIdx.x * kScanTile;
     int sum = 0;
     for (int t = 0; t < kScanPer; ++t) {
@@ -85,7 +87,8 @@ __global__ void k_scan_reduce(const int *count, int n, int *block_tmp) {
     if (threadIdx.x == 0) block_tmp[blockIdx.x] = total;
 }
 
-__global__ void k_scan_top(int *block_tmp, int nb) {
+__global__ void k_scan_top(int *block_tmp, int nb, const int *gate) {
+    if (gate && *gate == 0) return;
     // single block, sequential chunks of 1024
     int carry = 0;
     for (int base = 0; base < nb; base += kScanBlock) {
@@ -99,7 +102,9 @@ __global__ void k_scan_top(int *block_tmp, int nb) {
     if (threadIdx.x == 0) block_tmp[nb] = carry;
 }
 
-__global__ void k_scan_apply(const int *count, int *start, int n, const int *block_tmp, int nb) {
+__global__ void k_scan_apply(const int *count, int *start, int n, const int *block_tmp, int nb,
+                             const int *gate) {
+    if (gate && *gate == 0) return;
     int base = blockIdx.x * kScanTile;
     // each thread owns kScanPer consecutive elements
     int i0 = base + threadIdx.x * kScanPer;
@@ -120,17 +125,19 @@ __global__ void k_scan_apply(const int *count, int *start, int n, const int *blo
     if (blockIdx.x == 0 && threadIdx.x == 0) start[n] = block_tmp[nb];
 }
 
-void launch_scan(int *count, int *start, int n, int *block_tmp, cudaStream_t s) {
+void launch_scan(int *count, int *start, int n, int *block_tmp, cudaStream_t s,
+                 const int *gate) {
     int nb = (n + kScanTile - 1) / kScanTile;
     if (nb < 1) nb = 1;
-    k_scan_reduce<<<nb, kScanBlock, 0, s>>>(count, n, block_tmp);
-    k_scan_top<<<1, kScanBlock, 0, s>>>(block_tmp, nb);
-    k_scan_apply<<<nb, kScanBlock, 0, s>>>(count, start, n, block_tmp, nb);
+    k_scan_reduce<<<nb, kScanBlock, 0, s>>>(count, n, block_tmp, gate);
+    k_scan_top<<<1, kScanBlock, 0, s>>>(block_tmp, nb, gate);
+    k_scan_apply<<<nb, kScanBlock, 0, s>>>(count, start, n, block_tmp, nb, gate);
 }
 
 __global__ void k_scatter(View v, int np_a) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= np_a) return;
+    if (v.rebin_gate && *v.rebin_gate == 0) return;
     int c = v.cell_of[k];
     if (c >= 0) v.order_tmp[v.cell_start[c] + v.rank[k]] = k;
 }
@@ -150,6 +157,7 @@ __global__ void k_cellsort(View v, int ncells) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (warp >= ncells) return;
+    if (v.rebin_gate && *v.rebin_gate == 0) return;
     int b = v.cell_start[warp], e = v.cell_start[warp + 1];
     int m = e - b;
     for (int x = lane; x < m; x += 32) {
@@ -174,6 +182,8 @@ template <typename R>
 __global__ void k_permute(View v) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= v.np) return;
+    if (v.rebin_gate && *v.rebin_gate == 0) return;
+    if (j == 0 && !v.rebin_gate && v.bin_count) ++*v.bin_count;
     int k = v.order[j];
     int s = v.a_sim[k];
     const SimDev &S = v.sims[s];
@@ -264,14 +274,26 @@ void launch_store_R(double *dst, const void *src, int precision, const int *id, 
     else k_store_R<double><<<nb, 256, 0, s>>>(dst, (const double *)src, id, off, n);
 }
 
-__global__ void k_fill_int(int *dst, int val, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = val;
+__global__ void k_fill_int(int *dst, int val, int n, const int *gate) {
+    if (gate && *gate == 0) return;
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = val;
 }
 
-void launch_fill_int(int *dst, int val, int n, cudaStream_t s) {
+void launch_fill_int(int *dst, int val, int n, cudaStream_t s, const int *gate) {
     if (n <= 0) return;
-    k_fill_int<<<(n + 255) / 256, 256, 0, s>>>(dst, val, n);
+    k_fill_int<<<(n + 255) / 256, 256, 0, s>>>(dst, val, n, gate);
+}
+
+__global__ void k_rebin_close(int *gate, unsigned long long *bin_count) {
+    if (*gate) {
+        *gate = 0;
+        ++*bin_count;
+    }
+}
+
+void launch_rebin_close(int *gate, unsigned long long *bin_count, cudaStream_t s) {
+    k_rebin_close<<<1, 1, 0, s>>>(gate, bin_count);
 }
 
 __global__ void k_iota_sim(int *id, int *sim, int sim_id, int n) {

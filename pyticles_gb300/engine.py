@@ -198,15 +198,25 @@ class Engine:
         t = SphTuning()
         check(self._lib.sph_get_tuning(self._h, ctypes.byref(t)), "sph_get_tuning")
         return {"block_size": t.block_size, "use_graph": t.use_graph,
-                "steps_per_graph": t.steps_per_graph, "cell_ratio": t.cell_ratio}
+                "steps_per_graph": t.steps_per_graph, "rebin": t.rebin,
+                "cell_ratio": t.cell_ratio}
 
     def set_tuning(self, **kw):
+        """block_size, use_graph, steps_per_graph, cell_ratio, and rebin (1:
+        bin into cells only when a particle has used half of the cell slack,
+        VerletList.ponder_rebuild's skin reuse; 0: every step)."""
         cur = self.tuning
         cur.update(kw)
         t = SphTuning(block_size=int(cur["block_size"]), use_graph=int(cur["use_graph"]),
-                      steps_per_graph=int(cur["steps_per_graph"]), reserved=0,
+                      steps_per_graph=int(cur["steps_per_graph"]), rebin=int(cur["rebin"]),
                       cell_ratio=float(cur["cell_ratio"]))
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), "sph_set_tuning")
+
+    def rebin_count(self):
+        """Binnings (cell-list builds) performed so far."""
+        n = ctypes.c_int64()
+        check(self._lib.sph_rebin_count(self._h, ctypes.byref(n)), "sph_rebin_count")
+        return n.value
 
     # -- launch-ready graphs and per-pass timing --
     def prepare(self):

@@ -284,7 +284,7 @@ def test_skin_violation_is_flagged():
     with Engine(prm, "mixed", max_particles=len(r)) as e:
         s = e.add(prm, r, v, m, u)
         v2 = v.copy()
-        v2[3] = [900.0, 0.0]   # 0.9 per step against a slack of 0.2
+        v2[3] = [5000.0, 0.0]  # 5 per step: out of its cell grown by the slack
         e.set_state(s, r, v2, m, u)
         e.advance(1)
         with pytest.raises(SphError) as ei:
