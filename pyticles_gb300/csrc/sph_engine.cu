@@ -118,6 +118,8 @@ struct sph_engine {
     int *rebin_gate = nullptr;     // tuning.rebin: bin before the next step
     unsigned long long *bin_count = nullptr;
     bool bins_valid = false;       // B, its packed copies and the cells match A
+    bool one_sim = false;          // exactly one live simulation (one_dev)
+    SimDev one_dev;
 
     // profiling: event pairs recorded around each pass
     bool prof_on = false;
@@ -444,6 +446,8 @@ View make_view(const sph_engine *e) {
     v.err = e->err;
     v.err_any = e->err_any;
     v.bin_count = e->bin_count;
+    v.one_sim = e->one_sim ? 1 : 0;
+    if (e->one_sim) v.one = e->one_dev;
     return v;
 }
 
@@ -535,6 +539,12 @@ int relayout(sph_engine *e) {
         else memset(&sd[s], 0, sizeof(SimDev));
     }
     CK(cudaMemcpyAsync(e->sims_d, sd.data(), sizeof(SimDev) * e->cap_s, cudaMemcpyHostToDevice, st));
+    // a single live simulation: its constants travel as kernel parameters
+    int live = 0, last = -1;
+    for (int s = 0; s < (int)e->sims.size(); ++s)
+        if (e->sims[s].active) ++live, last = s;
+    e->one_sim = live == 1;
+    if (e->one_sim) e->one_dev = sd[last];
     CK(cudaStreamSynchronize(st));
     free_graph(e);
     e->layout_dirty = false;

@@ -120,6 +120,11 @@ struct View {
     int *rebin_gate;
     int reuse;
     unsigned long long *bin_count;
+    // one_sim: every particle belongs to simulation `one` (a copy of
+    // sims[that id]); the pair kernels then read its constants from the
+    // kernel parameters instead of holding them in registers
+    int one_sim;
+    SimDev one;
 };
 
 // Strided view of an n x 3 (SoA, stride 1) or n x dim (row-major, stride

@@ -193,6 +193,8 @@ extern "C" int sph_derivatives_noalloc(const sph_params *p, int32_t precision, i
 
     // inputs and tables; what must start at zero is cleared here
     NA_CK(cudaMemcpyAsync(w.sims, &sd, sizeof(SimDev), cudaMemcpyHostToDevice, st));
+    w.one_sim = 1;
+    w.one = sd;
     NA_CK(cudaMemcpyAsync(w.morton, morton.data(), sizeof(int) * ncells, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(w.cell_xyz, cxyz.data(), sizeof(int) * ncells, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));

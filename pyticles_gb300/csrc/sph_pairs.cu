@@ -1,198 +1,26 @@
-// sph_pairs.cu -- the pair passes of one derivative evaluation and the
-// fused integrator epilogue.
+// sph_pairs.cu -- density and heat-flux passes of one derivative evaluation,
+// the thermostat reductions and the pair-set export.
 //
 //   k_density : rho_s, rho_l summation (self term W(0,h), no m_i:
 //               properties.py:77-91), fused EOS epilogue (T from u, clamp,
 //               p, pco: properties.py:38-49, spam_complete_force.py:134-152)
 //   k_heat    : Fourier heat flux q_i (f_properties.py:129-130 restated)
-//   k_force   : pressure + cohesive accelerations, Monaghan viscosity, energy
-//               rate incl. conduction (forces.py:338-405, c_forces.pyx:96-111,
-//               163-178, 224-237) fused with the integrator stage update
-//               (integrator.py:14-103), periodic teleport (box.py:33-47) and the
-//               thermostat (particles.py:450-457).
-//
-// Every pass is a gather: thread i sums over all neighbours j in the 3^dim
-// cells around its own cell, so each unordered pair is evaluated from both
-// sides and no atomics touch particle data.  Positions are cell-local
-// (relative to the particle's cell centre), which keeps FP32 differences
-// accurate; the pair-set test runs on those FP32 distances with a 2^-12
-// guard band and falls back to the reference's FP64 test for pairs inside
-// the band, so the pair set is bit-exact.
-#include <type_traits>
-
-#include "sph_device.cuh"
+#include "sph_pairs.cuh"
 
 namespace sph {
 
-__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-
-// 1/x for the EOS: FP64 division in FP64 mode; in mixed mode an FP32
-// reciprocal refined by one FP64 Newton step (relative error ~1e-14), which
-// spares the narrow FP64 pipe a full division per particle.
-template <typename R> __device__ __forceinline__ double recip64(double x);
-template <> __device__ __forceinline__ double recip64<double>(double x) { return 1.0 / x; }
-template <> __device__ __forceinline__ double recip64<float>(double x) {
-    double r = (double)__frcp_rn((float)x);
-    return r * fma(-x, r, 2.0);
-}
-__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
-
-template <typename R, int D>
-struct PairFrame {
-    R thr_lo, thr_hi, thr_s;
-    R edge[3], L[3], hL[3];
-    R ext[3];       // half extent of a cell including the allowed drift
-    int small_mask;
-    __device__ __forceinline__ void init(const SimDev &S) {
-        const SimConst<R> &c = sconst<R>(S);
-        thr_lo = c.thr_lo;
-        thr_hi = c.thr_hi;
-        thr_s = c.thr_s;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            edge[a] = c.edge[a];
-            L[a] = c.L[a];
-            hL[a] = c.hL[a];
-            ext[a] = c.ext[a];
-        }
-        small_mask = S.small_mask;
-    }
-    __device__ __forceinline__ void min_image(R *d) const {
-        if (small_mask) {
-#pragma unroll
-            for (int a = 0; a < D; ++a)
-                if (small_mask & (1 << a)) {
-                    if (d[a] > hL[a]) d[a] -= L[a];
-                    if (d[a] < -hL[a]) d[a] += L[a];
-                }
-        }
-    }
-};
-
-template <int D> struct NbrCount { static constexpr int value = D == 2 ? 9 : 27; };
-
-// max(|c| - ext, 0): distance along one axis from particle i to a cell whose
-// centre sits at c relative to i
-template <typename R> __device__ __forceinline__ R fmaxf_(R c, R ext) {
-    R a = (c < (R)0 ? -c : c) - ext;
-    return a > (R)0 ? a : (R)0;
-}
-
-// Iterates the pair set of particle i.  body(j, pj, d[3], rsq, near) is called
-// for every j != i that passes the exact pair test, in a fixed order: neighbour
-// cells in raster order (z, y, x) of their offset from i's cell, particles in
-// cell order.  The order depends only on i's cell, never on which particles
-// share a warp or a launch, so every particle sums its pairs identically
-// whether its simulation runs alone or in a batch.
-//
-// Cells are (cutoff + skin)/W wide and the window spans +-W cells per axis;
-// a cell whose box (grown by the allowed drift) lies beyond the cutoff from
-// particle i is skipped before any of its particles is loaded.
-//
-// near is std::true_type unless the cell lies beyond the short kernel's
-// support from every lane of the warp that visits it (a warp-uniform choice,
-// so the two loop bodies never diverge); with std::false_type the body may
-// drop every short-kernel term, which is exactly zero there.
-//
-// PF: load the next candidate's position before testing the current one
-// (measured: 4-7% faster for the 3D heat and force passes, slower for the
-// 2D passes and for density, where more warps already hide the latency).
-template <typename R, int D, bool PF = false, typename T4, typename F, typename G>
-__device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
-                                          const PairFrame<R, D> &fr, const T4 *__restrict__ P,
-                                          int i, const T4 &pi, F body, G cell_done) {
-    const int cp = v.cell_xyz[v.cell_b[i]];
-    const int c0 = cp & 2047, c1 = (cp >> 11) & 2047, c2 = (cp >> 22) & 1023;
-    const int w0 = S.win[0], w1 = S.win[1], w2 = D == 3 ? S.win[2] : 0;
-    const int n0 = S.nc[0], n1 = S.nc[1], n2 = S.nc[2];
-    const int *mort = v.morton + S.cell_off;
-    for (int oz = -w2; oz <= w2; ++oz) {
-        R dz = (R)0;
-        int z = 0;
-        if (D == 3) {
-            dz = fmaxf_((R)oz * fr.edge[2] - pi.z, fr.ext[2]);
-            z = c2 + oz;
-            z += (z < 0) ? n2 : 0;
-            z -= (z >= n2) ? n2 : 0;
-        }
-        for (int oy = -w1; oy <= w1; ++oy) {
-            R dy = fmaxf_((R)oy * fr.edge[1] - pi.y, fr.ext[1]);
-            R dyz = dy * dy + dz * dz;
-            if (dyz > fr.thr_hi) continue;
-            int y = c1 + oy;
-            y += (y < 0) ? n1 : 0;
-            y -= (y >= n1) ? n1 : 0;
-            const int row = (z * n1 + y) * n0;
-            for (int ox = -w0; ox <= w0; ++ox) {
-                R dx = fmaxf_((R)ox * fr.edge[0] - pi.x, fr.ext[0]);
-                if (dx * dx + dyz > fr.thr_hi) continue;
-                int x = c0 + ox;
-                x += (x < 0) ? n0 : 0;
-                x -= (x >= n0) ? n0 : 0;
-                const int gc = S.cell_off + mort[row + x];
-                const R ox_ = (R)ox * fr.edge[0] - pi.x;
-                const R oy_ = (R)oy * fr.edge[1] - pi.y;
-                const R oz_ = (D == 3) ? (R)oz * fr.edge[2] - pi.z : (R)0;
-                const int jb = v.cell_start[gc], je = v.cell_start[gc + 1];
-                auto scan = [&](auto near) {
-                    T4 pn;
-                    if (PF) pn = P[jb < je ? jb : i];
-                    for (int j = jb; j < je; ++j) {
-                        T4 pj;
-                        if (PF) {
-                            pj = pn;
-                            if (j + 1 < je) pn = P[j + 1];
-                        }
-                        if (j == i) continue;
-                        if (!PF) pj = P[j];
-                        R d[3];
-                        d[0] = pj.x + ox_;
-                        d[1] = pj.y + oy_;
-                        d[2] = (D == 3) ? pj.z + oz_ : (R)0;
-                        fr.min_image(d);
-                        R rsq = d[0] * d[0] + d[1] * d[1];
-                        if (D == 3) rsq += d[2] * d[2];
-                        if (rsq > fr.thr_hi) continue;
-                        if (rsq >= fr.thr_lo && !exact_in_set<D>(v.xe_in, &S, i, j)) continue;
-                        body(j, pj, d, rsq, near);
-                    }
-                };
-                if (__any_sync(__activemask(), dx * dx + dyz < fr.thr_s))
-                    scan(std::true_type{});
-                else
-                    scan(std::false_type{});
-                cell_done();
-            }
-        }
-    }
-}
-
-// Warp-aggregated per-simulation counter update.
-__device__ __forceinline__ void add_pair_count(unsigned long long *cnt, int s, unsigned c) {
-    unsigned act = __activemask();
-    unsigned grp = __match_any_sync(act, s);
-    unsigned long long tot = 0;
-    // sum over the group (lanes with the same simulation)
-    for (int l = 0; l < 32; ++l) {
-        if (!(act & (1u << l))) continue;
-        unsigned x = __shfl_sync(act, c, l);
-        if (grp & (1u << l)) tot += x;
-    }
-    int leader = __ffs(grp) - 1;
-    if ((threadIdx.x & 31) == leader) atomicAdd(&cnt[s], tot);
-}
-
 // At most 64 registers (4 blocks of 256 per SM): the two loop bodies of
-// for_pairs would otherwise take 80 and cost 5-20% in occupancy.
-template <typename R, int D, int K>
-__global__ void __launch_bounds__(256, 4) k_density(View v, int stage) {
+// for_pairs would otherwise take 80 and cost 5-20% in occupancy; 51 for a
+// single simulation (its constants are kernel parameters), 3% faster again.
+template <typename R, int D, int K, bool ONE>
+__global__ void __launch_bounds__(256, ONE ? 5 : 4) k_density(const __grid_constant__ View v, int stage) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
     using T4 = typename V4<R>::T;
     const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
     const int s = v.b_sim[ii];
-    const SimDev &S = v.sims[s];
+    const SimDev &S = ONE ? v.one : v.sims[s];
     KConst<R> ks = make_kconst<R>(S, 0);
     KConst<R> kl = make_kconst<R>(S, 1);
     BAcc<R> rs, rl;
@@ -257,8 +85,8 @@ __global__ void __launch_bounds__(256, 4) k_density(View v, int stage) {
 }
 
 // At most 64 registers (4 blocks of 256 per SM): 8% faster in 3D than 80.
-template <typename R, int D, int K>
-__global__ void __launch_bounds__(256, 4) k_heat(View v) {
+template <typename R, int D, int K, bool ONE>
+__global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
@@ -266,7 +94,7 @@ __global__ void __launch_bounds__(256, 4) k_heat(View v) {
     const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
     const T4 *__restrict__ F = (const T4 *)v.pk_f;
     const int s = v.b_sim[ii];
-    const SimDev &S = v.sims[s];
+    const SimDev &S = ONE ? v.one : v.sims[s];
     KConst<R> ks = make_kconst<R>(S, 0);
     const T4 fi = F[ii];
     BAcc<R> q[3];
@@ -304,337 +132,25 @@ __global__ void __launch_bounds__(256, 4) k_heat(View v) {
     ((T4 *)v.pk_q)[i] = make_v4<R>(qq[0] * ir2, qq[1] * ir2, qq[2] * ir2, (R)0);
 }
 
-// Next evaluation state: positions/velocities/energy in FP64 plus packed
-// cell-local copies relative to the particle's cell (binned at x0).
-template <typename R, int D>
-__device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S, int i,
-                                                 const double *x, const double *vel, double u,
-                                                 double m) {
-    using T4 = typename V4<R>::T;
-    R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
-    bool skin = false;
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-        // relative to the cell the particle was binned in; with binning on
-        // demand the step may have started from a wrapped position
-        double d = x[a] - v.org[a][i];
-        if (d > S.half_L[a]) d -= S.L[a];
-        if (d < -S.half_L[a]) d += S.L[a];
-        xl[a] = (R)d;
-        vv[a] = (R)vel[a];
-        v.xe_out[a][i] = x[a];
-        v.ve_out[a][i] = vel[a];
-        // the cell list finds every pair while each particle stays within its
-        // cell grown by the slack
-        skin |= fabs(d) > S.box_half[a];
-    }
-    if (skin) set_err(v.err, v.err_any, v.b_sim[i], SPH_ESKIN);
-    v.ue_out[i] = u;
-    ((T4 *)v.pk_pos_out)[i] = make_v4<R>(xl[0], xl[1], xl[2], (R)m);
-    ((T4 *)v.pk_vel_out)[i] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
-}
-
-// Final state of the step into A (same slot as B), with the teleport wrap.
-// In rebin mode it is also the next step's start state in B and its packed
-// stage-0 copies, relative to the unchanged cells (the final stage writes
-// pk_*_out == buffer 0 for improved Euler and RK4); a particle past half of
-// its cell slack asks for a binning before the next step.
-template <typename R, int D>
-__device__ __forceinline__ void write_final_state(const View &v, const SimDev &S, int i,
-                                                  double *x, const double *vel, double u) {
-    using T4 = typename V4<R>::T;
-    R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
-    bool far = false;
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-        double L = S.L[a];
-        if (x[a] > L) x[a] = 0;
-        if (x[a] < 0) x[a] = L;
-        v.a_pos[a][i] = x[a];
-        v.a_vel[a][i] = vel[a];
-        if (v.reuse) {
-            double d = x[a] - v.org[a][i];
-            if (d > S.half_L[a]) d -= L;   // the wrap moved it across the box
-            if (d < -S.half_L[a]) d += L;
-            far |= fabs(d) > S.rebin_half[a];
-            xl[a] = (R)d;
-            vv[a] = (R)vel[a];
-            v.b_pos[a][i] = x[a];
-            v.b_vel[a][i] = vel[a];
-        }
-    }
-    v.a_u[i] = u;
-    v.a_m[i] = v.b_m[i];
-    v.a_id[i] = v.b_id[i];
-    v.a_sim[i] = v.b_sim[i];
-    if (v.reuse) {
-        v.b_u[i] = u;
-        ((T4 *)v.pk_pos_out)[i] = make_v4<R>(xl[0], xl[1], xl[2], (R)v.b_m[i]);
-        ((T4 *)v.pk_vel_out)[i] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
-        if (far) *v.rebin_gate = 1;
-    }
-}
-
-// Integrator stage of particle i (c = xdot dt as in integrator.py:14-103)
-// from its rates vdr, udr, followed on the last stage by the teleport wrap
-// and the thermostat.
-template <typename R, int D>
-__device__ __forceinline__ void integrate_stage(const View &v, const SimDev &S, int i, int s,
-                                                int stage, int integ, const R *vdr, R udr) {
-    const double dt = S.dt;
-    double x0[3] = {0, 0, 0}, v0[3] = {0, 0, 0}, rd[3] = {0, 0, 0}, vd[3] = {0, 0, 0};
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-        x0[a] = v.b_pos[a][i];
-        v0[a] = v.b_vel[a][i];
-        rd[a] = v.ve_in[a][i];
-        vd[a] = (double)vdr[a];
-    }
-    double u0 = v.b_u[i], udd = (double)udr, m = v.b_m[i];
-    double x[3] = {0, 0, 0}, vel[3] = {0, 0, 0}, u;
-    bool final_stage = false;
-    // Euler and improved Euler in FMA form: x0 + dt f and x0 + dt/2 (f0 + f1)
-    // (integrator.py:14-59 round c = f dt and (c1 + c2)/2 separately; the
-    // difference is one rounding per step, far below the FP64 tolerance)
-    if (integ == SPH_EULER) {
-        for (int a = 0; a < D; ++a) {
-            x[a] = fma(dt, rd[a], x0[a]);
-            vel[a] = fma(dt, vd[a], v0[a]);
-        }
-        u = fma(dt, udd, u0);
-        final_stage = true;
-    } else if (integ == SPH_IEULER) {
-        if (stage == 0) {
-            for (int a = 0; a < D; ++a) {
-                ((R *)v.f0v[a])[i] = vdr[a];
-                x[a] = fma(dt, rd[a], x0[a]);
-                vel[a] = fma(dt, vd[a], v0[a]);
-            }
-            ((R *)v.f0u)[i] = udr;
-            u = fma(dt, udd, u0);
-            write_eval_state<R, D>(v, S, i, x, vel, u, m);
-        } else {
-            const double hdt = S.hdt;
-            for (int a = 0; a < D; ++a) {
-                x[a] = fma(hdt, v0[a] + rd[a], x0[a]);
-                vel[a] = fma(hdt, (double)((const R *)v.f0v[a])[i] + vd[a], v0[a]);
-            }
-            u = fma(hdt, (double)((const R *)v.f0u)[i] + udd, u0);
-            final_stage = true;
-        }
-    } else {  // RK4
-        double cr[3], cv[3], cu = dmul(udd, dt);
-        for (int a = 0; a < D; ++a) {
-            cr[a] = dmul(rd[a], dt);
-            cv[a] = dmul(vd[a], dt);
-        }
-        if (stage == 0) {
-            for (int a = 0; a < D; ++a) {
-                v.acc_r[a][i] = cr[a];
-                v.acc_v[a][i] = cv[a];
-                x[a] = dadd(x0[a], cr[a] / 2.0);
-                vel[a] = dadd(v0[a], cv[a] / 2.0);
-            }
-            v.acc_u[i] = cu;
-            u = dadd(u0, cu / 2.0);
-            write_eval_state<R, D>(v, S, i, x, vel, u, m);
-        } else if (stage < 3) {
-            for (int a = 0; a < D; ++a) {
-                v.acc_r[a][i] = dadd(v.acc_r[a][i], dmul(2.0, cr[a]));
-                v.acc_v[a][i] = dadd(v.acc_v[a][i], dmul(2.0, cv[a]));
-                x[a] = stage == 1 ? dadd(x0[a], cr[a] / 2.0) : dadd(x0[a], cr[a]);
-                vel[a] = stage == 1 ? dadd(v0[a], cv[a] / 2.0) : dadd(v0[a], cv[a]);
-            }
-            v.acc_u[i] = dadd(v.acc_u[i], dmul(2.0, cu));
-            u = stage == 1 ? dadd(u0, cu / 2.0) : dadd(u0, cu);
-            write_eval_state<R, D>(v, S, i, x, vel, u, m);
-        } else {
-            for (int a = 0; a < D; ++a) {
-                x[a] = dadd(x0[a], dmul(1.0 / 6.0, dadd(v.acc_r[a][i], cr[a])));
-                vel[a] = dadd(v0[a], dmul(1.0 / 6.0, dadd(v.acc_v[a][i], cv[a])));
-            }
-            u = dadd(u0, dmul(1.0 / 6.0, dadd(v.acc_u[i], cu)));
-            final_stage = true;
-        }
-    }
-    if (final_stage) {
-        if (S.thermostat) {
-            // particles.py:450-457: T <- T * target / mean(T); u <- k_B T - a rho
-            R *tp = (R *)v.temp;
-            double T = (double)tp[i] * v.t_scale[s];
-            u = dadd(dmul(T, S.kb), -dmul(S.a, (double)((const R *)v.rho0)[i]));
-            tp[i] = (R)T;
-        }
-        write_final_state<R, D>(v, S, i, x, vel, u);
-    }
-}
-
-// VH: bit 0 viscosity, bit 1 heat flux (compile-time, so a workload without
-// them carries neither their registers nor their branches)
-// At most 64 registers (4 blocks of 256 per SM): measured 17% faster than the
-// unconstrained 80-104 despite a few spilled words outside the pair loop.
-template <typename R, int D, int K, int VH>
-__global__ void __launch_bounds__(256, 4) k_force(View v, int stage, int mode, int integ) {
-    constexpr bool visc = (VH & 1) != 0;
-    constexpr bool heat = (VH & 2) != 0;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < v.np;
-    const int ii = active ? i : v.np - 1;
-    using T4 = typename V4<R>::T;
-    const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
-    const T4 *__restrict__ FV = (const T4 *)v.pk_fv;
-    const R *__restrict__ RHO = (const R *)v.rho;
-    const T4 *__restrict__ Q = (const T4 *)v.pk_q;
-    const int s = v.b_sim[ii];
-    const SimDev &S = v.sims[s];
-    KConst<R> ks = make_kconst<R>(S, 0);
-    KConst<R> kl = make_kconst<R>(S, 1);
-    const SimConst<R> &sc = sconst<R>(S);
-    const R hs = sc.hs, eps_h2 = sc.eps_h2;
-    const R alpha_c = sc.alpha_c, beta = sc.beta;
-    const R pl2 = sc.pl2;  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
-    // own velocity, p/rho^2 and rho
-    const T4 fvi = FV[ii];
-    const R vix = fvi.x, viy = fvi.y, viz = D == 3 ? fvi.z : (R)0;
-    const R fsi = D == 2 ? fvi.z : fvi.w;
-    const R rhoi = D == 2 ? fvi.w : RHO[ii];
-    const T4 qi = heat ? Q[ii] : make_v4<R>(0, 0, 0, 0);
-    BAcc<R> ax[3], ud;
-    ax[0].init(0);
-    ax[1].init(0);
-    ax[2].init(0);
-    ud.init(0);
-    auto body = [&](int j, const T4 &pj, const R *d, R rsq, auto near) {
-        constexpr bool NEAR = decltype(near)::value;
-        R r = fsqrt<R>(rsq);
-        R gl = kernel_g<K, R>(kl, r);
-        const T4 fvj = FV[j];
-        R dvdx = (fvj.x - vix) * d[0] + (fvj.y - viy) * d[1];
-        if (D == 3) dvdx += (fvj.z - viz) * d[2];
-        // beyond the short support gs = 0: the pressure and viscosity terms
-        // vanish and gsum = pl2 gl bit for bit
-        R gsum = pl2 * gl, gs = (R)0;
-        if constexpr (NEAR) {
-            gs = kernel_g<K, R>(ks, r);
-            R ps = fsi + (D == 2 ? fvj.z : fvj.w);
-            if (visc && dvdx < (R)0) {
-                // Monaghan viscosity on approaching pairs
-                const R rhoj = D == 2 ? fvj.w : RHO[j];
-                R mu = fdiv<R>(hs * dvdx, rsq + eps_h2);
-                ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), rhoi + rhoj);
-            }
-            gsum = ps * gs + pl2 * gl;
-        }
-        ax[0].add(gsum * d[0]);
-        ax[1].add(gsum * d[1]);
-        if (D == 3) ax[2].add(gsum * d[2]);
-        R du = (R)0.5 * gsum * dvdx * pj.w;
-        if (heat && NEAR) {
-            T4 qj = Q[j];
-            R dq = (qi.x + qj.x) * d[0] + (qi.y + qj.y) * d[1];
-            if (D == 3) dq += (qi.z + qj.z) * d[2];
-            du -= dq * gs * pj.w;
-        }
-        ud.add(du);
-    };
-    auto cell_done = [&]() {
-        ax[0].flush();
-        ax[1].flush();
-        if (D == 3) ax[2].flush();
-        ud.flush();
-    };
-    if (!active) return;
-    {
-        PairFrame<R, D> fr;
-        fr.init(S);
-        for_pairs<R, D, D == 3>(v, S, fr, P, i, P[i], body, cell_done);
-    }
-    R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
-    R udr = ud.get();
-    for (int a = 0; a < D; ++a) ((R *)v.vdot[a])[i] = vdr[a];
-    ((R *)v.udot)[i] = udr;
-    if (!isfinite(vdr[0]) || !isfinite(udr)) set_err(v.err, v.err_any, s, SPH_ENAN);
-    if (mode == 0) return;
-
-    integrate_stage<R, D>(v, S, i, s, stage, integ, vdr, udr);
-}
-
-// Integrator stage from the stored rates: the epilogue of k_force as a pass
-// of its own, for steps whose velocities change between the force pass and
-// the update (hard collisions).
-template <typename R, int D>
-__global__ void __launch_bounds__(256) k_integrate(View v, int stage, int integ) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.np) return;
-    const int s = v.b_sim[i];
-    const SimDev &S = v.sims[s];
-    if (!S.active) return;
-    R vdr[3] = {0, 0, 0};
-    for (int a = 0; a < D; ++a) vdr[a] = ((const R *)v.vdot[a])[i];
-    integrate_stage<R, D>(v, S, i, s, stage, integ, vdr, ((const R *)v.udot)[i]);
-}
-
-// ---- dispatch ----
-#define SPH_DISPATCH(PREC, DIM, KERN, CALL)                                       \
-    do {                                                                          \
-        if (PREC == SPH_MIXED) {                                                  \
-            using R = float;                                                      \
-            if (DIM == 2) { constexpr int D = 2; SPH_DISPATCH_K(KERN, CALL); }    \
-            else { constexpr int D = 3; SPH_DISPATCH_K(KERN, CALL); }             \
-        } else {                                                                  \
-            using R = double;                                                     \
-            if (DIM == 2) { constexpr int D = 2; SPH_DISPATCH_K(KERN, CALL); }    \
-            else { constexpr int D = 3; SPH_DISPATCH_K(KERN, CALL); }             \
-        }                                                                         \
-    } while (0)
-#define SPH_DISPATCH_K(KERN, CALL)                                                \
-    switch (KERN) {                                                               \
-        case SPH_KERNEL_GAUSSIAN: { constexpr int K = SPH_KERNEL_GAUSSIAN; CALL; break; } \
-        case SPH_KERNEL_LUCY: { constexpr int K = SPH_KERNEL_LUCY; CALL; break; }         \
-        case SPH_KERNEL_DEBRUN: { constexpr int K = SPH_KERNEL_DEBRUN; CALL; break; }     \
-        default: { constexpr int K = SPH_KERNEL_CUBIC; CALL; break; }                     \
-    }
-
 void launch_density(const View &v, int precision, int kernel, int stage, int block,
                     cudaStream_t s) {
     if (v.np <= 0) return;
     int nb = (v.np + block - 1) / block;
-    SPH_DISPATCH(precision, v.dim, kernel, (k_density<R, D, K><<<nb, block, 0, s>>>(v, stage)));
+    if (v.one_sim)
+        SPH_DISPATCH(precision, v.dim, kernel,
+                     (k_density<R, D, K, true><<<nb, block, 0, s>>>(v, stage)));
+    else
+        SPH_DISPATCH(precision, v.dim, kernel,
+                     (k_density<R, D, K, false><<<nb, block, 0, s>>>(v, stage)));
 }
 
 void launch_heat(const View &v, int precision, int kernel, int block, cudaStream_t s) {
     if (v.np <= 0) return;
     int nb = (v.np + block - 1) / block;
-    SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K><<<nb, block, 0, s>>>(v)));
-}
-
-void launch_force(const View &v, int precision, int kernel, int viscosity, int heat,
-                  int integrator, int stage, int mode, int block, cudaStream_t s) {
-    if (v.np <= 0) return;
-    int nb = (v.np + block - 1) / block;
-    const int vh = (viscosity ? 1 : 0) | (heat ? 2 : 0);
-#define SPH_FORCE(VH_) k_force<R, D, K, VH_><<<nb, block, 0, s>>>(v, stage, mode, integrator)
-    SPH_DISPATCH(precision, v.dim, kernel, ({
-                     switch (vh) {
-                         case 0: SPH_FORCE(0); break;
-                         case 1: SPH_FORCE(1); break;
-                         case 2: SPH_FORCE(2); break;
-                         default: SPH_FORCE(3); break;
-                     }
-                 }));
-#undef SPH_FORCE
-}
-
-void launch_integrate(const View &v, int precision, int integrator, int stage, cudaStream_t s) {
-    if (v.np <= 0) return;
-    int nb = (v.np + 255) / 256;
-    if (precision == SPH_MIXED) {
-        if (v.dim == 2) k_integrate<float, 2><<<nb, 256, 0, s>>>(v, stage, integrator);
-        else k_integrate<float, 3><<<nb, 256, 0, s>>>(v, stage, integrator);
-    } else {
-        if (v.dim == 2) k_integrate<double, 2><<<nb, 256, 0, s>>>(v, stage, integrator);
-        else k_integrate<double, 3><<<nb, 256, 0, s>>>(v, stage, integrator);
-    }
+    if (v.one_sim)
+        SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K, true><<<nb, block, 0, s>>>(v)));
+    else
+        SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K, false><<<nb, block, 0, s>>>(v)));
 }
 
 // ---- thermostat: per-chunk FP64 partial sums of T, then one thread per
