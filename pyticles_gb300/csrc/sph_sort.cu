@@ -10,10 +10,16 @@
 
 namespace sph {
 
-__global__ void k_bin(View v, int np_a) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= np_a) return;
-    if (v.rebin_gate && *v.rebin_gate == 0) return;
+// Grids of the binning kernels are capped (grid-stride loops), so that the
+// gated launches of a step that keeps its cells cost little.
+constexpr int kSortMaxBlocks = 152 * 16;
+
+inline int sort_blocks(long long work, int per_block) {
+    long long nb = (work + per_block - 1) / per_block;
+    return (int)(nb < 1 ? 1 : (nb > kSortMaxBlocks ? kSortMaxBlocks : nb));
+}
+
+__device__ __forceinline__ void bin_one(const View &v, int k) {
     int s = v.a_sim[k];
     int c = -1, rk = 0;
     if (s >= 0) {
@@ -34,9 +40,16 @@ __global__ void k_bin(View v, int np_a) {
     v.rank[k] = rk;
 }
 
+
+__global__ void k_bin(View v, int np_a) {
+    if (v.rebin_gate && *v.rebin_gate == 0) return;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np_a; k += gridDim.x * blockDim.x)
+        bin_one(v, k);
+}
+
 void launch_bin(const View &v, int np_a, cudaStream_t s) {
     if (np_a <= 0) return;
-    k_bin<<<(np_a + 255) / 256, 256, 0, s>>>(v, np_a);
+    k_bin<<<sort_blocks(np_a, 256), 256, 0, s>>>(v, np_a);
 }
 
 // ---- exclusive scan of int counts: start[i] = sum count[<i], start[n] = total ----
@@ -135,16 +148,16 @@ void launch_scan(int *count, int *start, int n, int *block_tmp, cudaStream_t s,
 }
 
 __global__ void k_scatter(View v, int np_a) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= np_a) return;
     if (v.rebin_gate && *v.rebin_gate == 0) return;
-    int c = v.cell_of[k];
-    if (c >= 0) v.order_tmp[v.cell_start[c] + v.rank[k]] = k;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np_a; k += gridDim.x * blockDim.x) {
+        int c = v.cell_of[k];
+        if (c >= 0) v.order_tmp[v.cell_start[c] + v.rank[k]] = k;
+    }
 }
 
 void launch_scatter(const View &v, int np_a, cudaStream_t s) {
     if (np_a <= 0) return;
-    k_scatter<<<(np_a + 255) / 256, 256, 0, s>>>(v, np_a);
+    k_scatter<<<sort_blocks(np_a, 256), 256, 0, s>>>(v, np_a);
 }
 
 // One warp per cell: the rank of each member is the number of members with a
@@ -154,36 +167,33 @@ void launch_scatter(const View &v, int np_a, cudaStream_t s) {
 // the layout the state had before -- so every pass sums its pairs in an order
 // that is a function of the positions alone.
 __global__ void k_cellsort(View v, int ncells) {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (warp >= ncells) return;
     if (v.rebin_gate && *v.rebin_gate == 0) return;
-    int b = v.cell_start[warp], e = v.cell_start[warp + 1];
-    int m = e - b;
-    for (int x = lane; x < m; x += 32) {
-        int val = v.order_tmp[b + x];
-        int key = v.a_id[val];
-        int r = 0;
-        for (int t = 0; t < m; ++t) r += (v.a_id[v.order_tmp[b + t]] < key) ? 1 : 0;
-        v.order[b + r] = val;
-        v.cell_b[b + r] = warp;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < ncells;
+         cell += nwarps) {
+        int b = v.cell_start[cell], e = v.cell_start[cell + 1];
+        int m = e - b;
+        for (int x = lane; x < m; x += 32) {
+            int val = v.order_tmp[b + x];
+            int key = v.a_id[val];
+            int r = 0;
+            for (int t = 0; t < m; ++t) r += (v.a_id[v.order_tmp[b + t]] < key) ? 1 : 0;
+            v.order[b + r] = val;
+            v.cell_b[b + r] = cell;
+        }
     }
 }
 
 void launch_cellsort(const View &v, int ncells, cudaStream_t s) {
     if (ncells <= 0) return;
-    int threads = ncells * 32;
-    k_cellsort<<<(threads + 255) / 256, 256, 0, s>>>(v, ncells);
+    k_cellsort<<<sort_blocks((long long)ncells * 32, 256), 256, 0, s>>>(v, ncells);
 }
 
 // Gather the state into B (cell order) and pack the first evaluation's
 // cell-local coordinates: xl = wrap(x) - centre of the particle's cell.
 template <typename R>
-__global__ void k_permute(View v) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= v.np) return;
-    if (v.rebin_gate && *v.rebin_gate == 0) return;
-    if (j == 0 && !v.rebin_gate && v.bin_count) ++*v.bin_count;
+__device__ __forceinline__ void permute_one(const View &v, int j) {
     int k = v.order[j];
     int s = v.a_sim[k];
     const SimDev &S = v.sims[s];
@@ -210,9 +220,17 @@ __global__ void k_permute(View v) {
     ((T4 *)v.pk_vel_out)[j] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
 }
 
+template <typename R>
+__global__ void k_permute(View v) {
+    if (v.rebin_gate && *v.rebin_gate == 0) return;
+    const int first = blockIdx.x * blockDim.x + threadIdx.x;
+    if (first == 0 && !v.rebin_gate && v.bin_count) ++*v.bin_count;
+    for (int j = first; j < v.np; j += gridDim.x * blockDim.x) permute_one<R>(v, j);
+}
+
 void launch_permute(const View &v, int precision, cudaStream_t s) {
     if (v.np <= 0) return;
-    int nb = (v.np + 255) / 256;
+    int nb = sort_blocks(v.np, 256);
     if (precision == SPH_MIXED) k_permute<float><<<nb, 256, 0, s>>>(v);
     else k_permute<double><<<nb, 256, 0, s>>>(v);
 }
@@ -276,13 +294,13 @@ void launch_store_R(double *dst, const void *src, int precision, const int *id, 
 
 __global__ void k_fill_int(int *dst, int val, int n, const int *gate) {
     if (gate && *gate == 0) return;
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) dst[k] = val;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        dst[k] = val;
 }
 
 void launch_fill_int(int *dst, int val, int n, cudaStream_t s, const int *gate) {
     if (n <= 0) return;
-    k_fill_int<<<(n + 255) / 256, 256, 0, s>>>(dst, val, n, gate);
+    k_fill_int<<<sort_blocks(n, 256), 256, 0, s>>>(dst, val, n, gate);
 }
 
 __global__ void k_rebin_close(int *gate, unsigned long long *bin_count) {
