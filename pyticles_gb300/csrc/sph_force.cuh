@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
     {
         PairFrame<R, D> fr;
         fr.init(S);
-        for_pairs<R, D, D == 3>(v, S, fr, P, i, P[i], body, cell_done);
+        for_pairs<R, D, D == 3, false>(v, S, fr, P, i, P[i], body, cell_done);
     }
     R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
     R udr = ud.get();

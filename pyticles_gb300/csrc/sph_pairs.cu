@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v)
         // only the short kernel enters q: cells and pairs beyond its support
         // contribute exactly zero and are not visited
         fr.thr_hi = fr.thr_s;
-        for_pairs<R, D, D == 3>(v, S, fr, P, i, P[i], body, cell_done);
+        for_pairs<R, D, D == 3, false>(v, S, fr, P, i, P[i], body, cell_done);
     }
     R kap = sconst<R>(S).kappa;
     R qq[3] = {kap * q[0].get(), kap * q[1].get(), kap * q[2].get()};

@@ -90,7 +90,13 @@ template <typename R> __device__ __forceinline__ R fmaxf_(R c, R ext) {
 // PF: load the next candidate's position before testing the current one
 // (measured: 4-7% faster for the 3D heat and force passes, slower for the
 // 2D passes and for density, where more warps already hide the latency).
-template <typename R, int D, bool PF = false, typename T4, typename F, typename G>
+//
+// SELF: test j == i and skip it.  A pass whose pair terms all carry the
+// separation d (force, heat flux) may leave it out: for j == i, d = 0 exactly
+// and every kernel's gradient factor is finite at r = 0, so the terms add +0
+// and the sums keep their bits.
+template <typename R, int D, bool PF = false, bool SELF = true, typename T4, typename F,
+          typename G>
 __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                                           const PairFrame<R, D> &fr, const T4 *__restrict__ P,
                                           int i, const T4 &pi, F body, G cell_done) {
@@ -136,7 +142,7 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                             pj = pn;
                             if (j + 1 < je) pn = P[j + 1];
                         }
-                        if (j == i) continue;
+                        if (SELF && j == i) continue;
                         if (!PF) pj = P[j];
                         R d[3];
                         d[0] = pj.x + ox_;

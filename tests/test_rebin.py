@@ -99,3 +99,23 @@ def test_state_upload_forces_a_binning():
         e.advance(1)
         e.sync()
         assert e.rebin_count() == b0 + 1
+
+
+def test_rebin_with_collisions_and_thermostat_tracks_oracle():
+    """Binning on demand combined with hard collisions (extra collision and
+    integrator passes) and the thermostat ramp, RK4."""
+    from pyticles_gb300 import _abi
+    prm, r, v, m, u = hot_fluid("rk4", side=20, temperature=2.0, dt=2e-3, seed=72)
+    prm.collision = _abi.SPH_COLLIDE_EXCHANGE
+    prm.collision_cutoff = 0.9
+    prm.thermostat = 1
+    prm.thermostat_temp = 2.0
+    prm.thermostat_temp_end = 1.0
+    prm.thermostat_ramp_steps = 20
+    steps = 24
+    (rg, vg, ug), bins = run(prm, r, v, m, u, "fp64", steps, rebin=1, per_graph=6)
+    ro, vo, uo, _ = oracle.advance(prm, r, v, m, u, steps)
+    errs = (rel_l2(rg, ro), rel_l2(vg, vo), rel_l2(ug, uo))
+    print("bins", bins, errs)
+    assert max(errs) < STEP_TOL
+    assert bins < steps
