@@ -91,10 +91,11 @@ template <typename R> __device__ __forceinline__ R fmaxf_(R c, R ext) {
 // (measured: 4-7% faster for the 3D heat and force passes, slower for the
 // 2D passes and for density, where more warps already hide the latency).
 //
-// SELF: test j == i and skip it.  A pass whose pair terms all carry the
-// separation d (force, heat flux) may leave it out: for j == i, d = 0 exactly
-// and every kernel's gradient factor is finite at r = 0, so the terms add +0
-// and the sums keep their bits.
+// SELF: skip j == i, which only the home cell (offset 0) can hold, so only its
+// loop tests for it.  A pass whose pair terms all carry the separation d
+// (force, heat flux) may leave the test out: for j == i, d = 0 exactly and
+// every kernel's gradient factor is finite at r = 0, so the terms add +0 and
+// the sums keep their bits.
 template <typename R, int D, bool PF = false, bool SELF = true, typename T4, typename F,
           typename G>
 __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
@@ -133,7 +134,7 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                 const R oy_ = (R)oy * fr.edge[1] - pi.y;
                 const R oz_ = (D == 3) ? (R)oz * fr.edge[2] - pi.z : (R)0;
                 const int jb = v.cell_start[gc], je = v.cell_start[gc + 1];
-                auto scan = [&](auto near) {
+                auto scan = [&](auto near, auto self) {
                     T4 pn;
                     if (PF) pn = P[jb < je ? jb : i];
                     for (int j = jb; j < je; ++j) {
@@ -142,7 +143,7 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                             pj = pn;
                             if (j + 1 < je) pn = P[j + 1];
                         }
-                        if (SELF && j == i) continue;
+                        if (decltype(self)::value && j == i) continue;
                         if (!PF) pj = P[j];
                         R d[3];
                         d[0] = pj.x + ox_;
@@ -156,10 +157,12 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                         body(j, pj, d, rsq, near);
                     }
                 };
-                if (__any_sync(__activemask(), dx * dx + dyz < fr.thr_s))
-                    scan(std::true_type{});
+                if (SELF && ox == 0 && oy == 0 && oz == 0)
+                    scan(std::true_type{}, std::true_type{});
+                else if (__any_sync(__activemask(), dx * dx + dyz < fr.thr_s))
+                    scan(std::true_type{}, std::false_type{});
                 else
-                    scan(std::false_type{});
+                    scan(std::false_type{}, std::false_type{});
                 cell_done();
             }
         }
