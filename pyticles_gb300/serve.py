@@ -30,11 +30,13 @@ from .workloads import lattice_system, rng_for, vdw_energy
 # Bytes of engine state per particle (mirrors alloc_particles in
 # csrc/sph_engine.cu): FP64 state A/B, evaluation positions/velocities, cell
 # origins (3 axes x 8 arrays x 8 B), rates and factors in the pass precision,
-# ids and sort scratch, packed vectors, staging.
+# ids and sort scratch, seven packed vectors (positions and velocities of two
+# stages, force factors, heat factors, the force pass's neighbour record),
+# staging.
 def bytes_per_particle(precision="mixed", integrator="ieuler"):
     rs = 4 if precision == "mixed" else 8
     v4 = 4 * rs
-    b = 3 * 8 * 8 + 9 * rs + 5 * 8 + 9 * 4 + 6 * v4 + 10 * rs + 4 * 8
+    b = 3 * 8 * 8 + 9 * rs + 5 * 8 + 9 * 4 + 7 * v4 + 10 * rs + 4 * 8
     if integrator == "rk4":
         b += 7 * 8
     return b
