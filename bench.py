@@ -129,16 +129,22 @@ def measured_peaks():
         return 6800.0, "fallback", 2070.0
 
 
-def committed_traffic(name):
-    """DRAM bytes per particle of one force launch from the committed ncu
-    summary (`dram_bytes_per_particle: X` line), or None."""
+def committed_figure(name, key):
+    """A per-particle figure (`key: X` line) of one launch from a committed ncu
+    summary under profiles/, or None."""
     path = os.path.join(ROOT, "profiles", name)
     try:
         txt = open(path).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_particle:\s*([0-9.eE+-]+)", txt)
+    m = re.search(key + r":\s*([0-9.eE+-]+)", txt)
     return float(m.group(1)) if m else None
+
+
+def committed_traffic(name):
+    """DRAM bytes per particle of one force launch from the committed ncu
+    summary (`dram_bytes_per_particle: X` line), or None."""
+    return committed_figure(name, "dram_bytes_per_particle")
 
 
 def initial_state(side, seed):
@@ -403,6 +409,10 @@ def main():
     bpp = 0.5 * (force_bytes_per_particle(2, 4, False) + force_bytes_per_particle(2, 4, True))
     achieved = bpp * n / (avg_ms * 1e-3) / 1e9
     trafpp = committed_traffic("k_force_2d_mixed.md")
+    # issue roofline: the launch's warp instructions (ncu, per particle) over
+    # the live launch time against 152 SMs x 4 schedulers x 1 per cycle
+    winst_pp = committed_figure("k_force_2d_mixed.md", "warp_instructions_per_particle")
+    issue_peak = 152 * 4 * sm_max * 1e6
     flops = FLOPS_FORCE[2] * pairs / (avg_ms * 1e-3) / 1e12
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
     total_pass_ms = sum(p["ms"] for p in passes.values())
@@ -455,6 +465,13 @@ def main():
                           "frac": flops / fp32_peak,
                           "note": "algorithmic flops of the force pass; peak = 152 SMs x 128 "
                                   "FP32 lanes x 2 x max SM clock (nominal)"},
+            "issue": None if winst_pp is None else {
+                "achieved_warp_inst_per_s": winst_pp * n / (avg_ms * 1e-3),
+                "peak_warp_inst_per_s": issue_peak,
+                "frac": winst_pp * n / (avg_ms * 1e-3) / issue_peak,
+                "note": "the binding limit: warp instructions of one force launch from the "
+                        "committed ncu summary over the live launch time; peak = 152 SMs x 4 "
+                        "issue slots x max SM clock"},
             "force_share_of_step": f["ms"] / total_pass_ms if total_pass_ms > 0 else None,
         },
         "cpu_baseline": cpu,
