@@ -122,13 +122,6 @@ template <> __device__ __forceinline__ float fsqrt<float>(float x) {
 }
 template <> __device__ __forceinline__ double fsqrt<double>(double x) { return sqrt(x); }
 
-// Fast-test bounds around the pair threshold.  In mixed mode the squared
-// distance comes from FP32 cell-local coordinates whose error is below
-// 5e-6 relative for cell edges up to twice the cutoff; pairs whose FP32
-// rsq lies within 2^-12 of the threshold are re-tested exactly in FP64.
-template <typename R> struct Margin;
-template <> struct Margin<float> { static constexpr double rel = 1.0 / 4096.0; };
-template <> struct Margin<double> { static constexpr double rel = 1e-9; };
 
 // ---- smoothing kernels: W(r) and g = (dW/dr)/r, so dwdx = g (r_j - r_i) ----
 // Lucy (spkernel.py:86-118), Gaussian (spkernel.py:39-52, Lucy's gradient

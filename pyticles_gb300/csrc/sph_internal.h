@@ -21,8 +21,6 @@
 
 namespace sph {
 
-constexpr int kMaxNbr = 27;
-
 // Pair-pass constants of one simulation in the arithmetic type of the
 // passes, precomputed on the host so that no thread spends FP64 work (or a
 // division) deriving them.  Index 0 = short smoothing length, 1 = long.

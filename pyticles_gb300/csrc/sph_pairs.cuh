@@ -62,8 +62,6 @@ struct PairFrame {
     }
 };
 
-template <int D> struct NbrCount { static constexpr int value = D == 2 ? 9 : 27; };
-
 // max(|c| - ext, 0): distance along one axis from particle i to a cell whose
 // centre sits at c relative to i
 template <typename R> __device__ __forceinline__ R fmaxf_(R c, R ext) {
