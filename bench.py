@@ -34,31 +34,11 @@ if ROOT not in sys.path:
 METRIC = "pair-interactions/s & p50/p99 job latency, mixed vs plain FP64, 1 GB300"
 UNIT = "pair-interactions/s"
 L2_BYTES = 129e6
-# algorithmic flops per unordered pair per evaluation (add/mul/div/sqrt = 1,
-# fma = 2; compares and minimum image = 0): density 3d+24, force 10d+42,
-# 3D heat flux adds 7d+12 + 3d+4
-FLOPS_DENSITY = {2: 30, 3: 33}
-FLOPS_FORCE = {2: 62, 3: 72}
 
 
 def rank_info():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
-
-
-def force_bytes_per_particle(dim, rsize, stage_final):
-    """Unique bytes the force pass moves per particle (each array read or
-    written once): packed position/velocity/force factors, cell and
-    simulation ids, FP64 x0, v0, evaluation velocity, u0, m; writes of the
-    rates plus either the next evaluation state or the final state."""
-    v4 = 4 * rsize
-    reads = 3 * v4 + 8 + 3 * 8 * dim + 16
-    if stage_final:
-        reads += (dim + 1) * rsize            # stage-0 rates
-        writes = (dim + 1) * rsize + 8 * (2 * dim + 2) + 8
-    else:
-        writes = 2 * (dim + 1) * rsize + 8 * (2 * dim + 1) + 2 * v4
-    return reads + writes
 
 
 class ClockSampler:
@@ -284,6 +264,32 @@ def run_e2e(prm, r, v, m, u, steps, torch, stream):
     return wall, pairs, n * (2 * d + 2) * 8, n * (2 * d + 1) * 8
 
 
+def accuracy_track(prm, r, v, m, u, steps, every, stream):
+    """Mixed-precision accuracy along the benchmarked trajectory: every
+    `every` steps the GPU evaluates f(x) at its current state and the FP64
+    oracle re-evaluates it at the same state; relative L2 of rho, vdot and
+    udot."""
+    from oracle import oracle
+    from pyticles_gb300 import Engine
+    out = []
+    with Engine(prm, "mixed", max_particles=len(r), stream=stream.cuda_stream) as e:
+        s = e.add(prm, r, v, m, u)
+        e.set_tuning(rebin=1, steps_per_graph=every)
+        done = 0
+        while done < steps:
+            e.advance(every)
+            done += every
+            rs, vs, us = e.get_state(s)
+            g = e.derivatives(s)
+            e.sync()
+            ref = oracle.derivatives(prm, rs, vs, m, us)
+            row = {"step": done}
+            for k in ("rho", "vdot", "udot"):
+                row[k] = float(np.linalg.norm(g[k] - ref[k]) / np.linalg.norm(ref[k]))
+            out.append(row)
+    return out
+
+
 def oracle_rate(side, seed, budget_s, max_steps):
     """FP64 C oracle (OpenMP, all host threads) on a bounded sample."""
     from oracle import oracle
@@ -355,6 +361,8 @@ def main():
     ap.add_argument("--steps3d", type=int, default=20)
     ap.add_argument("--serve-jobs", type=int, default=12)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--accuracy-steps", type=int, default=1000,
+                    help="trajectory length of the mixed-vs-FP64 accuracy report (0: skip)")
     ap.add_argument("--rebin", type=int, default=1, choices=[0, 1],
                     help="single-simulation workloads: 1 bins into cells on demand "
                          "(tuning.rebin), 0 every step")
@@ -406,14 +414,15 @@ def main():
     f = passes["force"]
     nlaunch = max(1, f["launches"])
     avg_ms = f["ms"] / nlaunch
-    bpp = 0.5 * (force_bytes_per_particle(2, 4, False) + force_bytes_per_particle(2, 4, True))
+    from pyticles_gb300 import opcount
+    bpp = opcount.force_bytes_per_step_average(2, 4, reuse=bool(args.rebin))
     achieved = bpp * n / (avg_ms * 1e-3) / 1e9
     trafpp = committed_traffic("k_force_2d_mixed.md")
     # issue roofline: the launch's warp instructions (ncu, per particle) over
     # the live launch time against 152 SMs x 4 schedulers x 1 per cycle
     winst_pp = committed_figure("k_force_2d_mixed.md", "warp_instructions_per_particle")
     issue_peak = 152 * 4 * sm_max * 1e6
-    flops = FLOPS_FORCE[2] * pairs / (avg_ms * 1e-3) / 1e12
+    flops = opcount.FLOPS_FORCE[2] * pairs / (avg_ms * 1e-3) / 1e12
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
     total_pass_ms = sum(p["ms"] for p in passes.values())
 
@@ -424,6 +433,11 @@ def main():
         extras["fluid3d"] = timed_workload(fluid3d_workload(args.side3d), args.steps3d, 3,
                                            torch, stream, rebin=args.rebin)
         extras["serve"] = serve_window(args.serve_jobs, args.serve_seconds)
+
+    accuracy = None
+    if rank == 0 and not args.no_cpu and args.accuracy_steps > 0:
+        accuracy = accuracy_track(prm, r, v, m, u, args.accuracy_steps,
+                                  max(1, min(100, args.accuracy_steps)), stream)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -475,6 +489,11 @@ def main():
             "force_share_of_step": f["ms"] / total_pass_ms if total_pass_ms > 0 else None,
         },
         "cpu_baseline": cpu,
+        "accuracy": None if accuracy is None else {
+            "what": "relative L2 of the mixed-precision evaluation against the FP64 oracle "
+                    "at the GPU state, every 100 steps of the benchmarked trajectory",
+            "max": {k: max(row[k] for row in accuracy) for k in ("rho", "vdot", "udot")},
+            "track": accuracy},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
         "gpu_launches": kps * args.steps,

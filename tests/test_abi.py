@@ -82,3 +82,14 @@ def test_params_roundtrip():
                          thermostat_ramp_steps=500)
     q = _abi.params_from_dict(_abi.params_dict(p))
     assert bytes(q) == bytes(p)
+
+
+def test_algorithmic_counts():
+    """Work units of the rooflines: 92 flops per pair in 2D and 151 in 3D with
+    heat flux; 216 unique bytes per particle for the first 2D mixed force
+    launch."""
+    from pyticles_gb300 import opcount
+    assert opcount.flops_per_pair(2) == 92
+    assert opcount.flops_per_pair(3, heat=True) == 151
+    assert opcount.force_bytes_per_particle(2, 4, False) == 216
+    assert opcount.force_bytes_per_step_average(2, 4) == (216 + 184) / 2
