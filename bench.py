@@ -34,6 +34,8 @@ if ROOT not in sys.path:
 METRIC = "pair-interactions/s & p50/p99 job latency, mixed vs plain FP64, 1 GB300"
 UNIT = "pair-interactions/s"
 L2_BYTES = 129e6
+WORKLOAD_2D = ("2D van der Waals fluid, {side}^2 lattice, Lucy h_s=3 h_l=6, viscosity, "
+               "improved Euler dt=1e-3, periodic")
 
 
 def rank_info():
@@ -313,7 +315,9 @@ def reference_arm(args):
     rank, world, _ = rank_info()
     if rank != 0:
         return 0
-    side = min(args.side, 512)
+    # a bounded sample of the workload: 512^2 (256^2 for long runs, so that
+    # the whole run stays within a few minutes on the host cores)
+    side = min(args.side, 512 if args.steps <= 300 else 256)
     from oracle import oracle
     prm, r, v, m, T0 = initial_state(side, 1000)
     u = oracle.initial_energy(prm, r, v, m, T0)
@@ -330,8 +334,9 @@ def reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "2d_vdw_fluid", "n": len(r), "pairs_per_eval": nip,
-                       "evals_per_step": 2, "precision": "fp64"},
+            "config": {"workload": WORKLOAD_2D.format(side=args.side), "n": args.side ** 2,
+                       "evals_per_step": 2, "precision": "fp64 (the reference's arithmetic)",
+                       "sample": {"n": len(r), "pairs_per_eval": nip}},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.threads(),
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -457,8 +462,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded lattice + jitter, Maxwell velocities)",
         "config": {
-            "workload": "2D van der Waals fluid, 1024^2 lattice, Lucy h_s=3 h_l=6, viscosity, "
-                        "improved Euler dt=1e-3, periodic",
+            "workload": WORKLOAD_2D.format(side=args.side),
             "n": n, "pairs_per_eval": pairs, "evals_per_step": 2,
             "precision": "mixed: f32 pair arithmetic + compensated sums, f64 pair test, "
                          "integrator and reductions",
