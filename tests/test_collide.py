@@ -239,3 +239,22 @@ def test_collision_params_survive_the_dict_roundtrip():
     back = _abi.params_from_dict(_abi.params_dict(prm))
     assert back.collision == 1 and back.collision_cutoff == 0.5
     assert ctypes.sizeof(back) == ctypes.sizeof(_abi.SphParams)
+
+
+@pytest.mark.gpu
+def test_collision_capacity_overflow_is_reported(built):
+    """More colliding pairs than particles in one evaluation: the engine
+    reports SPH_ECAPACITY and applies none of them."""
+    prm, r, v, m, T0 = workloads.lattice_system(12, 2, spacing=1.0, jitter=0.1,
+                                                temperature=0.6, seed=81, kernel="lucy",
+                                                h_short=2.0, h_long=3.0, dt=1e-3)
+    prm.collision = _abi.SPH_COLLIDE_EXCHANGE
+    prm.collision_cutoff = 2.9       # ~25 partners per particle
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    with Engine(prm, "mixed", max_particles=len(r)) as e:
+        s = e.add(prm, r, v, m, u)
+        e.advance(1)
+        with pytest.raises(_abi.SphError) as ei:
+            e.sync()
+        assert ei.value.status == _abi.SPH_ECAPACITY
+        assert e.status(s) == _abi.SPH_ECAPACITY
