@@ -85,12 +85,16 @@ class SmoothParticleSystem(ParticleSystem):
 
     precision -- 'fp64' (default: the reference's arithmetic) or 'mixed'
                  (FP32 pair arithmetic, FP64 pair test and integrator)
+    rebin     -- keep the cell list of the last binning across steps of run()
+                 until a particle has used half of its cell slack (the skin
+                 reuse of VerletList.compress/ponder_rebuild); the pair set
+                 stays exact, the summation order follows the binning times
     """
 
     def __init__(self, n, d=3, maxn=100, controllers=(), xmax=XMAX, ymax=YMAX, zmax=ZMAX,
                  vmax=VMAX, rinit=None, side=None, mass=1.0, spacing=None, temperature=1.0,
                  thermostat_temp=1.0, thermostat=False, hshort=1.0, hlong=3.0, source=None,
-                 integrator="ieuler", simbox=None, precision="fp64"):
+                 integrator="ieuler", simbox=None, precision="fp64", rebin=False):
         ParticleSystem.__init__(self, n=n, d=d, xmax=xmax, ymax=ymax, zmax=zmax, rinit=rinit,
                                 side=side, mass=mass, source=source, spacing=spacing,
                                 integrator=integrator, vmax=vmax, maxn=maxn, simbox=simbox,
@@ -116,6 +120,7 @@ class SmoothParticleSystem(ParticleSystem):
         self.P = np.zeros([self.maxn, self.dim, self.dim])
         self.thermostat_temp = thermostat_temp
         self.precision = precision
+        self.rebin = bool(rebin)
         self.timing["SPAM time"] = -1
         self.timing["nlist rebuild time"] = -1
         self._engine = None
@@ -198,6 +203,7 @@ class SmoothParticleSystem(ParticleSystem):
                 self._engine.close()
             self._engine = Engine(prm, precision=self.precision, max_particles=max(n, 1),
                                   max_sims=1)
+            self._engine.set_tuning(rebin=int(self.rebin))
             self._sim = self._engine.add(prm, self.r[:n], self.v[:n], self.m[:n], self.u[:n])
             self._engine_key = key
         else:

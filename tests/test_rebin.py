@@ -119,3 +119,26 @@ def test_rebin_with_collisions_and_thermostat_tracks_oracle():
     print("bins", bins, errs)
     assert max(errs) < STEP_TOL
     assert bins < steps
+
+
+def test_particle_system_run_with_rebin():
+    """SmoothParticleSystem(rebin=True).run: the Python API path."""
+    from pyticles_gb300 import PeriodicBox, SmoothParticleSystem, SpamComplete, VerletList
+    prm, r, v, m, u = hot_fluid("ieuler", side=20)
+    n = len(r)
+    box = PeriodicBox(xmax=20.0, ymax=20.0, zmax=1)
+    p = SmoothParticleSystem(n, d=2, maxn=n, hshort=2.0, hlong=3.0, simbox=box,
+                             precision="fp64", rebin=True)
+    p.r[:] = r
+    p.v[:] = v
+    p.m[:] = m
+    p.u[:] = u
+    nl = VerletList(p, cutoff=3.0, tolerance=0.0)
+    p.nlists.append(nl)
+    p.nl_default = nl
+    p.forces.append(SpamComplete(p, nl, eta=prm.visc_alpha, zeta=prm.visc_beta))
+    p.run(prm.dt, 30)
+    assert p._engine.rebin_count() < 30
+    ro, vo, uo, _ = oracle.advance(prm, r, v, m, u, 30)
+    assert rel_l2(p.r[:n], ro) < STEP_TOL and rel_l2(p.v[:n], vo) < STEP_TOL
+    p.close()
