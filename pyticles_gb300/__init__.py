@@ -9,6 +9,7 @@ Reference-facing API (same names as andrewcharles/pyticles):
     Force, SpamForce, CohesiveSpamForce, SpamConduction, SpamComplete
     CollisionForce, CollisionForce3d, FortranCollisionForce
     PeriodicBox
+    properties.spam_properties, vdw, vdw_energy, vdw_temp
 Engine-level API: Engine (many simulations per engine), workloads, serve.
 """
 from ._abi import KERNELS, SphError, SphParams, make_params  # noqa: F401
@@ -18,5 +19,6 @@ from .forces import (CohesiveSpamForce, CollisionForce, CollisionForce3d,  # noq
                      Force, FortranCollisionForce, SpamComplete, SpamConduction, SpamForce)
 from .neighbour_list import NeighbourList, SortedVerletList, VerletList  # noqa: F401
 from .particles import ParticleSystem, SmoothParticleSystem  # noqa: F401
+from . import properties  # noqa: F401
 
 __version__ = "0.1.0"

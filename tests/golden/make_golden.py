@@ -347,6 +347,32 @@ def collision_lists(R):
     print("collide_lists:", {k: v.shape for k, v in out.items() if k.startswith("iap")})
 
 
+def spam_properties_case(R):
+    """properties.spam_properties (properties.py:63-120) on the 3D lattice of
+    lucy3d_27 with T = T0: densities, pressures, u from T."""
+    particles, nlm, boxm, props = R["particles"], R["neighbour_list"], R["box"], R["properties"]
+    prm, r, v, m, T0 = workloads.lattice_system(3, 3, spacing=1.1, jitter=0.1,
+                                                temperature=0.6, seed=11)
+    n = len(r)
+    sbox = boxm.PeriodicBox(xmax=3.3, ymax=3.3, zmax=3.3)
+    p = particles.SmoothParticleSystem(n, d=3, maxn=n, xmax=3.3, ymax=3.3, zmax=3.3,
+                                       hshort=1.2, hlong=1.6, simbox=sbox)
+    sbox.p = p
+    p.r[:, :] = r
+    p.v[:, :] = v
+    p.m[:] = m
+    p.t[:] = T0
+    nl = nlm.VerletList(p, cutoff=1.6, tolerance=0.0)
+    nl.build()
+    nlm.NeighbourList.separations(nl)
+    props.spam_properties(p, nl)
+    np.savez_compressed(os.path.join(HERE, "spam_props.npz"), r=r, v=v, m=m, T0=T0,
+                        box=np.array([3.3, 3.3, 3.3]), h=1.2, hlr=1.6, cutoff=1.6,
+                        rho=p.rho[:n].copy(), p=p.p[:n].copy(), pco=p.pco[:n].copy(),
+                        u=p.u[:n].copy(), t=p.t[:n].copy())
+    print("spam_props:", n, float(p.rho[:n].mean()))
+
+
 def kernel_table(R):
     spk = R["spkernel"]
     rows = []
@@ -476,6 +502,8 @@ def main():
             pair_edge_cases(R)
         if want("splat"):
             splat_maps(R)
+        if want("spam_props"):
+            spam_properties_case(R)
         if want("collide_lists"):
             collision_lists(R)
         if want("collide2d_144"):

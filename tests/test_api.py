@@ -182,3 +182,24 @@ def test_run_many_steps_equals_update_loop():
         p.close()
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_spam_properties_matches_reference():
+    """properties.spam_properties(p, nl) on the GPU against the reference's
+    own output (tests/golden/spam_props.npz)."""
+    from pyticles_gb300 import properties
+    g = load("spam_props")
+    n = len(g["r"])
+    box = PeriodicBox(xmax=3.3, ymax=3.3, zmax=3.3)
+    p = SmoothParticleSystem(n, d=3, maxn=n, hshort=float(g["h"]), hlong=float(g["hlr"]),
+                             simbox=box)
+    p.r[:] = g["r"]
+    p.v[:] = g["v"]
+    p.m[:] = g["m"]
+    p.t[:] = float(g["T0"])
+    nl = VerletList(p, cutoff=float(g["cutoff"]), tolerance=0.0)
+    properties.spam_properties(p, nl)
+    for k in ("rho", "p", "pco", "u", "t"):
+        a, b = getattr(p, k)[:n], g[k]
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-12, k

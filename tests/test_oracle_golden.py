@@ -145,3 +145,23 @@ def test_collision_steps_match_reference():
     _, v_free, _, _ = oracle.advance(collide_params(g, collision_cutoff=0.0), g["r0"], g["v0"],
                                      g["m"], g["u0"], int(g["steps"]))
     assert rel_l2(v_free, g["v_step3"]) > 0.1
+
+
+def test_spam_properties_formulas_match_reference():
+    """properties.spam_properties: the EOS steps applied to the reference's
+    own densities reproduce its pressures, energies and temperatures bit for
+    bit; the oracle's density matches the reference's."""
+    from pyticles_gb300 import properties
+    g = load("spam_props")
+    rho = g["rho"]
+    p, pco = properties.vdw(rho, np.full(len(rho), float(g["T0"])))
+    assert np.array_equal(p, g["p"]) and np.array_equal(pco, g["pco"])
+    u = properties.vdw_energy(rho, float(g["T0"]))
+    assert np.array_equal(u, g["u"])
+    assert np.array_equal(properties.vdw_temp(rho, u), g["t"])
+    prm = params_of({"dim": 3, "kernel": "lucy", "box": g["box"], "h_short": float(g["h"]),
+                     "h_long": float(g["hlr"]), "cutoff": float(g["cutoff"]), "tolerance": 0.0,
+                     "dt": 1e-3, "integrator": "ieuler", "thermostat": 0,
+                     "thermostat_temp": 1.0})
+    d = oracle.derivatives(prm, g["r"], g["v"], g["m"], np.zeros(len(rho)))
+    assert rel_l2(d["rho"], rho) < EVAL_TOL
