@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE ONLY: ctypes wrapper of the FP64 CPU oracle
 (oracle/sph_oracle.c).  Imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline / reference legs only, as the checker.
+bench.py's CPU-baseline / reference legs only, to compare results against.
 
 build() compiles oracle/sph_oracle.c with gcc (-O2 -fopenmp
 -ffp-contract=off) into oracle/_build/liboracle.so.

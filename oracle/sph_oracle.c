@@ -2,8 +2,8 @@
  * sph_oracle.c -- TEST INFRASTRUCTURE ONLY (the oracle).
  *
  * FP64 CPU restatement of pyticles' SPH step, used by tests/, by
- * __graft_entry__.smoke() and by bench.py's CPU-baseline / reference legs as
- * the checker.  Nothing in pyticles_gb300/ links or calls it.
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline / reference legs to
+ * compare results against.  Nothing in pyticles_gb300/ links or calls it.
  *
  * Parity pinning: tests/test_oracle_golden.py checks this file against golden
  * vectors in tests/golden/ that tests/golden/make_golden.py produced by
