@@ -6,7 +6,7 @@ the van der Waals pressures from the current temperatures and the energies
 those temperatures imply (properties.py:63-120).  The density comes from
 libsph's density pass at the current positions (the pair set of a freshly
 built list); the velocity gradient tensor p.gradv, which no force uses, is
-not computed.  The drivers call it once to initialise u from T.
+not computed.  pyticles' run scripts call it once to initialise u from T.
 
 vdw, vdw_energy, vdw_temp -- the equation-of-state formulas of
 properties.py:38-49 on host arrays, for setting up states.

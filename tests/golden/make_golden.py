@@ -229,7 +229,7 @@ def build_system(R, r, v, m, u, box_len, dim, hs, hl, cutoff, tol, kname, integ=
 
 def ref_initial_energy(R, r, v, m, box_len, dim, hs, hl, cutoff, tol, kname, T0):
     """u0 = vdw_energy(rho0, T0) after one density evaluation
-    (properties.py:116-119, the drivers' spam_properties call)."""
+    (properties.py:116-119, the run scripts' spam_properties call)."""
     p, nl, force = build_system(R, r, v, m, np.zeros(len(r)), box_len, dim, hs, hl, cutoff,
                                 tol, kname)
     force.apply()
@@ -290,7 +290,7 @@ def run_case(R, name, r, v, m, box_len, dim, hs, hl, cutoff, tol, kname, T0, ste
 def collision_case(R, name, r, v, m, box_len, dim, hs, hl, cutoff, kname, T0, steps, coll,
                    dt=1e-3, integ="ieuler"):
     """SmoothParticleSystem.update with p.forces = [SpamComplete's sequence,
-    forces.CollisionForce(p, nl, cutoff=coll)] -- the order of the drivers
+    forces.CollisionForce(p, nl, cutoff=coll)] -- the order of the run scripts
     (bspana.py:45-46, fspana.py:117-119)."""
     t0 = time.time()
     n = r.shape[0]
