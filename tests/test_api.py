@@ -1,7 +1,7 @@
 """The reference-facing API (pyticles_gb300 mirrors of particles.py,
 neighbour_list.py, forces.py, spam_complete_force.py, box.py), with the
 reference's own unit tests re-expressed (test/neighbour_list_test.py,
-test/force_test.py) and a driver in the shape of run_scripts/bspana_profile.py.
+test/force_test.py) and a run script in the shape of run_scripts/bspana_profile.py.
 Host-side logic runs on CPU; anything that evaluates runs on the GPU."""
 import numpy as np
 import pytest
