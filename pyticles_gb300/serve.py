@@ -11,10 +11,14 @@ released -- when its steps are done.  The 2D and 3D engines run their chunks
 concurrently.  Per job: queueing delay (admission - arrival), service time
 (completion - admission) and latency (completion - arrival).
 
-Failure handling: a job larger than its group's whole capacity is rejected at
-admission; a job whose state turns non-finite (or whose particles outrun the
-cell slack) is retired with that error after the chunk in which it happened,
-and the other jobs continue unaffected (their particles never interact).
+Failure handling: a malformed job (array shapes that disagree with its
+dimension or size, no steps) or one larger than its group's whole capacity is
+rejected at admission; a job the engine refuses to add (an allocation or
+parameter error) fails with that status; a job whose state turns non-finite
+(or whose particles outrun the cell slack) is retired with that error after
+the chunk in which it happened.  The other jobs continue unaffected (their
+particles never interact).  The report carries the HBM budget, each group's
+particle capacity and its peak use.
 """
 import collections
 import math
@@ -121,6 +125,7 @@ class Group:
         self.engine.set_tuning(steps_per_graph=chunk, use_graph=1)
         self.active = {}          # sim id -> job
         self.live = 0
+        self.peak = 0
 
     def fits(self, job):
         return len(self.active) < self.max_sims and self.live + job.n <= self.capacity
@@ -131,6 +136,7 @@ class Group:
         job.remaining = job.steps
         self.active[job.sim] = job
         self.live += job.n
+        self.peak = max(self.peak, self.live)
 
     def launch(self):
         """Enqueues one chunk (asynchronous); returns its step count."""
@@ -174,6 +180,24 @@ class Group:
         self.engine.close()
 
 
+def malformed(job):
+    """Why a job cannot be served as given, or None."""
+    if job.dim not in (2, 3):
+        return "dimension must be 2 or 3"
+    n = len(job.r)
+    if n == 0:
+        return "no particles"
+    for name, a, shape in (("r", job.r, (n, job.dim)), ("v", job.v, (n, job.dim)),
+                           ("m", job.m, (n,)), ("u", job.u, (n,))):
+        if np.shape(a) != shape:
+            return f"{name} has shape {np.shape(a)}, expected {shape}"
+    if job.steps <= 0:
+        return "no steps"
+    if job.params is not None and getattr(job.params, "dim", job.dim) != job.dim:
+        return "parameters of another dimension"
+    return None
+
+
 def default_engine_factory(params, precision, capacity, max_sims, stream):
     return Engine(params, precision, max_particles=capacity, max_sims=max_sims, stream=stream)
 
@@ -187,6 +211,7 @@ class Server:
         self.precision = precision
         self.chunk = chunk
         self.clock = clock
+        self.hbm_budget = float(hbm_budget_bytes)
         bpp = bytes_per_particle(precision)
         caps = {2: hbm_budget_bytes * share_2d / bpp, 3: hbm_budget_bytes * (1 - share_2d) / bpp}
         if group_params is None:
@@ -218,13 +243,24 @@ class Server:
             # admission: first fit in arrival order
             still = []
             for job in waiting:
+                why = malformed(job)
+                if why is not None:
+                    job.error = "rejected: " + why
+                    job.finished = t
+                    self.rejected.append(job)
+                    continue
                 g = self.groups[job.dim]
                 if job.n > g.capacity:
                     job.error = "rejected: larger than the group's HBM budget"
                     job.finished = t
                     self.rejected.append(job)
                 elif g.fits(job):
-                    g.admit(job, t)
+                    try:
+                        g.admit(job, t)
+                    except _abi.SphError as exc:
+                        job.error = _abi.STATUS_NAMES.get(exc.status, str(exc.status))
+                        job.finished = t
+                        completed.append(job)
                 else:
                     still.append(job)
             waiting = still
@@ -247,7 +283,12 @@ class Server:
         service = np.array([j.finished - j.admitted for j in ok]) if ok else np.zeros(1)
         work = sum(j.work for j in completed)
         window = max(j.arrival for j in jobs) if jobs else 0.0
+        bpp = bytes_per_particle(self.precision)
         return {
+            "hbm_budget_bytes": self.hbm_budget,
+            "capacity_particles": {d: g.capacity for d, g in self.groups.items()},
+            "peak_particles": {d: g.peak for d, g in self.groups.items()},
+            "peak_hbm_bytes": sum(g.peak for g in self.groups.values()) * bpp,
             "jobs": len(jobs), "completed": len(ok),
             "failed": len([j for j in completed if j.error]), "rejected": len(self.rejected),
             "latency_p50_s": float(np.percentile(lat, 50)),

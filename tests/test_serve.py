@@ -23,6 +23,8 @@ class FakeEngine:
         pass
 
     def add(self, prm, r, v, m, u):
+        if len(r) == 77:          # an allocation the device refuses
+            raise _abi.SphError(_abi.SPH_ENOMEM, "sph_sim_add")
         sid = self.next_id
         self.next_id += 1
         self.sims[sid] = {"n": len(r), "steps": 0, "nan": bool(np.isnan(u).any())}
@@ -119,6 +121,25 @@ def test_failed_job_is_retired_and_others_continue():
     assert jobs[1].error == "SPH_ENAN" and jobs[1].result is None
     assert jobs[0].result == (20,) and jobs[2].result == (20,)
     assert rep["failed"] == 1 and rep["completed"] == 2
+
+
+def test_malformed_and_refused_jobs_fail_alone():
+    """Host-side injected failures: a malformed request and an allocation
+    the engine refuses; the other jobs complete with their full steps."""
+    srv = fake_server(1000, chunk=5)
+    bad = fake_job(1, 0.0, 2, 50, 10)
+    bad.r = np.zeros((50, 3))                     # 3 columns in the 2D group
+    nomem = fake_job(2, 0.0, 2, 77, 10)
+    nosteps = fake_job(3, 0.0, 3, 20, 0)
+    good = [fake_job(0, 0.0, 2, 100, 20), fake_job(4, 0.0, 3, 60, 15)]
+    rep = srv.run(good + [bad, nomem, nosteps], realtime=False)
+    assert bad.error.startswith("rejected: r has shape")
+    assert nosteps.error == "rejected: no steps"
+    assert nomem.error == "SPH_ENOMEM" and nomem.result is None
+    assert [j.result[0] for j in good] == [20, 15]
+    assert rep["completed"] == 2 and rep["rejected"] == 2 and rep["failed"] == 1
+    assert rep["peak_particles"][2] == 100 and rep["peak_particles"][3] == 60
+    assert rep["peak_hbm_bytes"] == 160 * serve.bytes_per_particle("mixed")
 
 
 def test_latency_accounting_uses_arrival_times():
