@@ -49,7 +49,9 @@ enum sph_status {
     SPH_ESKIN = 7,           /* a particle moved further within one step than the
                                 cell slack allows (cell list would miss pairs)   */
     SPH_ECAPACITY = 8,       /* engine particle / simulation capacity exceeded  */
-    SPH_ENOTFOUND = 9        /* unknown simulation id                           */
+    SPH_ENOTFOUND = 9,       /* unknown simulation id                           */
+    SPH_EBOUNDS = 10         /* an index check of a checking build failed (the
+                                access was skipped; release builds do not check) */
 };
 
 /* Kernel ids follow spkernel.ktable (spkernel.py:20): 1 gaussian, 2 lucy,

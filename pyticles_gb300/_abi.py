@@ -9,7 +9,11 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libsph.so")
+# PYTICLES_CHECKS=1 selects the checking build (device-side index checks that
+# report SPH_EBOUNDS instead of accessing out of range), made by
+# build.build(checks=True)
+CHECKS = os.environ.get("PYTICLES_CHECKS", "0") == "1"
+LIB_PATH = os.path.join(HERE, "_build", "libsph_checks.so" if CHECKS else "libsph.so")
 
 # status codes (enum sph_status)
 SPH_OK = 0
@@ -22,13 +26,14 @@ SPH_ECUDA = 6
 SPH_ESKIN = 7
 SPH_ECAPACITY = 8
 SPH_ENOTFOUND = 9
+SPH_EBOUNDS = 10
 PASSES = ("sort", "density", "heat", "tsum", "force")
 NOALLOC_MAX_PARTICLES = 16384
 
 STATUS_NAMES = {
     0: "SPH_OK", 1: "SPH_EINVAL", 2: "SPH_ENOMEM", 3: "SPH_ECELL_OVERFLOW",
     4: "SPH_ETIMEOUT", 5: "SPH_ENAN", 6: "SPH_ECUDA", 7: "SPH_ESKIN",
-    8: "SPH_ECAPACITY", 9: "SPH_ENOTFOUND",
+    8: "SPH_ECAPACITY", 9: "SPH_ENOTFOUND", 10: "SPH_EBOUNDS",
 }
 
 # kernel ids follow spkernel.ktable (spkernel.py:20) plus the cubic spline

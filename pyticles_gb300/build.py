@@ -37,38 +37,48 @@ def _deps():
     return files
 
 
-def up_to_date():
-    if not os.path.exists(LIB):
+def lib_path(checks=False):
+    return os.path.join(OUT, "libsph_checks.so" if checks else "libsph.so")
+
+
+def up_to_date(checks=False):
+    path = lib_path(checks)
+    if not os.path.exists(path):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(path)
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
-def _compile(src):
-    obj = os.path.join(OUT, os.path.basename(src).replace(".cu", ".o"))
-    cmd = [nvcc()] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(src, checks=False):
+    suffix = "_checks.o" if checks else ".o"
+    obj = os.path.join(OUT, os.path.basename(src).replace(".cu", suffix))
+    extra = ["-DSPH_DEBUG_CHECKS"] if checks else []
+    cmd = [nvcc()] + ARCH + FLAGS + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{res.stderr}")
     return obj
 
 
-def build(force=False, verbose=False):
-    """Compiles every CUDA translation unit and links libsph.so."""
-    if not force and up_to_date():
-        return LIB
+def build(force=False, verbose=False, checks=False):
+    """Compiles every CUDA translation unit and links libsph.so; with checks,
+    libsph_checks.so, whose kernels test their cell and particle indices and
+    report SPH_EBOUNDS instead of accessing out of range."""
+    path = lib_path(checks)
+    if not force and up_to_date(checks):
+        return path
     os.makedirs(OUT, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(_compile, SOURCES))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda src: _compile(src, checks), SOURCES))
+    tmp = path + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, path)
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", path)
+    return path
 
 
 if __name__ == "__main__":

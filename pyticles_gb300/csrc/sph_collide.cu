@@ -63,8 +63,11 @@ __device__ void for_partners(const View &v, const SimDev &S, int i, F f) {
             const int y = wrap_cell(c1 + oy, S.nc[1]);
             for (int ox = -w0; ox <= w0; ++ox) {
                 const int x = wrap_cell(c0 + ox, S.nc[0]);
-                const int gc = S.cell_off + mort[(z * S.nc[1] + y) * S.nc[0] + x];
+                const int lin = (z * S.nc[1] + y) * S.nc[0] + x;
+                if (!SPH_IN_BOUNDS(lin >= 0 && lin < S.ncells, v.err_any)) continue;
+                const int gc = S.cell_off + mort[lin];
                 const int jb = v.cell_start[gc], je = v.cell_start[gc + 1];
+                if (!SPH_IN_BOUNDS(jb >= 0 && jb <= je && je <= v.np, v.err_any)) continue;
                 for (int j = jb; j < je; ++j) {
                     const int idj = v.b_id[j];
                     if (idj <= idi) continue;

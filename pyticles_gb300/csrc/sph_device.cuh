@@ -229,4 +229,17 @@ __device__ __forceinline__ void set_err(int *err, int *err_any, int s, int code)
     atomicCAS(err_any, 0, code);
 }
 
+// Index checks of the checking build (-DSPH_DEBUG_CHECKS): a failed check
+// records SPH_EBOUNDS and the caller skips the access; the release build
+// compiles them away.
+#ifdef SPH_DEBUG_CHECKS
+__device__ __forceinline__ bool sph_in_bounds(bool ok, int *err_any) {
+    if (!ok && err_any) atomicCAS(err_any, 0, SPH_EBOUNDS);
+    return ok;
+}
+#define SPH_IN_BOUNDS(cond, err_any) sph_in_bounds((cond), (err_any))
+#else
+#define SPH_IN_BOUNDS(cond, err_any) true
+#endif
+
 }  // namespace sph

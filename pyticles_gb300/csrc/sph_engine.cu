@@ -943,6 +943,7 @@ const char *sph_status_string(int status) {
         case SPH_ESKIN: return "SPH_ESKIN: displacement within a step exceeded the cell slack";
         case SPH_ECAPACITY: return "SPH_ECAPACITY: engine capacity exceeded";
         case SPH_ENOTFOUND: return "SPH_ENOTFOUND: unknown simulation id";
+        case SPH_EBOUNDS: return "SPH_EBOUNDS: an index check failed";
         default: return "unknown status";
     }
 }

@@ -127,11 +127,15 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                 int x = c0 + ox;
                 x += (x < 0) ? n0 : 0;
                 x -= (x >= n0) ? n0 : 0;
+                if (!SPH_IN_BOUNDS(row + x >= 0 && row + x < S.ncells, v.err_any)) continue;
                 const int gc = S.cell_off + mort[row + x];
+                if (!SPH_IN_BOUNDS(gc >= S.cell_off && gc < S.cell_off + S.ncells, v.err_any))
+                    continue;
                 const R ox_ = (R)ox * fr.edge[0] - pi.x;
                 const R oy_ = (R)oy * fr.edge[1] - pi.y;
                 const R oz_ = (D == 3) ? (R)oz * fr.edge[2] - pi.z : (R)0;
                 const int jb = v.cell_start[gc], je = v.cell_start[gc + 1];
+                if (!SPH_IN_BOUNDS(jb >= 0 && jb <= je && je <= v.np, v.err_any)) continue;
                 auto scan = [&](auto near, auto self) {
                     T4 pn;
                     if (PF) pn = P[jb < je ? jb : i];

@@ -32,8 +32,13 @@ __device__ __forceinline__ void bin_one(const View &v, int k) {
                 lin += ci * mul;
                 mul *= S.nc[a];
             }
-            c = S.cell_off + v.morton[S.cell_off + lin];
-            rk = atomicAdd(&v.cell_count[c], 1);
+            if (SPH_IN_BOUNDS(lin >= 0 && lin < S.ncells, v.err_any)) {
+                c = S.cell_off + v.morton[S.cell_off + lin];
+                if (SPH_IN_BOUNDS(c >= S.cell_off && c < S.cell_off + S.ncells, v.err_any))
+                    rk = atomicAdd(&v.cell_count[c], 1);
+                else
+                    c = -1;
+            }
         }
     }
     v.cell_of[k] = c;
@@ -151,7 +156,10 @@ __global__ void k_scatter(View v, int np_a) {
     if (v.rebin_gate && *v.rebin_gate == 0) return;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < np_a; k += gridDim.x * blockDim.x) {
         int c = v.cell_of[k];
-        if (c >= 0) v.order_tmp[v.cell_start[c] + v.rank[k]] = k;
+        if (c >= 0) {
+            const int dst = v.cell_start[c] + v.rank[k];
+            if (SPH_IN_BOUNDS(dst >= 0 && dst < v.np, v.err_any)) v.order_tmp[dst] = k;
+        }
     }
 }
 
