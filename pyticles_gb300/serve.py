@@ -299,6 +299,22 @@ class Server:
             "achieved_pair_interactions_per_s": work / makespan if makespan > 0 else 0.0,
         }
 
+    @staticmethod
+    def job_records(jobs):
+        """One structured record per job (JSON-ready): size, timing in server
+        seconds, latency split, pair-interactions done and the error if any."""
+        out = []
+        for j in jobs:
+            rec = {"job": j.job_id, "dim": j.dim, "n": j.n, "steps": j.steps,
+                   "arrival": j.arrival, "visible": j.visible, "admitted": j.admitted,
+                   "finished": j.finished, "pair_interactions": j.work, "error": j.error}
+            if j.finished is not None and j.visible is not None:
+                rec["latency"] = j.finished - j.visible
+            if j.admitted is not None and j.visible is not None:
+                rec["queue"] = j.admitted - j.visible
+            out.append(rec)
+        return out
+
     def close(self):
         for g in self.groups.values():
             g.close()

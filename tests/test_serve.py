@@ -152,6 +152,17 @@ def test_latency_accounting_uses_arrival_times():
     assert rep["latency_p99_s"] >= rep["latency_p50_s"] > 0
 
 
+def test_job_records_are_json_lines():
+    import json
+    srv = fake_server(1000, chunk=10)
+    jobs = [fake_job(0, 0.0, 2, 10, 10), fake_job(1, 0.5, 3, 10, 20)]
+    srv.run(jobs, realtime=False)
+    recs = [json.loads(json.dumps(r)) for r in srv.job_records(jobs)]
+    assert [r["job"] for r in recs] == [0, 1]
+    assert all(r["latency"] >= r["queue"] >= 0 and r["error"] is None for r in recs)
+    assert all(r["pair_interactions"] > 0 for r in recs)
+
+
 def test_poisson_workload_shape():
     jobs = serve.poisson_jobs(60, n_lo=1e3, n_hi=2e3, steps_lo=100, steps_hi=200, seed=9)
     arr = np.array([j.arrival for j in jobs])
