@@ -232,6 +232,7 @@ def serve_window(njobs, time_limit, seed=5000):
     offered = sum(j.n * (56.5 if j.dim == 2 else 200.0) * 2 * j.steps for j in jobs)
     srv = serve.Server(60e9, chunk=25, max_sims=256)
     rep = srv.run(jobs, realtime=True, time_limit=time_limit)
+    rep["job_records"] = srv.job_records(jobs)
     srv.close()
     rep["offered_pair_interactions_per_s"] = offered / max(rep["arrival_window_s"], 1e-9)
     rep["time_limit_s"] = time_limit
