@@ -194,11 +194,26 @@ static int grid_build(const sph_params *p, int64_t n, const double *r, grid_t *g
             g->edge[a] = 1.0;
             continue;
         }
-        int nc = (int)floor(p->box[a] / rc);
+        double q = floor(p->box[a] / rc);
+        int nc = q > 1e6 ? 1000000 : (int)q;
         if (nc < 3) nc = 1;
         g->nc[a] = nc;
-        g->edge[a] = p->box[a] / nc;
-        g->ncell *= nc;
+    }
+    /* a sparse system in a large box: coarser cells, at most 8 per particle
+     * (at least 2^16) */
+    int64_t limit = 8 * n > (1 << 16) ? 8 * n : (1 << 16);
+    for (;;) {
+        int64_t total = (int64_t)g->nc[0] * g->nc[1] * g->nc[2];
+        if (total <= limit) break;
+        int a = 0;
+        for (int b = 1; b < d; ++b)
+            if (g->nc[b] > g->nc[a]) a = b;
+        int nc = (int)(g->nc[a] * 0.9);
+        g->nc[a] = nc < 3 ? 1 : nc;
+    }
+    for (int a = 0; a < 3; ++a) {
+        g->edge[a] = a < d ? p->box[a] / g->nc[a] : 1.0;
+        g->ncell *= g->nc[a];
     }
     g->start = (int64_t *)calloc((size_t)g->ncell + 1, sizeof(int64_t));
     g->idx = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));

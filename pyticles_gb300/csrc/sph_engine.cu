@@ -231,8 +231,29 @@ void make_grid(Sim &S, int dim, double ratio) {
             S.win[a] = W;
         }
         S.nc[a] = nc;
-        S.edge[a] = S.prm.box[a] / nc;
-        S.ncells *= nc;
+    }
+    // A sparse simulation in a large box gets coarser cells: at most 8 cells
+    // per particle (at least 2^16, at most 2^24 cells), so the cell table
+    // stays proportional to the particles.  Larger cells keep the +-W window
+    // covering the reach.
+    const int64_t limit =
+        std::min<int64_t>(int64_t(1) << 24, std::max<int64_t>(int64_t(1) << 16, 8 * S.n));
+    for (;;) {
+        int64_t total = int64_t(S.nc[0]) * S.nc[1] * S.nc[2];
+        if (total <= limit) break;
+        int a = 0;
+        for (int b = 1; b < dim; ++b)
+            if (S.nc[b] > S.nc[a]) a = b;
+        int nc = std::max(1, (int)(S.nc[a] * 0.9));
+        if (nc < 2 * W + 1) {
+            nc = 1;
+            S.win[a] = 0;
+        }
+        S.nc[a] = nc;
+    }
+    for (int a = 0; a < 3; ++a) {
+        S.edge[a] = a < dim ? S.prm.box[a] / S.nc[a] : 1.0;
+        S.ncells *= S.nc[a];
     }
     // Morton order of the grid cells
     std::vector<std::pair<uint64_t, int>> codes(S.ncells);

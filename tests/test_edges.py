@@ -109,3 +109,27 @@ def test_argument_errors_are_reported():
         with pytest.raises(SphError) as ei:
             e.add(prm, r, v, m, u)                          # no simulation slot left
         assert ei.value.status == _abi.SPH_ECAPACITY
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_sparse_system_in_a_huge_box(dim):
+    """A few hundred particles in a box millions of cutoffs wide: the cell
+    table is coarsened to a multiple of the particle count and the pair set
+    and forces stay exact."""
+    L = 2.0e5 if dim == 2 else 4.0e3
+    rng = np.random.Generator(np.random.PCG64(90 + dim))
+    n = 300
+    centres = rng.uniform(0.0, L, size=(30, dim))
+    r = (centres[:, None, :] + rng.uniform(-1.5, 1.5, size=(30, 10, dim))).reshape(n, dim) % L
+    v = rng.normal(0.0, 0.5, size=(n, dim))
+    m = np.ones(n)
+    prm = make_params(dim=dim, box=[L] * dim, h_short=1.0, h_long=2.0, viscosity=True)
+    u = oracle.initial_energy(prm, r, v, m, 0.6)
+    ref = oracle.derivatives(prm, r, v, m, u)
+    with Engine(prm, "fp64", max_particles=n) as e:
+        s = e.add(prm, r, v, m, u)
+        d = e.derivatives(s)
+        e.sync()
+        assert e.pair_count(s) == ref["nip"] > 0
+    for k in ("rho", "vdot", "udot"):
+        assert rel_l2(d[k], ref[k]) < 1e-12
