@@ -436,8 +436,15 @@ def main():
     if rank == 0 and not args.no_extras:
         extras["batched"] = timed_workload(batched_workload(args.batched_sims),
                                            args.batched_steps, 3, torch, stream)
-        extras["fluid3d"] = timed_workload(fluid3d_workload(args.side3d), args.steps3d, 3,
-                                           torch, stream, rebin=args.rebin)
+        w3 = fluid3d_workload(args.side3d)
+        extras["fluid3d"] = timed_workload(w3, args.steps3d, 3, torch, stream,
+                                           rebin=args.rebin)
+        if not args.no_cpu:
+            acc3 = accuracy_track(*w3[0], args.steps3d, args.steps3d, stream)
+            extras["fluid3d"]["accuracy"] = {
+                "what": "relative L2 of the mixed-precision evaluation against the FP64 "
+                        "oracle at the GPU state after the timed steps",
+                **acc3[-1]}
         extras["serve"] = serve_window(args.serve_jobs, args.serve_seconds)
 
     accuracy = None
