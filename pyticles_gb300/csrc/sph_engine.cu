@@ -205,16 +205,19 @@ int validate_params(const sph_engine *e, const sph_params *p) {
 
 // Cell grid of one simulation.  reach = cutoff + 8 dt vmax: the cutoff plus
 // room for the largest displacement between binning and an evaluation of
-// the step (checked on the device, SPH_ESKIN).  With ratio r < 1 the cells
-// are reach/W wide (W = round(1/r)) and the pair passes scan +-W cells per
-// axis, culling cells beyond the cutoff; r >= 1 gives cells of r * reach
-// and W = 1.  An axis with fewer than 2W+1 cells becomes a single cell
-// (the passes then apply the minimum image on it).
+// the step (checked on the device, SPH_ESKIN).  Cells are r * reach wide
+// (r = tuning.cell_ratio) and the pair passes scan +-W cells per axis with
+// W = ceil(1/r) for r < 1 (1 otherwise), culling cells beyond the cutoff.
+// An axis with fewer than 2W+1 cells becomes a single cell (the passes then
+// apply the minimum image on it).
 void make_grid(Sim &S, int dim, double ratio) {
     double rc = std::sqrt(S.prm.cutoff * S.prm.cutoff + S.prm.tolerance * S.prm.tolerance);
     double reach = rc + 8.0 * S.prm.dt * S.vmax;
-    int W = ratio < 1.0 ? std::max(1, (int)std::lround(1.0 / ratio)) : 1;
-    double need = (ratio < 1.0 ? reach / W : reach * ratio) * (1.0 + 1e-9);
+    // cells of ratio x reach; the window spans the W = ceil(1/ratio) cells
+    // per side that cover the reach (1/2 -> 2, 1/3 -> 3, 0.6 -> 2 with room
+    // to spare)
+    int W = ratio < 1.0 ? std::max(1, (int)std::ceil(1.0 / ratio - 1e-9)) : 1;
+    double need = reach * ratio * (1.0 + 1e-9);
     S.ncells = 1;
     for (int a = 0; a < 3; ++a) {
         S.win[a] = 0;
