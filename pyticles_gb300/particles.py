@@ -23,6 +23,7 @@ import numpy as np
 
 from . import _abi
 from .box import MirrorBox, PeriodicBox
+from .neighbour_list import SortedVerletList
 from .engine import Engine
 from .forces import (CohesiveSpamForce, CollisionForce, CollisionForce3d, SpamComplete,
                      SpamConduction, SpamForce)
@@ -189,6 +190,12 @@ class SmoothParticleSystem(ParticleSystem):
             raise NotImplementedError("a collision force must come after the SPH forces")
         if self.dim == 3 and f.dims == 2:
             raise NotImplementedError("CollisionForce (x/y only) in a 3D engine step")
+        if isinstance(f.nl, SortedVerletList):
+            # the engine applies collisions in VerletList's (i, j) order; the
+            # reference's sort_by_r permutes rij twice (neighbour_list.py:276-278),
+            # so its sorted-list collision order has no consistent meaning
+            raise NotImplementedError("collision forces over a SortedVerletList in the engine "
+                                      "step; apply() them over the list instead")
         fc, ft = f.nl._cutoff_tol()
         if f.cutoff ** 2 > min(cutoff * cutoff + tol * tol, fc * fc + ft * ft):
             raise NotImplementedError("collision range beyond the neighbour list's pairs")

@@ -258,3 +258,13 @@ def test_collision_capacity_overflow_is_reported(built):
             e.sync()
         assert ei.value.status == _abi.SPH_ECAPACITY
         assert e.status(s) == _abi.SPH_ECAPACITY
+
+
+def test_collision_over_sorted_list_is_refused_in_the_step():
+    from pyticles_gb300 import SortedVerletList
+    g = load("collide2d_144")
+    p = api_system(g, None)
+    snl = SortedVerletList(p, cutoff=float(g["cutoff"]), tolerance=0.0)
+    p.forces.append(CollisionForce(p, snl, cutoff=0.9))
+    with pytest.raises(NotImplementedError):
+        p.engine_params(1e-3)
