@@ -50,8 +50,10 @@ enum sph_status {
                                 cell slack allows (cell list would miss pairs)   */
     SPH_ECAPACITY = 8,       /* engine particle / simulation capacity exceeded  */
     SPH_ENOTFOUND = 9,       /* unknown simulation id                           */
-    SPH_EBOUNDS = 10         /* an index check of a checking build failed (the
-                                access was skipped; release builds do not check) */
+    SPH_EBOUNDS = 10         /* an index check failed and the access was
+                                skipped: the checking build's checks, and in
+                                every build the cluster pair lists' agreement
+                                between counting and writing                 */
 };
 
 /* Kernel ids follow spkernel.ktable (spkernel.py:20): 1 gaussian, 2 lucy,
@@ -202,6 +204,17 @@ typedef struct sph_tuning {
                                  and a 5^d window, 1/3 -> 7^d (down to 1/5);
                                  cells beyond the cutoff from a particle are
                                  skipped                                       */
+    int32_t pair_scheme;      /* 0: cell windows, a particle per lane.
+                                 1: cluster pairs -- clusters of 8 compact
+                                 particles against listed clusters of 4, 8 x 4
+                                 pairs per warp step.  Applies to an engine
+                                 holding one 3D simulation in mixed precision
+                                 without collisions, whose box spans at least
+                                 five columns of about 8 particles per axis;
+                                 otherwise the cell scheme runs.  Lists are
+                                 built every step; same pair set, rounding
+                                 differs from scheme 0                        */
+    int32_t reserved;         /* 0 */
 } sph_tuning;
 int sph_get_tuning(sph_engine *e, sph_tuning *t);
 int sph_set_tuning(sph_engine *e, const sph_tuning *t);

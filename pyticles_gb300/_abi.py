@@ -89,6 +89,8 @@ class SphTuning(ctypes.Structure):
         ("steps_per_graph", ctypes.c_int32),
         ("rebin", ctypes.c_int32),
         ("cell_ratio", ctypes.c_double),
+        ("pair_scheme", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

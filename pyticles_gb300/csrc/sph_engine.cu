@@ -120,6 +120,9 @@ struct sph_engine {
     bool bins_valid = false;       // B, its packed copies and the cells match A
     bool one_sim = false;          // exactly one live simulation (one_dev)
     SimDev one_dev;
+    ClusterSet cl = {};            // tuning.pair_scheme = 1 (sph_cluster.cu)
+    int64_t cl_np = 0, cl_fine = 0, cl_col = 0, cl_ncl = 0;  // allocated sizes
+    long long cl_ent = 0;
 
     // profiling: event pairs recorded around each pass
     bool prof_on = false;
@@ -391,6 +394,121 @@ void free_graph(sph_engine *e) {
     e->graph_steps = 0;
 }
 
+void cluster_free(sph_engine *e) {
+    ClusterSet &c = e->cl;
+    void *ptrs[] = {c.fcount, c.fstart, c.fkey,  c.frank, c.ford,   c.scan_tmp, c.colcnt,
+                    c.colcl,  c.slot_idx, c.slot_of, c.cref, c.ibox, c.jbox,    c.lnear,
+                    c.lfar,   c.ent,    c.cpos,  c.cfv,   c.cf,     c.cq,       c.crho};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    c = ClusterSet{};
+    e->cl_np = e->cl_fine = e->cl_col = e->cl_ncl = 0;
+    e->cl_ent = 0;
+}
+
+// Cluster geometry of the engine's single 3D simulation (tuning.pair_scheme
+// = 1): columns about 8 particles wide (the cube root of the volume of 8 at
+// the mean density), slabs a quarter of that, the column reach of the cutoff
+// plus twice the allowed drift, and the buffers.  Leaves c.on = 0 (the cell
+// scheme runs) where the scheme does not apply.
+int cluster_setup(sph_engine *e) {
+    ClusterSet &c = e->cl;
+    c.on = 0;
+    if (e->tune.pair_scheme != 1 || !e->one_sim || e->dim != 3 || e->precision != SPH_MIXED ||
+        e->group.collision != SPH_COLLIDE_OFF || e->np_b < 8)
+        return SPH_OK;
+    int sid = -1;
+    for (int s = 0; s < (int)e->sims.size(); ++s)
+        if (e->sims[s].active) sid = s;
+    const Sim &S = e->sims[sid];
+    const SimDev &d = e->one_dev;
+    const double *L = S.prm.box;
+    const double vol = L[0] * L[1] * L[2];
+    const double wt = std::cbrt(8.0 * vol / (double)S.n);
+    const int ncx = std::max(1, (int)std::floor(L[0] / wt));
+    const int ncy = std::max(1, (int)std::floor(L[1] / wt));
+    const int nslab = std::max(1, (int)std::floor(L[2] / (0.25 * wt)));
+    const double wx = L[0] / ncx, wy = L[1] / ncy, gz = L[2] / nslab;
+    const double rc = std::sqrt(d.thr);
+    double drift[3];
+    for (int a = 0; a < 3; ++a) {
+        drift[a] = 2.0 * d.slack_half[a];
+        if (!(drift[a] < 0.25 * L[a])) return SPH_OK;   // single-cell axis or no slack room
+    }
+    // a column dx over lies at least (|dx| - 1) widths away
+    const int rx = (int)std::ceil((rc + drift[0] + 1e-3) / wx);
+    const int ry = (int)std::ceil((rc + drift[1] + 1e-3) / wy);
+    // every column and every z image within reach must be distinct
+    if (2 * rx + 1 > ncx || 2 * ry + 1 > ncy || rx > 100 || ry > 100) return SPH_OK;
+    if (L[2] < 2.0 * (rc + drift[2]) + 4.0 * gz || nslab > 30000) return SPH_OK;
+    const int64_t nfine = (int64_t)ncx * ncy * nslab;
+    if (nfine > std::max<int64_t>(int64_t(1) << 16, 16 * S.n) || nfine > (int64_t(1) << 30))
+        return SPH_OK;
+    const int64_t ncol = (int64_t)ncx * ncy;
+    const int64_t ncl_max = S.n / 8 + ncol + 1;
+    if (8 * ncl_max > (int64_t(1) << 30)) return SPH_OK;
+    // list capacity: the j-halves in the box of an i-cluster grown by the reach
+    const double rho_n = (double)S.n / vol;
+    const double R = rc + std::max(drift[0], std::max(drift[1], drift[2]));
+    const double hz = 8.0 / (rho_n * wx * wy) + gz;
+    const double box = (2 * wx + 2 * R) * (2 * wy + 2 * R) * (2 * hz + 2 * R);
+    // (2.6 times the mean list length of a uniform fluid)
+    const int per = (int)std::min(65536.0, std::max(64.0, std::ceil(rho_n * box / 4.0)));
+    const long long cap = (long long)per * ncl_max;
+    if (S.n > e->cl_np || nfine > e->cl_fine || ncol > e->cl_col || ncl_max > e->cl_ncl ||
+        cap > e->cl_ent || (long long)e->cl_ent < (long long)per * e->cl_ncl) {
+        cluster_free(e);
+        const int64_t np = std::max<int64_t>(S.n, 1);
+        const int64_t scan = std::max(nfine, ncol) / 4096 + 2;
+        TRY(dalloc(&c.fcount, nfine));
+        TRY(dalloc(&c.fstart, nfine + 1));
+        TRY(dalloc(&c.fkey, np));
+        TRY(dalloc(&c.frank, np));
+        TRY(dalloc(&c.ford, np));
+        TRY(dalloc(&c.scan_tmp, scan));
+        TRY(dalloc(&c.colcnt, ncol));
+        TRY(dalloc(&c.colcl, ncol + 1));
+        TRY(dalloc(&c.slot_idx, 8 * ncl_max));
+        TRY(dalloc(&c.slot_of, np));
+        TRY(dalloc(&c.cref, ncl_max));
+        TRY(dalloc(&c.ibox, 2 * ncl_max));
+        TRY(dalloc(&c.jbox, 4 * ncl_max));
+        TRY(dalloc(&c.lnear, ncl_max));
+        TRY(dalloc(&c.lfar, ncl_max));
+        TRY(dalloc(&c.ent, cap));
+        TRY(dalloc(&c.cpos, 8 * ncl_max));
+        TRY(dalloc(&c.cfv, 8 * ncl_max));
+        TRY(dalloc(&c.cf, 8 * ncl_max));
+        TRY(dalloc(&c.cq, 8 * ncl_max));
+        TRY(dalloc(&c.crho, 8 * ncl_max));
+        e->cl_np = np;
+        e->cl_fine = nfine;
+        e->cl_col = ncol;
+        e->cl_ncl = ncl_max;
+        e->cl_ent = cap;
+    }
+    c.sim = sid;
+    c.ncx = ncx;
+    c.ncy = ncy;
+    c.nslab = nslab;
+    c.ncol = (int)ncol;
+    c.nfine = (int)nfine;
+    c.rx = rx;
+    c.ry = ry;
+    c.wxd = wx;
+    c.wyd = wy;
+    c.gzd = gz;
+    c.wx = (float)wx;
+    c.wy = (float)wy;
+    c.gz = (float)gz;
+    for (int a = 0; a < 3; ++a) c.drift2[a] = (float)drift[a];
+    c.ncl_max = (int)ncl_max;
+    c.slots_max = (int)(8 * ncl_max);
+    c.lstride = per;
+    c.on = 1;
+    return SPH_OK;
+}
+
 int alloc_cells(sph_engine *e, int64_t cells) {
     if (cells <= e->cap_c) return SPH_OK;
     int64_t c = std::max<int64_t>(cells, e->cap_c * 2);
@@ -569,6 +687,7 @@ int relayout(sph_engine *e) {
         if (e->sims[s].active) ++live, last = s;
     e->one_sim = live == 1;
     if (e->one_sim) e->one_dev = sd[last];
+    TRY(cluster_setup(e));
     CK(cudaStreamSynchronize(st));
     free_graph(e);
     e->layout_dirty = false;
@@ -652,6 +771,35 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
         v.reuse = 1;
         v.rebin_gate = e->rebin_gate;
     }
+    if (e->cl.on) {
+        // cluster pairs: build at the step's first evaluation, repack at the
+        // later ones; the rates pass leaves the stage update to k_integrate
+        const ClusterSet &c = e->cl;
+        const int kern = e->group.kernel;
+        if (s == 0) {
+            ProfScope ps(e, SPH_PASS_SORT, st);
+            launch_cluster_build(v, c, st);
+        }
+        {
+            ProfScope ps(e, SPH_PASS_DENSITY, st);
+            if (s > 0) launch_cluster_pack(v, c, s, st);
+            launch_cluster_density(v, c, kern, s, st);
+        }
+        if (e->group.heat_flux) {
+            ProfScope ps(e, SPH_PASS_HEAT, st);
+            launch_cluster_heat(v, c, kern, st);
+        }
+        if (mode == 1 && s == e->nstage - 1 && e->any_thermostat) {
+            ProfScope ps(e, SPH_PASS_TSUM, st);
+            launch_tsum(v, e->precision, (int)e->sims.size(), st);
+        }
+        {
+            ProfScope ps(e, SPH_PASS_FORCE, st);
+            launch_cluster_force(v, c, kern, e->group.viscosity, e->group.heat_flux, st);
+            if (mode == 1) launch_integrate(v, e->precision, e->group.integrator, s, st);
+        }
+        return;
+    }
     int blk = e->tune.block_size;
     const bool coll = mode == 1 && e->group.collision != SPH_COLLIDE_OFF;
     if (coll && s == 0) {
@@ -689,6 +837,15 @@ void enqueue_step(sph_engine *e, cudaStream_t st) {
 }
 
 int64_t kernels_per_step(const sph_engine *e) {
+    if (e->cl.on) {
+        // cluster build; per evaluation density, [heat,] force and the stage
+        // update; the later evaluations' repacking
+        int64_t k = kSortKernels + cluster_build_kernels();
+        k += (int64_t)e->nstage * (3 + (e->group.heat_flux ? 1 : 0)) + (e->nstage - 1);
+        if (e->any_thermostat) k += 2;
+        if (rebin_on_demand(e)) k += 2;
+        return k;
+    }
     int64_t k = kSortKernels;
     k += (int64_t)e->nstage * (2 + (e->group.heat_flux ? 1 : 0));
     if (e->any_thermostat) k += 2;
@@ -919,6 +1076,7 @@ void free_all(sph_engine *e) {
                   c.touch_start, c.touch_fill, c.touch, c.pred, c.level, c.info};
     for (void *p : cp)
         if (p) cudaFree(p);
+    cluster_free(e);
     for (int a = 0; a < 3; ++a) {
         void *pa[] = {e->org[a], e->a_pos[a], e->a_vel[a], e->b_pos[a], e->b_vel[a], e->xe[0][a],
                       e->xe[1][a], e->ve[a], e->q[a], e->vdot[a], e->f0v[a], e->acc_r[a],
@@ -1001,6 +1159,8 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->tune.cell_ratio = 0.5;
     e->tune.use_graph = 1;
     e->tune.steps_per_graph = 1;
+    e->tune.pair_scheme = 0;
+    e->tune.reserved = 0;
     if (stream) {
         e->stream = (cudaStream_t)stream;
     } else {
@@ -1396,10 +1556,12 @@ int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
     if (!e || !t) return SPH_EINVAL;
     if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) ||
         !(t->cell_ratio >= 0.2 && t->cell_ratio <= 4.0) || (t->rebin != 0 && t->rebin != 1) ||
-        t->steps_per_graph < 1)
+        t->steps_per_graph < 1 || (t->pair_scheme != 0 && t->pair_scheme != 1))
         return SPH_EINVAL;
     bool regrid = t->cell_ratio != e->tune.cell_ratio;
+    if (t->pair_scheme != e->tune.pair_scheme) e->layout_dirty = true;
     e->tune = *t;
+    e->tune.reserved = 0;
     free_graph(e);
     if (regrid) {
         for (auto &S : e->sims)

@@ -151,6 +151,54 @@ struct CollideSet {
     int *info;                      // [4]: count, overflow, max level, solver status
 };
 
+// Cluster-pair scheme (tuning.pair_scheme = 1, sph_cluster.cu): one
+// simulation's particles are binned into columns (x, y) of about eight
+// particles' width and thin z slabs, ordered by slab within a column and cut
+// into clusters of 8 consecutive particles (padded slots at a column's end).
+// Each cluster keeps its positions relative to a lattice point of its own
+// (column centre, slab floor), so a cluster pair's shift is an integer
+// lattice offset.  A list per i-cluster (8 particles) names the j-clusters
+// (halves of 4) whose bounding boxes lie within the cutoff plus the allowed
+// drift; a warp evaluates 8 i x 4 j pairs per list entry.  Lists live in
+// fixed regions of lstride entries, built in one pass.
+struct ClusterSet {
+    int on;                       // the scheme runs for this layout
+    int sim;                      // the simulation's slot
+    int ncx, ncy, nslab, ncol, nfine;
+    int rx, ry;                   // +-columns searched per axis
+    float wx, wy, gz;             // lattice steps
+    double wxd, wyd, gzd;
+    float drift2[3];              // twice the allowed drift per axis (list margin)
+    int ncl_max, slots_max;
+    int lstride;                  // list entries reserved per i-cluster
+    int *fcount, *fstart, *fkey, *frank, *ford, *scan_tmp;
+    int *colcnt, *colcl;          // [ncol + 1]: clusters per column, prefix
+    int *slot_idx, *slot_of;      // slot -> sorted index (-1 padding), inverse
+    int4 *cref;                   // per cluster {kx, ky, kz, column}
+    float4 *ibox, *jbox;          // bounding boxes (lo, hi) of clusters / halves
+    int *lnear, *lfar;            // [ncl_max] entries within / beyond the short
+                                  // support: the near ones from the front of the
+                                  // i-cluster's lstride slots, the far ones from
+                                  // the back
+    int2 *ent;                    // {j half | near << 31, lattice offset dx|dy<<8|dz<<16}
+    float4 *cpos, *cfv, *cf, *cq; // per slot: {x, y, z, m} local, {v, p/rho^2},
+                                  // {p/rho^2, rho, T_hi, T_lo}, {q/rho^2, 0}
+    float *crho;
+};
+
+// ---- launch wrappers (sph_cluster.cu) ----
+// Cluster build of the step (stage-0 positions) and its pair lists.
+void launch_cluster_build(const View &v, const ClusterSet &c, cudaStream_t s);
+// Cluster-local packed positions of evaluation `stage` (stage > 0 also
+// checks each particle's drift since the build).
+void launch_cluster_pack(const View &v, const ClusterSet &c, int stage, cudaStream_t s);
+void launch_cluster_density(const View &v, const ClusterSet &c, int kernel, int stage,
+                            cudaStream_t s);
+void launch_cluster_heat(const View &v, const ClusterSet &c, int kernel, cudaStream_t s);
+void launch_cluster_force(const View &v, const ClusterSet &c, int kernel, int viscosity, int heat,
+                          cudaStream_t s);
+int cluster_build_kernels();
+
 // ---- launch wrappers (sph_collide.cu) ----
 // Engine path: candidates of every simulation with collisions on, found
 // with the cell list at the evaluation positions v.xe_in.

@@ -199,17 +199,20 @@ class Engine:
         check(self._lib.sph_get_tuning(self._h, ctypes.byref(t)), "sph_get_tuning")
         return {"block_size": t.block_size, "use_graph": t.use_graph,
                 "steps_per_graph": t.steps_per_graph, "rebin": t.rebin,
-                "cell_ratio": t.cell_ratio}
+                "cell_ratio": t.cell_ratio, "pair_scheme": t.pair_scheme}
 
     def set_tuning(self, **kw):
-        """block_size, use_graph, steps_per_graph, cell_ratio, and rebin (1:
-        bin into cells only when a particle has used half of the cell slack,
-        VerletList.ponder_rebuild's skin reuse; 0: every step)."""
+        """block_size, use_graph, steps_per_graph, cell_ratio, rebin (1: bin
+        into cells only when a particle has used half of the cell slack,
+        VerletList.ponder_rebuild's skin reuse; 0: every step) and
+        pair_scheme (0: cell windows; 1: cluster pairs, for one 3D
+        simulation in mixed precision without collisions)."""
         cur = self.tuning
         cur.update(kw)
         t = SphTuning(block_size=int(cur["block_size"]), use_graph=int(cur["use_graph"]),
                       steps_per_graph=int(cur["steps_per_graph"]), rebin=int(cur["rebin"]),
-                      cell_ratio=float(cur["cell_ratio"]))
+                      cell_ratio=float(cur["cell_ratio"]),
+                      pair_scheme=int(cur["pair_scheme"]))
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), "sph_set_tuning")
 
     def rebin_count(self):

@@ -2,6 +2,7 @@
 
     python -m pyticles_gb300.profile_case --case 2d --side 1024 --steps 2
     python -m pyticles_gb300.profile_case --case 3d --side 64 --steps 2
+    python -m pyticles_gb300.profile_case --case 3d --side 64 --steps 2 --pair-scheme 1
 
 Each step launches the sort kernels, then per integrator stage k_density,
 [k_heat,] k_force; with --steps 2 and one warm-up step the second step's
@@ -20,6 +21,7 @@ def main():
     ap.add_argument("--side", type=int, default=1024)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--precision", default="mixed")
+    ap.add_argument("--pair-scheme", type=int, default=0, choices=[0, 1])
     args = ap.parse_args()
     build.build()
     if args.case == "2d":
@@ -30,7 +32,7 @@ def main():
         u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
     with Engine(prm, args.precision, max_particles=len(r)) as e:
         e.add(prm, r, v, m, u)
-        e.set_tuning(use_graph=0)
+        e.set_tuning(use_graph=0, pair_scheme=args.pair_scheme)
         e.advance(args.steps)
         e.sync()
         print(f"{args.case} n={len(r)} steps={args.steps} pairs/eval={e.last_pair_total()} "

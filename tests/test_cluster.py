@@ -1,0 +1,205 @@
+"""The cluster-pair scheme (tuning pair_scheme = 1): one 3D simulation in
+mixed precision, its pairs evaluated as 8 x 4 blocks of compact particle
+clusters from box-culled lists.  The pair set is the reference's exact set
+(neighbour_list.py:168-178), the results meet the mixed-precision bounds
+against the FP64 oracle like the cell-window scheme, runs are deterministic,
+and the cell scheme runs wherever the cluster scheme does not apply."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from pyticles_gb300 import Engine, SphError, build, workloads
+from pyticles_gb300._abi import SPH_ESKIN
+from tests.golden_cases import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-6
+JQ_TOL = 5e-6          # jq sums T_j - T_i: the pressure-only bound of the cell scheme's tests
+# Debrun's gradient factor (h - r)^2 / r weighs the closest pairs most: on the
+# Debrun system below the cell scheme shows 1.3e-6 (vdot, udot), this one 1.0e-6
+DEBRUN_TOL = 2e-6
+KEYS = ("rho", "rho_lr", "t", "p", "vdot", "udot")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    build.build()
+
+
+def with_gradient(prm, r, v, m, T0):
+    """Initial u with T = T0 (1 + 0.2 sin(2 pi x / L)) so the heat flux is real."""
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    return u + prm.kbdash * 0.2 * T0 * np.sin(2 * np.pi * r[:, 0] / prm.box[0])
+
+
+def case(name):
+    if name == "cubic_heat_8000":
+        prm, r, v, m, T0 = workloads.config_3d(20, 3100)
+    elif name == "lucy_heat_4096":
+        prm, r, v, m, T0 = workloads.config_3d(16, 3101, kernel="lucy", h_short=1.4, h_long=2.5)
+    elif name == "gauss_4096":
+        prm, r, v, m, T0 = workloads.config_3d(16, 3102, kernel="gaussian", h_short=0.9,
+                                               h_long=1.4, cutoff=3.0, heat_flux=False)
+    elif name == "debrun_rk4_4096":
+        prm, r, v, m, T0 = workloads.config_3d(16, 3103, kernel="debrun", h_short=1.4,
+                                               h_long=2.5, integrator="rk4")
+    else:
+        raise KeyError(name)
+    return prm, r, v, m, with_gradient(prm, r, v, m, T0)
+
+
+def engine(prm, r, v, m, u, scheme, precision="mixed", cap=1, **tune):
+    e = Engine(prm, precision, max_particles=cap * len(r), max_sims=2)
+    s = e.add(prm, r, v, m, u)
+    e.set_tuning(pair_scheme=scheme, **tune)
+    return e, s
+
+
+CASES = ["cubic_heat_8000", "lucy_heat_4096", "gauss_4096", "debrun_rk4_4096"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_cluster_scheme_matches_oracle(name):
+    prm, r, v, m, u = case(name)
+    ref = oracle.derivatives(prm, r, v, m, u)
+    e, s = engine(prm, r, v, m, u, 1)
+    with e:
+        d = e.derivatives(s)
+        e.sync()
+        keys = KEYS + (("jq",) if prm.heat_flux else ())
+        errs = {k: rel_l2(d[k], ref[k]) for k in keys}
+        print(name, errs)
+        tol = DEBRUN_TOL if name.startswith("debrun") else MIXED_TOL
+        for k, err in errs.items():
+            assert err < (JQ_TOL if k == "jq" else tol), (k, err)
+        assert e.last_pair_total() == ref["nip"]
+        e.advance(5)
+        e.sync()
+        rr, vv, uu = e.get_state(s)
+    r5, v5, u5, _ = oracle.advance(prm, r, v, m, u, 5)
+    assert rel_l2(rr, r5) < tol
+    assert rel_l2(vv, v5) < tol
+    assert rel_l2(uu, u5) < tol
+
+
+@pytest.mark.parametrize("integ", ["euler", "ieuler", "rk4"])
+def test_cluster_scheme_agrees_with_cell_scheme(integ):
+    """Same pair set (pair counts equal) and trajectories equal to rounding
+    over 12 steps, in graphs of 4."""
+    prm, r, v, m, T0 = workloads.config_3d(20, 3110, integrator=integ)
+    u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
+    out = {}
+    for scheme in (0, 1):
+        e, s = engine(prm, r, v, m, u, scheme, steps_per_graph=4)
+        with e:
+            d = e.derivatives(s)
+            e.sync()
+            pairs = e.last_pair_total()
+            ks = e.kernels_per_step()
+            e.advance(12)
+            e.sync()
+            out[scheme] = (d, pairs, ks, e.get_state(s))
+    (d0, p0, k0, st0), (d1, p1, k1, st1) = out[0], out[1]
+    assert p0 == p1
+    assert k1 != k0                   # the cluster passes ran
+    for k in ("rho", "vdot", "udot", "jq"):
+        assert rel_l2(d1[k], d0[k]) < (JQ_TOL if k == "jq" else MIXED_TOL), k
+    for a, b in zip(st1, st0):
+        assert rel_l2(a, b) < MIXED_TOL
+
+
+def test_cluster_scheme_is_deterministic():
+    """Lists and sums follow the state only: eager steps, graphs of 5 and a
+    second engine give the same bits."""
+    prm, r, v, m, u = case("cubic_heat_8000")
+    states = []
+    for per, graph in ((5, 1), (1, 0), (5, 1)):
+        e, s = engine(prm, r, v, m, u, 1, steps_per_graph=per, use_graph=graph)
+        with e:
+            e.advance(10)
+            e.sync()
+            states.append(e.get_state(s))
+    for st in states[1:]:
+        for a, b in zip(st, states[0]):
+            assert np.array_equal(a, b)
+
+
+def test_cluster_scheme_with_binning_on_demand_and_thermostat():
+    prm, r, v, m, T0 = workloads.config_3d(20, 3120, integrator="rk4", dt=2e-3)
+    prm.thermostat = 1
+    prm.thermostat_temp = 0.6
+    prm.thermostat_temp_end = 0.3
+    prm.thermostat_ramp_steps = 10
+    u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
+    e, s = engine(prm, r, v, m, u, 1, rebin=1, steps_per_graph=4)
+    with e:
+        e.advance(12)
+        e.sync()
+        rr, vv, uu = e.get_state(s)
+    ro, vo, uo, _ = oracle.advance(prm, r, v, m, u, 12)
+    assert rel_l2(rr, ro) < MIXED_TOL
+    assert rel_l2(vv, vo) < MIXED_TOL
+    assert rel_l2(uu, uo) < MIXED_TOL
+
+
+@pytest.mark.parametrize("what", ["2d", "fp64", "two_sims", "small_box"])
+def test_cell_scheme_runs_where_clusters_do_not_apply(what):
+    """pair_scheme = 1 leaves a 2D engine, an FP64 engine, an engine with two
+    simulations and a box narrower than five columns on the cell scheme: the
+    same launches and the same bits as pair_scheme = 0."""
+    precision = "mixed"
+    if what == "2d":
+        prm, r, v, m, T0 = workloads.config_2d(48, 3130)
+    elif what == "small_box":
+        prm, r, v, m, T0 = workloads.config_3d(12, 3131)
+    else:
+        prm, r, v, m, T0 = workloads.config_3d(20, 3132)
+        precision = "fp64" if what == "fp64" else "mixed"
+    u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
+    res = []
+    for scheme in (0, 1):
+        e, s = engine(prm, r, v, m, u, scheme, precision=precision, cap=2)
+        with e:
+            if what == "two_sims":
+                e.add(prm, r, v, m, u)
+            e.advance(3)
+            e.sync()
+            res.append((e.kernels_per_step(), e.get_state(s)))
+    assert res[0][0] == res[1][0]
+    for a, b in zip(res[0][1], res[1][1]):
+        assert np.array_equal(a, b)
+
+
+def test_cluster_scheme_flags_a_skin_violation():
+    """A particle that outruns the allowed drift within a step raises
+    SPH_ESKIN: the lists were culled with that drift as margin."""
+    prm, r, v, m, u = case("cubic_heat_8000")
+    e, s = engine(prm, r, v, m, u, 1)
+    with e:
+        v2 = v.copy()
+        v2[7] = [5000.0, 0.0, 0.0]
+        e.set_state(s, r, v2, m, u)
+        e.advance(1)
+        with pytest.raises(SphError) as ei:
+            e.sync()
+        assert ei.value.status == SPH_ESKIN
+
+
+def test_cluster_scheme_full_size_invariants():
+    """N = 110,592 (48^3): the pair count equals the oracle's, forces cancel
+    pairwise and momentum is conserved over 5 steps."""
+    prm, r, v, m, T0 = workloads.config_3d(48, 3140)
+    u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
+    n_ref = len(oracle.pairs(prm, r)[0])
+    e, s = engine(prm, r, v, m, u, 1)
+    with e:
+        d = e.derivatives(s)
+        assert e.last_pair_total() == n_ref
+        net = np.abs(d["vdot"].sum(axis=0)) / np.abs(d["vdot"]).sum(axis=0)
+        assert np.all(net < 1e-6), net
+        p0 = np.array(e.diagnostics(s)["momentum"])
+        e.advance(5)
+        e.sync()
+        p1 = np.array(e.diagnostics(s)["momentum"])
+    assert np.all(np.abs(p1 - p0) / np.abs(v).sum() < 1e-7), (p0, p1)
