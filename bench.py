@@ -267,7 +267,7 @@ def run_e2e(prm, r, v, m, u, steps, torch, stream):
     return wall, pairs, n * (2 * d + 2) * 8, n * (2 * d + 1) * 8
 
 
-def accuracy_track(prm, r, v, m, u, steps, every, stream):
+def accuracy_track(prm, r, v, m, u, steps, every, stream, knobs=None):
     """Mixed-precision accuracy along the benchmarked trajectory: every
     `every` steps the GPU evaluates f(x) at its current state and the FP64
     oracle re-evaluates it at the same state; relative L2 of rho, vdot and
@@ -277,7 +277,7 @@ def accuracy_track(prm, r, v, m, u, steps, every, stream):
     out = []
     with Engine(prm, "mixed", max_particles=len(r), stream=stream.cuda_stream) as e:
         s = e.add(prm, r, v, m, u)
-        e.set_tuning(rebin=1, steps_per_graph=every)
+        e.set_tuning(**dict(knobs or {}, rebin=1, steps_per_graph=every))
         done = 0
         while done < steps:
             e.advance(every)
@@ -440,7 +440,8 @@ def main():
         extras["fluid3d"] = timed_workload(w3, args.steps3d, 3, torch, stream,
                                            rebin=args.rebin)
         if not args.no_cpu:
-            acc3 = accuracy_track(*w3[0], args.steps3d, args.steps3d, stream)
+            acc3 = accuracy_track(*w3[0], args.steps3d, args.steps3d, stream,
+                                  knobs=extras["fluid3d"]["tuning"])
             extras["fluid3d"]["accuracy"] = {
                 "what": "relative L2 of the mixed-precision evaluation against the FP64 "
                         "oracle at the GPU state after the timed steps",

@@ -1,8 +1,10 @@
 """Autotuner for the engine's launch and grid knobs.
 
-Knobs (struct sph_tuning): threads per block of the pair passes and the
+Knobs (struct sph_tuning): threads per block of the pair passes, the
 cell-edge / cutoff ratio (1 -> cells of the cutoff and a 3^d window, 1/2 ->
-5^d, 1/3 -> 7^d, cells beyond the cutoff culled per particle).  A candidate is
+5^d, 1/3 -> 7^d, cells beyond the cutoff culled per particle) and, for a
+single 3D simulation in mixed precision, the pair scheme (cell windows or
+cluster pairs; the cluster scheme has its own fixed launch shape).  A candidate is
 timed with CUDA events over a few graph-captured steps on a clone of the
 simulations (same parameters, same current states), so tuning neither
 advances the live simulations nor shifts their thermostat schedules.  Results
@@ -27,14 +29,22 @@ def signature(group, precision, counts):
             precision, int(round(math.log2(max(total, 1)))), len(counts) > 1)
 
 
-def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream):
+def cluster_candidate(group, precision, sims):
+    """Whether the cluster-pair scheme can apply: one 3D simulation in mixed
+    precision without collisions (the engine itself checks the box)."""
+    return (group.dim == 3 and precision == "mixed" and len(sims) == 1
+            and group.collision == 0)
+
+
+def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream, scheme=0):
     import torch
     total = sum(len(s[1]) for s in sims)
     with Engine(group, precision, max_particles=total, max_sims=len(sims),
                 stream=stream.cuda_stream) as e:
         for prm, r, v, m, u in sims:
             e.add(prm, r, v, m, u)
-        e.set_tuning(block_size=block, cell_ratio=ratio, steps_per_graph=steps, use_graph=1)
+        e.set_tuning(block_size=block, cell_ratio=ratio, steps_per_graph=steps, use_graph=1,
+                     pair_scheme=scheme)
         e.advance(warmup)
         e.prepare()
         e.sync()
@@ -50,8 +60,9 @@ def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream):
 
 def tune(group, precision, sims, steps=4, warmup=2, blocks=BLOCKS, ratios=RATIOS,
          use_cache=True):
-    """Times every (block, ratio) candidate on the given simulations
-    [(params, r, v, m, u), ...] and returns (best_knobs, table)."""
+    """Times every (block, ratio) candidate of the cell scheme, and the
+    cluster scheme where it can apply, on the given simulations
+    [(params, r, v, m, u), ...]; returns (best_knobs, table)."""
     import torch
     key = signature(group, precision, [len(s[1]) for s in sims])
     if use_cache and key in _cache:
@@ -61,9 +72,14 @@ def tune(group, precision, sims, steps=4, warmup=2, blocks=BLOCKS, ratios=RATIOS
     for ratio in ratios:
         for block in blocks:
             ms = time_candidate(group, precision, sims, block, ratio, steps, warmup, stream)
-            table.append({"block_size": block, "cell_ratio": ratio, "ms_per_step": ms})
+            table.append({"block_size": block, "cell_ratio": ratio, "pair_scheme": 0,
+                          "ms_per_step": ms})
+    if cluster_candidate(group, precision, sims):
+        ms = time_candidate(group, precision, sims, 128, 0.5, steps, warmup, stream, scheme=1)
+        table.append({"block_size": 128, "cell_ratio": 0.5, "pair_scheme": 1, "ms_per_step": ms})
     best = min(table, key=lambda row: row["ms_per_step"])
-    knobs = {"block_size": best["block_size"], "cell_ratio": best["cell_ratio"]}
+    knobs = {"block_size": best["block_size"], "cell_ratio": best["cell_ratio"],
+             "pair_scheme": best["pair_scheme"]}
     _cache[key] = (knobs, table)
     return knobs, table
 

@@ -203,3 +203,16 @@ def test_cluster_scheme_full_size_invariants():
         e.sync()
         p1 = np.array(e.diagnostics(s)["momentum"])
     assert np.all(np.abs(p1 - p0) / np.abs(v).sum() < 1e-7), (p0, p1)
+
+
+def test_autotuner_times_the_cluster_scheme_for_one_3d_simulation():
+    from pyticles_gb300 import autotune
+    prm, r, v, m, T0 = workloads.config_3d(20, 3150)
+    u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
+    knobs, table = autotune.tune(prm, "mixed", [(prm, r, v, m, u)], steps=2, warmup=1,
+                                 blocks=(128,), ratios=(0.5,), use_cache=False)
+    assert [row["pair_scheme"] for row in table] == [0, 1]
+    assert knobs["pair_scheme"] in (0, 1)
+    _, table2 = autotune.tune(prm, "fp64", [(prm, r, v, m, u)], steps=2, warmup=1,
+                              blocks=(128,), ratios=(0.5,), use_cache=False)
+    assert [row["pair_scheme"] for row in table2] == [0]
