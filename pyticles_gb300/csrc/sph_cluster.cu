@@ -40,7 +40,7 @@ namespace sph {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr float kFar = 1.0e4f;     // padding slots: never within any cutoff
+constexpr float kFar = 1.0e18f;    // padding slots: beyond any cutoff and lattice shift
 constexpr float kEmpty = 1.0e30f;  // box of an empty half: lo > hi
 
 int nblocks(long long n, int block) { return (int)std::max<long long>(1, (n + block - 1) / block); }
@@ -202,6 +202,7 @@ struct ListFrame {
 // enumeration order (clusters in index order, images in ascending offset,
 // halves): the k-th within the short support at at_near + k, the k-th beyond
 // it at at_far - k, only inside [lo_end, hi_end); nn and nf count them.
+template <bool STORE>
 __device__ void cl_column(const ClusterSet &c, const ListFrame &f, int dy, int dx,
                           long long at_near, long long at_far, long long lo_end,
                           long long hi_end, int &nn, int &nf) {
@@ -266,7 +267,7 @@ __device__ void cl_column(const ClusterSet &c, const ListFrame &f, int dy, int d
                     const bool near = g2 < f.thr_s;
                     // near entries from the front, far ones from the back
                     const long long at = near ? at_near + nn : at_far - nf;
-                    if (at >= lo_end && at < hi_end)
+                    if (STORE && at >= lo_end && at < hi_end)
                         c.ent[at] = make_int2(
                             (int)((unsigned)(2 * cj + h) | (near ? 0x80000000u : 0u)),
                             (dx & 0xff) | ((dy & 0xff) << 8) | (dz << 16));
@@ -285,11 +286,11 @@ __device__ void cl_column(const ClusterSet &c, const ListFrame &f, int dy, int d
 // raster order, then each column's own order).  A list longer than the
 // region raises SPH_ECAPACITY and keeps only what fits.  (A warp per
 // i-cluster with a lane per column measured 3x slower: the lanes' columns
-// differ widely in work.)
-__global__ void __launch_bounds__(128) k_cl_list(const __grid_constant__ View v,
-                                                 const __grid_constant__ ClusterSet c) {
-    const int cl = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cl >= c.ncl_max || cl >= c.colcl[c.ncol]) return;
+// differ widely in work.)  Every thread also records its list length into
+// c.maxfill; with STORE false nothing else is written (the engine sizes the
+// regions from that measurement).
+template <bool STORE>
+__device__ int cl_list_one(const View &v, const ClusterSet &c, int cl) {
     const long long base = (long long)cl * c.lstride, top = base + c.lstride;
     ListFrame f;
     const SimConst<float> &k = v.one.cf;
@@ -313,18 +314,33 @@ __global__ void __launch_bounds__(128) k_cl_list(const __grid_constant__ View v,
         for (int dx = -c.rx; dx <= c.rx; ++dx) {
             int nn, nf;
             // the regions stay apart: near entries below top - tot_far, far above
-            cl_column(c, f, dy, dx, base + tot_near, top - 1 - tot_far, base + tot_near,
-                      top - tot_far, nn, nf);
+            cl_column<STORE>(c, f, dy, dx, base + tot_near, top - 1 - tot_far, base + tot_near,
+                             top - tot_far, nn, nf);
             tot_near += nn;
             tot_far += nf;
         }
-    if (tot_near + tot_far > c.lstride) {
+    const int total = tot_near + tot_far;
+    if (!STORE) return total;
+    if (total > c.lstride) {
         set_err(v.err, v.err_any, c.sim, SPH_ECAPACITY);
         tot_far = 0;
         tot_near = min(tot_near, c.lstride);
     }
     c.lnear[cl] = tot_near;
     c.lfar[cl] = tot_far;
+    return total;
+}
+
+// A thread per i-cluster; the warp's longest list goes to c.maxfill.
+template <bool STORE>
+__global__ void __launch_bounds__(128) k_cl_list(const __grid_constant__ View v,
+                                                 const __grid_constant__ ClusterSet c) {
+    const int cl = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = cl < c.ncl_max && cl < c.colcl[c.ncol];
+    int total = 0;
+    if (live) total = cl_list_one<STORE>(v, c, cl);
+    const int wmax = __reduce_max_sync(0xffffffffu, total);
+    if ((threadIdx.x & 31) == 0 && wmax > 0) atomicMax(c.maxfill, wmax);
 }
 
 // Prefetching the next entry and its j record, per pass: measured faster
@@ -333,15 +349,16 @@ __global__ void __launch_bounds__(128) k_cl_list(const __grid_constant__ View v,
 constexpr bool kPfDensity = false, kPfHeat = false, kPfForce = true;
 
 // Pairs of one lane over n entries from p (step +1 or -1): i = slot si (lane
-// & 7 of the warp's cluster), j = the lane's quarter (lane >> 3) of each
-// listed j-cluster.  body(sj, pj, d, rsq, near) for every pair of the exact
-// set (FP32 test, FP64 in the guard band); near is the entry's flag, uniform
-// across the warp; flush() after every 16th entry of the list (blocked
-// compensated sums).
+// & 7 of the warp's cluster; gi its particle, -1 for a padding slot, which
+// takes no pairs: two padding slots lie at the same far point), j = the
+// lane's quarter (lane >> 3) of each listed j-cluster.  body(sj, pj, d, rsq,
+// near) for every pair of the exact set (FP32 test, FP64 in the guard band);
+// near is the entry's flag, uniform across the warp; flush() after every
+// 16th entry of the list (blocked compensated sums).
 
 template <bool PF, typename F, typename G>
 __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, float thr_lo,
-                                           float thr_hi, int si, const float4 &pi,
+                                           float thr_hi, int si, int gi, const float4 &pi,
                                            const int2 *p, int n, int step, int &flushes,
                                            F body, G flush) {
     const int jj = (threadIdx.x & 31) >> 3;
@@ -375,8 +392,8 @@ __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, f
         d[1] = (pj.y + sy) - pi.y;
         d[2] = (pj.z + sz) - pi.z;
         const float rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        if (rsq <= thr_hi && sj != si &&
-            (rsq < thr_lo || exact_in_set<3>(v.xe_in, &v.one, c.slot_idx[si], c.slot_idx[sj]))) {
+        if (gi >= 0 && rsq <= thr_hi && sj != si &&
+            (rsq < thr_lo || exact_in_set<3>(v.xe_in, &v.one, gi, c.slot_idx[sj]))) {
             if (near) body(sj, pj, d, rsq, std::true_type{});
             else body(sj, pj, d, rsq, std::false_type{});
         }
@@ -388,13 +405,14 @@ __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, f
 // NEAR_ONLY) the far ones from its back, in list order.
 template <bool NEAR_ONLY, bool PF, typename F, typename G>
 __device__ __forceinline__ void cl_for_pairs(const View &v, const ClusterSet &c, float thr_lo,
-                                             float thr_hi, int wid, int si, const float4 &pi,
-                                             F body, G flush) {
+                                             float thr_hi, int wid, int si, int gi,
+                                             const float4 &pi, F body, G flush) {
     const int2 *region = c.ent + (long long)wid * c.lstride;
     int flushes = 0;
-    cl_segment<PF>(v, c, thr_lo, thr_hi, si, pi, region, c.lnear[wid], 1, flushes, body, flush);
+    cl_segment<PF>(v, c, thr_lo, thr_hi, si, gi, pi, region, c.lnear[wid], 1, flushes, body,
+                   flush);
     if (!NEAR_ONLY)
-        cl_segment<PF>(v, c, thr_lo, thr_hi, si, pi, region + c.lstride - 1, c.lfar[wid], -1,
+        cl_segment<PF>(v, c, thr_lo, thr_hi, si, gi, pi, region + c.lstride - 1, c.lfar[wid], -1,
                        flushes, body, flush);
 }
 
@@ -429,7 +447,7 @@ __global__ void __launch_bounds__(kBlock) k_cl_density(const __grid_constant__ V
     rl.init(0.0f);
     unsigned cnt = 0;
     cl_for_pairs<false, kPfDensity>(
-        v, c, k.thr_lo, k.thr_hi, wid, si, pi,
+        v, c, k.thr_lo, k.thr_hi, wid, si, gi, pi,
         [&](int, const float4 &pj, const float *, float rsq, auto near) {
             const float r = sqrtf(rsq);
             float w, g;
@@ -496,7 +514,7 @@ __global__ void __launch_bounds__(kBlock) k_cl_heat(const __grid_constant__ View
     q[2].init(0.0f);
     // only the short kernel enters q: entries beyond its support are skipped
     cl_for_pairs<true, kPfHeat>(
-        v, c, k.thr_lo, k.thr_s, wid, si, pi,
+        v, c, k.thr_lo, k.thr_s, wid, si, gi, pi,
         [&](int sj, const float4 &pj, const float *d, float rsq, auto) {
             const float r = fsqrt<float>(rsq);
             const float g = kernel_g<K, float>(ks, r);
@@ -550,7 +568,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_cl_force(const __grid_constant__ 
     ud.init(0.0f);
     // the pair terms of k_force (forces.py:338-405, c_forces.pyx:96-111, 163-178, 224-237)
     cl_for_pairs<false, kPfForce>(
-        v, c, sc.thr_lo, sc.thr_hi, wid, si, pi,
+        v, c, sc.thr_lo, sc.thr_hi, wid, si, gi, pi,
         [&](int sj, const float4 &pj, const float *d, float rsq, auto near) {
             constexpr bool NEAR = decltype(near)::value;
             const float r = fsqrt<float>(rsq);
@@ -600,7 +618,7 @@ int warp_blocks(const ClusterSet &c) { return nblocks((long long)c.ncl_max * 32,
 
 int cluster_build_kernels() { return 15; }
 
-void launch_cluster_build(const View &v, const ClusterSet &c, cudaStream_t s) {
+void launch_cluster_build(const View &v, const ClusterSet &c, cudaStream_t s, bool store) {
     if (v.np <= 0) return;
     cudaMemsetAsync(c.fcount, 0, sizeof(int) * c.nfine, s);
     k_cl_key<<<nblocks(v.np, kBlock), kBlock, 0, s>>>(v, c);
@@ -613,7 +631,8 @@ void launch_cluster_build(const View &v, const ClusterSet &c, cudaStream_t s) {
     k_cl_slots<<<nblocks(v.np, kBlock), kBlock, 0, s>>>(v, c);
     k_cl_pack<<<nblocks(c.slots_max, kBlock), kBlock, 0, s>>>(v, c, 0);
     k_cl_bbox<<<nblocks(c.ncl_max, kBlock), kBlock, 0, s>>>(c);
-    k_cl_list<<<nblocks(c.ncl_max, 128), 128, 0, s>>>(v, c);
+    if (store) k_cl_list<true><<<nblocks(c.ncl_max, 128), 128, 0, s>>>(v, c);
+    else k_cl_list<false><<<nblocks(c.ncl_max, 128), 128, 0, s>>>(v, c);
 }
 
 void launch_cluster_pack(const View &v, const ClusterSet &c, int stage, cudaStream_t s) {

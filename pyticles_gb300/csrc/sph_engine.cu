@@ -123,6 +123,11 @@ struct sph_engine {
     ClusterSet cl = {};            // tuning.pair_scheme = 1 (sph_cluster.cu)
     int64_t cl_np = 0, cl_fine = 0, cl_col = 0, cl_ncl = 0;  // allocated sizes
     long long cl_ent = 0;
+    int cl_need = 0;               // list entries per i-cluster last measured (x margin)
+    bool cl_stale = true;          // the state changed since the lists were measured
+    int *cl_fill_host = nullptr;   // pinned: longest list of the last advance
+    cudaEvent_t cl_fill_ev = nullptr;
+    bool cl_fill_pending = false;
 
     // profiling: event pairs recorded around each pass
     bool prof_on = false;
@@ -396,9 +401,10 @@ void free_graph(sph_engine *e) {
 
 void cluster_free(sph_engine *e) {
     ClusterSet &c = e->cl;
-    void *ptrs[] = {c.fcount, c.fstart, c.fkey,  c.frank, c.ford,   c.scan_tmp, c.colcnt,
-                    c.colcl,  c.slot_idx, c.slot_of, c.cref, c.ibox, c.jbox,    c.lnear,
-                    c.lfar,   c.ent,    c.cpos,  c.cfv,   c.cf,     c.cq,       c.crho};
+    void *ptrs[] = {c.fcount, c.fstart,  c.fkey,    c.frank, c.ford, c.scan_tmp, c.colcnt,
+                    c.colcl,  c.slot_idx, c.slot_of, c.cref,  c.ibox, c.jbox,     c.lnear,
+                    c.lfar,   c.ent,     c.cpos,    c.cfv,   c.cf,   c.cq,       c.crho,
+                    c.maxfill};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     c = ClusterSet{};
@@ -452,8 +458,11 @@ int cluster_setup(sph_engine *e) {
     const double R = rc + std::max(drift[0], std::max(drift[1], drift[2]));
     const double hz = 8.0 / (rho_n * wx * wy) + gz;
     const double box = (2 * wx + 2 * R) * (2 * wy + 2 * R) * (2 * hz + 2 * R);
-    // (2.6 times the mean list length of a uniform fluid)
-    const int per = (int)std::min(65536.0, std::max(64.0, std::ceil(rho_n * box / 4.0)));
+    // before any measurement 2.6 times the mean list length of a uniform
+    // fluid; afterwards what the longest list measured needs (cluster_measure)
+    const int per = e->cl_need > 0
+                        ? e->cl_need
+                        : (int)std::min(65536.0, std::max(64.0, std::ceil(rho_n * box / 4.0)));
     const long long cap = (long long)per * ncl_max;
     if (S.n > e->cl_np || nfine > e->cl_fine || ncol > e->cl_col || ncl_max > e->cl_ncl ||
         cap > e->cl_ent || (long long)e->cl_ent < (long long)per * e->cl_ncl) {
@@ -481,6 +490,8 @@ int cluster_setup(sph_engine *e) {
         TRY(dalloc(&c.cf, 8 * ncl_max));
         TRY(dalloc(&c.cq, 8 * ncl_max));
         TRY(dalloc(&c.crho, 8 * ncl_max));
+        TRY(dalloc(&c.maxfill, 1));
+        CK(cudaMemset(c.maxfill, 0, sizeof(int)));
         e->cl_np = np;
         e->cl_fine = nfine;
         e->cl_col = ncol;
@@ -506,6 +517,7 @@ int cluster_setup(sph_engine *e) {
     c.slots_max = (int)(8 * ncl_max);
     c.lstride = per;
     c.on = 1;
+    e->cl_stale = true;
     return SPH_OK;
 }
 
@@ -836,6 +848,73 @@ void enqueue_step(sph_engine *e, cudaStream_t st) {
     for (int s = 0; s < e->nstage; ++s) enqueue_stage(e, s, 1, st);
 }
 
+// Measures the longest pair list of the current state (a binning and a
+// list build that only counts) and sizes the list regions to 1.25 times it,
+// growing or shrinking the entry buffer.  Runs before an advance or an
+// evaluation whenever the state was set from outside or the layout changed,
+// and when the previous advance filled a region past 80% (a fluid that
+// condensed into denser regions): an overflow inside an advance is then
+// unlikely, and still reported (SPH_ECAPACITY) if it happens.
+int cluster_measure(sph_engine *e) {
+    ClusterSet &c = e->cl;
+    if (!c.on) return SPH_OK;
+    cudaStream_t st = e->stream;
+    const bool prof = e->prof_on;
+    e->prof_on = false;
+    CK(cudaMemsetAsync(c.maxfill, 0, sizeof(int), st));
+    enqueue_prepare(e, st);
+    View v = make_view(e);
+    stage_view(e, v, 0);
+    launch_cluster_build(v, c, st, false);
+    e->prof_on = prof;
+    int fill = 0;
+    CK(cudaMemcpyAsync(&fill, c.maxfill, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemsetAsync(c.maxfill, 0, sizeof(int), st));
+    CK(cudaStreamSynchronize(st));
+    e->cl_stale = false;
+    const int need = std::max(64, (int)std::ceil(1.25 * fill) + 8);
+    if (need == c.lstride) return SPH_OK;
+    if ((long long)need * c.ncl_max > 2147483000LL) return SPH_ENOMEM;
+    cudaFree(c.ent);
+    c.ent = nullptr;
+    TRY(dalloc(&c.ent, (int64_t)need * c.ncl_max));
+    c.lstride = need;
+    e->cl_need = need;
+    e->cl_ent = (long long)need * c.ncl_max;
+    free_graph(e);
+    return SPH_OK;
+}
+
+// Before an advance or an evaluation with cluster pairs: re-measure if the
+// state changed or the last advance filled a list region past 80%.
+int cluster_check(sph_engine *e) {
+    ClusterSet &c = e->cl;
+    if (!c.on) return SPH_OK;
+    if (e->cl_fill_pending && cudaEventQuery(e->cl_fill_ev) == cudaSuccess) {
+        e->cl_fill_pending = false;
+        if (*e->cl_fill_host > 0.8 * c.lstride) e->cl_stale = true;
+    }
+    if (e->cl_stale) TRY(cluster_measure(e));
+    return SPH_OK;
+}
+
+// After an advance: the longest list of its steps, read back without a
+// wait (checked by the next cluster_check).
+int cluster_note_fill(sph_engine *e) {
+    ClusterSet &c = e->cl;
+    if (!c.on) return SPH_OK;
+    if (!e->cl_fill_host) {
+        CK(cudaMallocHost((void **)&e->cl_fill_host, sizeof(int)));
+        CK(cudaEventCreateWithFlags(&e->cl_fill_ev, cudaEventDisableTiming));
+    }
+    if (e->cl_fill_pending) return SPH_OK;   // the previous read is still in flight
+    CK(cudaMemcpyAsync(e->cl_fill_host, c.maxfill, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemsetAsync(c.maxfill, 0, sizeof(int), e->stream));
+    CK(cudaEventRecord(e->cl_fill_ev, e->stream));
+    e->cl_fill_pending = true;
+    return SPH_OK;
+}
+
 int64_t kernels_per_step(const sph_engine *e) {
     if (e->cl.on) {
         // cluster build; per evaluation density, [heat,] force and the stage
@@ -1077,6 +1156,10 @@ void free_all(sph_engine *e) {
     for (void *p : cp)
         if (p) cudaFree(p);
     cluster_free(e);
+    if (e->cl_fill_host) cudaFreeHost(e->cl_fill_host);
+    if (e->cl_fill_ev) cudaEventDestroy(e->cl_fill_ev);
+    e->cl_fill_host = nullptr;
+    e->cl_fill_ev = nullptr;
     for (int a = 0; a < 3; ++a) {
         void *pa[] = {e->org[a], e->a_pos[a], e->a_vel[a], e->b_pos[a], e->b_vel[a], e->xe[0][a],
                       e->xe[1][a], e->ve[a], e->q[a], e->vdot[a], e->f0v[a], e->acc_r[a],
@@ -1277,6 +1360,7 @@ int sph_sim_set_state(sph_engine *e, int32_t id, const double *r, const double *
     CK(cudaStreamSynchronize(e->stream));
     e->props_valid = false;
     e->bins_valid = false;
+    e->cl_stale = true;
     return SPH_OK;
 }
 
@@ -1335,6 +1419,7 @@ int sph_advance(sph_engine *e, int32_t nsteps) {
     if (nsteps == 0) return SPH_OK;
     TRY(ensure_layout(e));
     if (e->np_b == 0) return SPH_OK;
+    TRY(cluster_check(e));
     cudaStream_t st = e->stream;
     int per = std::max(1, e->tune.steps_per_graph);
     int done = 0;
@@ -1366,6 +1451,7 @@ int sph_advance(sph_engine *e, int32_t nsteps) {
         ++done;
     }
     CK(cudaGetLastError());
+    TRY(cluster_note_fill(e));
     return SPH_OK;
 }
 
@@ -1374,6 +1460,7 @@ int sph_sim_derivatives(sph_engine *e, int32_t id, double *rho, double *rho_lr, 
                         int32_t mem) {
     TRY(check_sim(e, id));
     TRY(ensure_layout(e));
+    TRY(cluster_check(e));
     cudaStream_t st = e->stream;
     enqueue_prepare(e, st);
     enqueue_stage(e, 0, 0, st);
@@ -1586,6 +1673,7 @@ int sph_prepare(sph_engine *e) {
     if (!e) return SPH_EINVAL;
     TRY(ensure_layout(e));
     if (e->np_b == 0 || !e->tune.use_graph) return SPH_OK;
+    TRY(cluster_check(e));
     if (e->a_extent != e->np_b) return SPH_OK;  // first step after a change runs eagerly
     return build_graph(e, std::max(1, e->tune.steps_per_graph));
 }

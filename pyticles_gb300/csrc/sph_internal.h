@@ -181,14 +181,16 @@ struct ClusterSet {
                                   // i-cluster's lstride slots, the far ones from
                                   // the back
     int2 *ent;                    // {j half | near << 31, lattice offset dx|dy<<8|dz<<16}
+    int *maxfill;                 // longest list since the host last read it
     float4 *cpos, *cfv, *cf, *cq; // per slot: {x, y, z, m} local, {v, p/rho^2},
                                   // {p/rho^2, rho, T_hi, T_lo}, {q/rho^2, 0}
     float *crho;
 };
 
 // ---- launch wrappers (sph_cluster.cu) ----
-// Cluster build of the step (stage-0 positions) and its pair lists.
-void launch_cluster_build(const View &v, const ClusterSet &c, cudaStream_t s);
+// Cluster build of the step (stage-0 positions) and its pair lists; with
+// store false the lists are only measured (c.maxfill), not written.
+void launch_cluster_build(const View &v, const ClusterSet &c, cudaStream_t s, bool store = true);
 // Cluster-local packed positions of evaluation `stage` (stage > 0 also
 // checks each particle's drift since the build).
 void launch_cluster_pack(const View &v, const ClusterSet &c, int stage, cudaStream_t s);

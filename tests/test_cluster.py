@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from pyticles_gb300 import Engine, SphError, build, workloads
+from pyticles_gb300 import Engine, SphError, build, make_params, workloads
 from pyticles_gb300._abi import SPH_ESKIN
 from tests.golden_cases import rel_l2
 
@@ -216,3 +216,62 @@ def test_autotuner_times_the_cluster_scheme_for_one_3d_simulation():
     _, table2 = autotune.tune(prm, "fp64", [(prm, r, v, m, u)], steps=2, warmup=1,
                               blocks=(128,), ratios=(0.5,), use_cache=False)
     assert [row["pair_scheme"] for row in table2] == [0]
+
+
+def droplet(seed=3160, gas=False):
+    """8000 particles at density 1.4 in a cube of side 17.9 inside a periodic
+    box of side 40 (mean density 0.125), or with gas=True the same particles
+    spread uniformly over the box.  Columns follow the mean density; the
+    lists of the dense region are about four times longer than a uniform
+    fluid's at that mean."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    side, dens, L = 20, 1.4, 40.0
+    if gas:
+        r = rng.uniform(0.0, L, size=(side ** 3, 3))
+    else:
+        s = dens ** (-1.0 / 3.0)
+        g = (np.arange(side) + 0.5) * s
+        r = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        r = r + rng.uniform(-0.1, 0.1, r.shape) * s + 4.0
+    prm = make_params(dim=3, kernel="cubic", box=[L] * 3, h_short=2.735 / 2, h_long=5.148 / 2,
+                      viscosity=True, heat_flux=True, dt=1e-3)
+    v = rng.normal(0.0, np.sqrt(0.6), size=r.shape)
+    v -= v.mean(axis=0)
+    m = np.ones(len(r))
+    return prm, r, v, m, oracle.initial_energy(prm, r, v, m, 0.6)
+
+
+def test_cluster_lists_are_sized_by_measurement_for_a_dense_droplet():
+    prm, r, v, m, u = droplet()
+    ref = oracle.derivatives(prm, r, v, m, u)
+    kps = {}
+    for scheme in (0, 1):
+        e, s = engine(prm, r, v, m, u, scheme)
+        with e:
+            d = e.derivatives(s)
+            e.sync()
+            kps[scheme] = e.kernels_per_step()
+            if scheme == 1:
+                for k in ("rho", "vdot", "udot"):
+                    assert rel_l2(d[k], ref[k]) < MIXED_TOL, k
+                assert e.last_pair_total() == ref["nip"]
+                e.advance(4)
+                e.sync()                     # no SPH_ECAPACITY
+    assert kps[1] != kps[0]
+
+
+def test_cluster_lists_follow_a_state_that_condenses():
+    """A gas whose state is replaced by the droplet (set_state): the engine
+    measures the lists again before the next step."""
+    prm, r, v, m, u = droplet(gas=True)
+    _, rd, vd, md, ud = droplet()
+    e, s = engine(prm, r, v, m, u, 1, steps_per_graph=2)
+    with e:
+        e.advance(4)
+        e.sync()
+        e.set_state(s, rd, vd, md, ud)
+        e.advance(4)
+        e.sync()                             # no SPH_ECAPACITY
+        rr, vv, uu = e.get_state(s)
+    ro, vo, uo, _ = oracle.advance(prm, rd, vd, md, ud, 4)
+    assert rel_l2(rr, ro) < MIXED_TOL and rel_l2(uu, uo) < MIXED_TOL
