@@ -854,7 +854,8 @@ void enqueue_step(sph_engine *e, cudaStream_t st) {
 // evaluation whenever the state was set from outside or the layout changed,
 // and when the previous advance filled a region past 80% (a fluid that
 // condensed into denser regions): an overflow inside an advance is then
-// unlikely, and still reported (SPH_ECAPACITY) if it happens.
+// unlikely, and still reported (SPH_ECAPACITY) if it happens.  Lists that
+// do not fit in device memory leave the layout on the cell scheme.
 int cluster_measure(sph_engine *e) {
     ClusterSet &c = e->cl;
     if (!c.on) return SPH_OK;
@@ -874,14 +875,22 @@ int cluster_measure(sph_engine *e) {
     e->cl_stale = false;
     const int need = std::max(64, (int)std::ceil(1.25 * fill) + 8);
     if (need == c.lstride) return SPH_OK;
-    if ((long long)need * c.ncl_max > 2147483000LL) return SPH_ENOMEM;
-    cudaFree(c.ent);
-    c.ent = nullptr;
-    TRY(dalloc(&c.ent, (int64_t)need * c.ncl_max));
+    free_graph(e);
+    int st_alloc = SPH_ENOMEM;
+    if ((long long)need * c.ncl_max <= 2147483000LL) {
+        cudaFree(c.ent);
+        c.ent = nullptr;
+        st_alloc = dalloc(&c.ent, (int64_t)need * c.ncl_max);
+    }
+    if (st_alloc != SPH_OK) {
+        // no room for the lists: this layout runs on the cell scheme
+        c.on = 0;
+        e->cl_ent = 0;
+        return SPH_OK;
+    }
     c.lstride = need;
     e->cl_need = need;
     e->cl_ent = (long long)need * c.ncl_max;
-    free_graph(e);
     return SPH_OK;
 }
 
