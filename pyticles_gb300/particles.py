@@ -90,12 +90,16 @@ class SmoothParticleSystem(ParticleSystem):
                  until a particle has used half of its cell slack (the skin
                  reuse of VerletList.compress/ponder_rebuild); the pair set
                  stays exact, the summation order follows the binning times
+    pair_scheme -- 0: cell-window pair passes; 1: cluster pairs (a 3D system
+                 in mixed precision, 1.5x faster; elsewhere the cell scheme
+                 runs); same pair set, rounding differs
     """
 
     def __init__(self, n, d=3, maxn=100, controllers=(), xmax=XMAX, ymax=YMAX, zmax=ZMAX,
                  vmax=VMAX, rinit=None, side=None, mass=1.0, spacing=None, temperature=1.0,
                  thermostat_temp=1.0, thermostat=False, hshort=1.0, hlong=3.0, source=None,
-                 integrator="ieuler", simbox=None, precision="fp64", rebin=False):
+                 integrator="ieuler", simbox=None, precision="fp64", rebin=False,
+                 pair_scheme=0):
         ParticleSystem.__init__(self, n=n, d=d, xmax=xmax, ymax=ymax, zmax=zmax, rinit=rinit,
                                 side=side, mass=mass, source=source, spacing=spacing,
                                 integrator=integrator, vmax=vmax, maxn=maxn, simbox=simbox,
@@ -122,6 +126,7 @@ class SmoothParticleSystem(ParticleSystem):
         self.thermostat_temp = thermostat_temp
         self.precision = precision
         self.rebin = bool(rebin)
+        self.pair_scheme = int(pair_scheme)
         self.timing["SPAM time"] = -1
         self.timing["nlist rebuild time"] = -1
         self._engine = None
@@ -210,7 +215,7 @@ class SmoothParticleSystem(ParticleSystem):
                 self._engine.close()
             self._engine = Engine(prm, precision=self.precision, max_particles=max(n, 1),
                                   max_sims=1)
-            self._engine.set_tuning(rebin=int(self.rebin))
+            self._engine.set_tuning(rebin=int(self.rebin), pair_scheme=self.pair_scheme)
             self._sim = self._engine.add(prm, self.r[:n], self.v[:n], self.m[:n], self.u[:n])
             self._engine_key = key
         else:

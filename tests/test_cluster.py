@@ -275,3 +275,30 @@ def test_cluster_lists_follow_a_state_that_condenses():
         rr, vv, uu = e.get_state(s)
     ro, vo, uo, _ = oracle.advance(prm, rd, vd, md, ud, 4)
     assert rel_l2(rr, ro) < MIXED_TOL and rel_l2(uu, uo) < MIXED_TOL
+
+
+def test_particle_system_with_cluster_pairs():
+    """SmoothParticleSystem(d=3, precision='mixed', pair_scheme=1).run: the
+    Python API path on cluster pairs, against the FP64 oracle."""
+    from pyticles_gb300 import PeriodicBox, SmoothParticleSystem, SpamComplete, VerletList
+    prm, r, v, m, u = case("cubic_heat_8000")
+    n = len(r)
+    L = prm.box[0]
+    p = SmoothParticleSystem(n, d=3, maxn=n, hshort=prm.h_short, hlong=prm.h_long,
+                             simbox=PeriodicBox(xmax=L, ymax=L, zmax=L), precision="mixed",
+                             pair_scheme=1)
+    p.r[:] = r
+    p.v[:] = v
+    p.m[:] = m
+    p.u[:] = u
+    nl = VerletList(p, cutoff=prm.cutoff, tolerance=0.0)
+    p.nlists.append(nl)
+    p.nl_default = nl
+    p.forces.append(SpamComplete(p, nl, eta=prm.visc_alpha, zeta=prm.visc_beta,
+                                 cutoff=prm.cutoff, kernel="cubic", heat_flux=True))
+    p.run(prm.dt, 6)
+    assert p._engine.tuning["pair_scheme"] == 1
+    ro, vo, uo, _ = oracle.advance(prm, r, v, m, u, 6)
+    assert rel_l2(p.r[:n], ro) < MIXED_TOL and rel_l2(p.v[:n], vo) < MIXED_TOL
+    assert rel_l2(p.u[:n], uo) < MIXED_TOL
+    p.close()
