@@ -107,7 +107,9 @@ struct sph_engine {
     void *rho0 = nullptr, *pres0 = nullptr, *pco0 = nullptr;
     void *q[3] = {}, *vdot[3] = {}, *udot = nullptr, *f0v[3] = {}, *f0u = nullptr;
     double *acc_r[3] = {}, *acc_v[3] = {}, *acc_u = nullptr;
-    double *stage_buf = nullptr;  // AoS staging (3 cap_p) + one component (cap_p)
+    double *stage_buf = nullptr;  // host transfers: two AoS regions (3 cap_p each), two
+                                  // components (cap_p each), so that one call's
+                                  // copies need no wait between them
     SimDev *sims_d = nullptr;
     double *t_scale = nullptr, *tsum_part = nullptr;
     long long *steps_d = nullptr;
@@ -989,14 +991,18 @@ int check_sim(sph_engine *e, int32_t id) {
     return SPH_OK;
 }
 
-// Copies n*k doubles from caller memory into the engine's staging buffer.
-int stage_in(sph_engine *e, const double *src, size_t count, int mem, double **out) {
+// Staging regions (offsets in cap_p units): positions, velocities, a scalar.
+constexpr int kStageR = 0, kStageV = 3, kStageU = 6;
+
+// Copies n*k doubles from caller memory into staging region `region`.
+int stage_in(sph_engine *e, const double *src, size_t count, int mem, int region, double **out) {
     if (mem == SPH_DEVICE) {
         *out = const_cast<double *>(src);
         return SPH_OK;
     }
-    CK(cudaMemcpyAsync(e->stage_buf, src, sizeof(double) * count, cudaMemcpyHostToDevice, e->stream));
-    *out = e->stage_buf;
+    double *dst = e->stage_buf + (size_t)region * e->cap_p;
+    CK(cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyHostToDevice, e->stream));
+    *out = dst;
     return SPH_OK;
 }
 
@@ -1007,12 +1013,11 @@ int write_state_range(sph_engine *e, int off, int64_t n, const double *r, const 
     double *vel[3] = {e->a_vel[0] + off, e->a_vel[1] + off, e->a_vel[2] + off};
     double *src;
     if (r) {
-        TRY(stage_in(e, r, (size_t)n * e->dim, mem, &src));
+        TRY(stage_in(e, r, (size_t)n * e->dim, mem, kStageR, &src));
         launch_load_aos(pos, src, (int)n, e->dim, st);
     }
     if (v) {
-        if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));  // staging buffer reuse
-        TRY(stage_in(e, v, (size_t)n * e->dim, mem, &src));
+        TRY(stage_in(e, v, (size_t)n * e->dim, mem, kStageV, &src));
         launch_load_aos(vel, src, (int)n, e->dim, st);
     }
     cudaMemcpyKind k = mem == SPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -1097,7 +1102,7 @@ int alloc_particles(sph_engine *e) {
                    &e->pco0, &e->udot, &e->f0u};
     for (void **p : rs) TRY(dalloc((char **)p, P * e->rsize));
     if (e->group.integrator == SPH_RK4) TRY(dalloc(&e->acc_u, P));
-    TRY(dalloc(&e->stage_buf, P * 4));
+    TRY(dalloc(&e->stage_buf, P * 8));
     if (e->group.collision != SPH_COLLIDE_OFF) {
         // up to one colliding pair per particle per evaluation (SPH_ECAPACITY beyond)
         CollideSet &c = e->coll;
@@ -1378,24 +1383,25 @@ int sph_sim_get_state(sph_engine *e, int32_t id, double *r, double *v, double *u
     Sim &S = e->sims[id];
     cudaStream_t st = e->stream;
     int n = (int)S.n;
+    // each component in its own staging region: the copies follow their
+    // gathers back to back, and one wait at the end covers them all
+    const size_t P = (size_t)e->cap_p;
     if (r) {
-        double *d = mem == SPH_DEVICE ? r : e->stage_buf;
+        double *d = mem == SPH_DEVICE ? r : e->stage_buf + kStageR * P;
         launch_store_aos(d, e->a_pos, e->a_id, S.a_off, n, e->dim, st);
         TRY(copy_out(e, r, (size_t)n * e->dim, mem, d));
-        if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));
     }
     if (v) {
-        double *d = mem == SPH_DEVICE ? v : e->stage_buf;
+        double *d = mem == SPH_DEVICE ? v : e->stage_buf + kStageV * P;
         launch_store_aos(d, e->a_vel, e->a_id, S.a_off, n, e->dim, st);
         TRY(copy_out(e, v, (size_t)n * e->dim, mem, d));
-        if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));
     }
     if (u) {
-        double *d = mem == SPH_DEVICE ? u : e->stage_buf;
+        double *d = mem == SPH_DEVICE ? u : e->stage_buf + kStageU * P;
         launch_store_scalar(d, e->a_u, e->a_id, S.a_off, n, st);
         TRY(copy_out(e, u, (size_t)n, mem, d));
-        if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));
     }
+    if (mem == SPH_HOST) CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     return SPH_OK;
 }

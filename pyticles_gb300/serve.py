@@ -40,7 +40,7 @@ from .workloads import lattice_system, rng_for, vdw_energy
 def bytes_per_particle(precision="mixed", integrator="ieuler"):
     rs = 4 if precision == "mixed" else 8
     v4 = 4 * rs
-    b = 3 * 8 * 8 + 9 * rs + 5 * 8 + 9 * 4 + 7 * v4 + 10 * rs + 4 * 8
+    b = 3 * 8 * 8 + 9 * rs + 5 * 8 + 9 * 4 + 7 * v4 + 10 * rs + 8 * 8
     if integrator == "rk4":
         b += 7 * 8
     return b
