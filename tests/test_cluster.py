@@ -302,3 +302,40 @@ def test_particle_system_with_cluster_pairs():
     assert rel_l2(p.r[:n], ro) < MIXED_TOL and rel_l2(p.v[:n], vo) < MIXED_TOL
     assert rel_l2(p.u[:n], uo) < MIXED_TOL
     p.close()
+
+
+def test_cluster_scheme_in_a_rectangular_box():
+    """Different extents per axis (different column counts and slab
+    heights): pair count and derivatives against the oracle, 3 RK4 steps."""
+    rng = np.random.Generator(np.random.PCG64(3170))
+    s = 0.7 ** (-1.0 / 3.0)
+    nx, ny, nz = 26, 19, 15
+    g = [(np.arange(k) + 0.5) * s for k in (nx, ny, nz)]
+    r = np.stack(np.meshgrid(*g, indexing="ij"), -1).reshape(-1, 3)
+    r = r + rng.uniform(-0.1, 0.1, r.shape) * s
+    box = [nx * s, ny * s, nz * s]
+    prm = make_params(dim=3, kernel="cubic", box=box, h_short=2.735 / 2, h_long=5.148 / 2,
+                      viscosity=True, heat_flux=True, dt=1e-3, integrator="rk4")
+    v = rng.normal(0.0, np.sqrt(0.6), size=r.shape)
+    v -= v.mean(axis=0)
+    m = np.ones(len(r))
+    u = with_gradient(prm, r, v, m, 0.6)
+    ref = oracle.derivatives(prm, r, v, m, u)
+    kps = []
+    for scheme in (0, 1):
+        e, s_ = engine(prm, r, v, m, u, scheme)
+        with e:
+            kps.append(e.kernels_per_step())
+            if scheme == 0:
+                continue
+            d = e.derivatives(s_)
+            e.sync()
+            for k in ("rho", "vdot", "udot"):
+                assert rel_l2(d[k], ref[k]) < MIXED_TOL, k
+            assert e.last_pair_total() == ref["nip"]
+            e.advance(3)
+            e.sync()
+            rr, vv, uu = e.get_state(s_)
+    assert kps[1] != kps[0]
+    ro, vo, uo, _ = oracle.advance(prm, r, v, m, u, 3)
+    assert rel_l2(rr, ro) < MIXED_TOL and rel_l2(uu, uo) < MIXED_TOL
