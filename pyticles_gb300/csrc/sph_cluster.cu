@@ -1,5 +1,6 @@
 // sph_cluster.cu -- the cluster-pair scheme of the pair passes (tuning
-// pair_scheme = 1): one 3D simulation in mixed precision.
+// pair_scheme = 1): 3D simulations in mixed precision, each with its own
+// columns, clusters and lists in flattened tables.
 //
 // The cell-window passes (sph_pairs.cu, sph_force.cuh) give every lane its own
 // particle and its own neighbour cells; in 3D the lanes of a warp then sit in
@@ -48,9 +49,11 @@ int nblocks(long long n, int block) { return (int)std::max<long long>(1, (n + bl
 __global__ void k_cl_key(const __grid_constant__ View v, const __grid_constant__ ClusterSet c) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.np) return;
-    const SimDev &S = v.one;
-    const double step[3] = {c.wxd, c.wyd, c.gzd};
-    const int nk[3] = {c.ncx, c.ncy, c.nslab};
+    const int sim = v.b_sim[i];
+    const SimDev &S = v.sims[sim];
+    const ClGeom &g = c.geom[sim];
+    const double step[3] = {g.wxd, g.wyd, g.gzd};
+    const int nk[3] = {g.ncx, g.ncy, g.nslab};
     int k[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -60,7 +63,7 @@ __global__ void k_cl_key(const __grid_constant__ View v, const __grid_constant__
         q = q < 0 ? 0 : (q >= nk[a] ? nk[a] - 1 : q);
         k[a] = q;
     }
-    const int key = (k[1] * c.ncx + k[0]) * c.nslab + k[2];
+    const int key = g.fine_off + (k[1] * g.ncx + k[0]) * g.nslab + k[2];
     c.fkey[i] = key;
     c.frank[i] = atomicAdd(&c.fcount[key], 1);
 }
@@ -89,10 +92,17 @@ __global__ void k_cl_fsort(const __grid_constant__ ClusterSet c) {
     }
 }
 
+// First fine cell of global column col.
+__device__ __forceinline__ int col_fine(const ClGeom &g, int col) {
+    return g.fine_off + (col - g.col_off) * g.nslab;
+}
+
 __global__ void k_cl_cols(const __grid_constant__ ClusterSet c) {
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= c.ncol) return;
-    const int cnt = c.fstart[(col + 1) * c.nslab] - c.fstart[col * c.nslab];
+    const ClGeom &g = c.geom[c.colsim[col]];
+    const int f0 = col_fine(g, col);
+    const int cnt = c.fstart[f0 + g.nslab] - c.fstart[f0];
     c.colcnt[col] = (cnt + 7) >> 3;
 }
 
@@ -100,16 +110,22 @@ __global__ void k_cl_slots(const __grid_constant__ View v, const __grid_constant
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= v.np) return;
     const int i = c.ford[p];
-    const int key = c.fkey[i];
-    const int col = key / c.nslab;
-    const int q = p - c.fstart[col * c.nslab];
+    const int sim = v.b_sim[i];
+    const ClGeom &g = c.geom[sim];
+    const int local = c.fkey[i] - g.fine_off;
+    const int lcol = local / g.nslab;
+    const int col = g.col_off + lcol;
+    const int q = p - c.fstart[g.fine_off + lcol * g.nslab];
     const int cl = c.colcl[col] + (q >> 3);
     const int slot = cl * 8 + (q & 7);
     if (!SPH_IN_BOUNDS(cl >= 0 && cl < c.ncl_max, v.err_any)) return;
     c.slot_idx[slot] = i;
     c.slot_of[i] = slot;
     // the first particle of a cluster lies in its lowest slab
-    if ((q & 7) == 0) c.cref[cl] = make_int4(col % c.ncx, col / c.ncx, key % c.nslab, col);
+    if ((q & 7) == 0) {
+        c.cref[cl] = make_int4(lcol % g.ncx, lcol / g.ncx, local % g.nslab, col);
+        c.csim[cl] = sim;
+    }
 }
 
 // Positions relative to the cluster's lattice point (column centre in x and
@@ -124,9 +140,11 @@ __global__ void k_cl_pack(const __grid_constant__ View v, const __grid_constant_
         c.cpos[slot] = make_float4(kFar, kFar, kFar, 0.0f);
         return;
     }
-    const SimDev &S = v.one;
+    const int sim = c.csim[slot >> 3];
+    const SimDev &S = v.sims[sim];
+    const ClGeom &g = c.geom[sim];
     const int4 r = c.cref[slot >> 3];
-    const double ref[3] = {(r.x + 0.5) * c.wxd, (r.y + 0.5) * c.wyd, r.z * c.gzd};
+    const double ref[3] = {(r.x + 0.5) * g.wxd, (r.y + 0.5) * g.wyd, r.z * g.gzd};
     float l[3];
     bool skin = false;
 #pragma unroll
@@ -143,7 +161,7 @@ __global__ void k_cl_pack(const __grid_constant__ View v, const __grid_constant_
             skin |= fabs(m) > S.slack_half[a];
         }
     }
-    if (skin) set_err(v.err, v.err_any, c.sim, SPH_ESKIN);
+    if (skin) set_err(v.err, v.err_any, sim, SPH_ESKIN);
     c.cpos[slot] = make_float4(l[0], l[1], l[2], (float)v.b_m[i]);
 }
 
@@ -188,8 +206,9 @@ __device__ __forceinline__ float gap_less(float alo, float ahi, float blo, float
 }
 __device__ __forceinline__ float sq_add(float acc, float g) { return __fadd_rn(acc, __fmul_rn(g, g)); }
 
-// Per-i-cluster constants of the list build.
+// Per-i-cluster constants of the list build (with its simulation's lattice).
 struct ListFrame {
+    ClGeom g;
     float4 ilo, ihi;
     int4 ri;
     float thr, thr_s, m0, m1, m2;
@@ -208,36 +227,38 @@ __device__ void cl_column(const ClusterSet &c, const ListFrame &f, int dy, int d
                           long long hi_end, int &nn, int &nf) {
     nn = 0;
     nf = 0;
-    const float sy = __fmul_rn((float)dy, c.wy), sx = __fmul_rn((float)dx, c.wx);
-    const float hwy = __fmul_rn(0.5f, c.wy), hwx = __fmul_rn(0.5f, c.wx);
+    const ClGeom &g = f.g;
+    const float sy = __fmul_rn((float)dy, g.wy), sx = __fmul_rn((float)dx, g.wx);
+    const float hwy = __fmul_rn(0.5f, g.wy), hwx = __fmul_rn(0.5f, g.wx);
     const float gy = gap_less(f.ilo.y, f.ihi.y, __fsub_rn(sy, hwy), __fadd_rn(sy, hwy), f.m1);
     const float gx = gap_less(f.ilo.x, f.ihi.x, __fsub_rn(sx, hwx), __fadd_rn(sx, hwx), f.m0);
     if (sq_add(__fmul_rn(gx, gx), gy) >= f.thr) return;
-    int ky = (f.ri.y + dy) % c.ncy;
-    ky += ky < 0 ? c.ncy : 0;
-    int kx = (f.ri.x + dx) % c.ncx;
-    kx += kx < 0 ? c.ncx : 0;
-    const int col = ky * c.ncx + kx;
+    int ky = (f.ri.y + dy) % g.ncy;
+    ky += ky < 0 ? g.ncy : 0;
+    int kx = (f.ri.x + dx) % g.ncx;
+    kx += kx < 0 ? g.ncx : 0;
+    const int lcol = ky * g.ncx + kx;
+    const int col = g.col_off + lcol;
     const int cb = c.colcl[col], ce = c.colcl[col + 1];
     if (cb == ce) return;
-    const int f0 = col * c.nslab;
+    const int f0 = g.fine_off + lcol * g.nslab;
     const int pstart = c.fstart[f0];
     // first cluster holding a particle of slab >= s (0 <= s <= nslab);
     // one past the last holding a particle of slab <= s (-1 <= s < nslab)
     auto first_cl = [&](int s) { return cb + ((c.fstart[f0 + s] - pstart) >> 3); };
     auto end_cl = [&](int s) { return cb + ((c.fstart[f0 + s + 1] - pstart + 7) >> 3); };
     int b0 = cb, b1 = cb, a0, a1;
-    if (f.shi - f.slo + 1 >= c.nslab) {
+    if (f.shi - f.slo + 1 >= g.nslab) {
         a0 = cb;
         a1 = ce;
     } else if (f.slo < 0) {
         b1 = end_cl(f.shi);
-        a0 = max(first_cl(f.slo + c.nslab), b1);
+        a0 = max(first_cl(f.slo + g.nslab), b1);
         a1 = ce;
-    } else if (f.shi >= c.nslab) {
+    } else if (f.shi >= g.nslab) {
         a0 = first_cl(f.slo);
         a1 = ce;
-        b1 = min(end_cl(f.shi - c.nslab), a0);
+        b1 = min(end_cl(f.shi - g.nslab), a0);
     } else {
         a0 = first_cl(f.slo);
         a1 = end_cl(f.shi);
@@ -252,8 +273,8 @@ __device__ void cl_column(const ClusterSet &c, const ListFrame &f, int dy, int d
             if (cxy >= f.thr) continue;
             const int dz0 = c.cref[cj].z - f.ri.z;
             for (int img = -1; img <= 1; ++img) {
-                const int dz = dz0 + img * c.nslab;
-                const float sz = __fmul_rn((float)dz, c.gz);
+                const int dz = dz0 + img * g.nslab;
+                const float sz = __fmul_rn((float)dz, g.gz);
                 const float cz = gap_less(f.ilo.z, f.ihi.z, __fadd_rn(clo.z, sz), __fadd_rn(chi.z, sz), f.m2);
                 if (sq_add(cxy, cz) >= f.thr) continue;
                 for (int h = 0; h < 2; ++h) {
@@ -292,26 +313,28 @@ __device__ void cl_column(const ClusterSet &c, const ListFrame &f, int dy, int d
 template <bool STORE>
 __device__ int cl_list_one(const View &v, const ClusterSet &c, int cl) {
     const long long base = (long long)cl * c.lstride, top = base + c.lstride;
+    const int sim = c.csim[cl];
     ListFrame f;
-    const SimConst<float> &k = v.one.cf;
+    f.g = c.geom[sim];
+    const SimConst<float> &k = v.sims[sim].cf;
     f.thr = k.thr_hi;
     f.thr_s = k.thr_s;
     const float eps = 1.0e-3f;  // rounding of boxes and shifts, far above it
-    f.m0 = c.drift2[0] + eps;
-    f.m1 = c.drift2[1] + eps;
-    f.m2 = c.drift2[2] + eps;
+    f.m0 = f.g.drift2[0] + eps;
+    f.m1 = f.g.drift2[1] + eps;
+    f.m2 = f.g.drift2[2] + eps;
     f.ilo = c.ibox[2 * cl];
     f.ihi = c.ibox[2 * cl + 1];
     f.ri = c.cref[cl];
     const float reach_z = __fadd_rn(__fsqrt_rn(f.thr), f.m2);
-    const float zref = __fmul_rn((float)f.ri.z, c.gz);
+    const float zref = __fmul_rn((float)f.ri.z, f.g.gz);
     const float zlo = __fsub_rn(__fadd_rn(zref, f.ilo.z), reach_z);
     const float zhi = __fadd_rn(__fadd_rn(zref, f.ihi.z), reach_z);
-    f.slo = (int)floorf(__fdiv_rn(zlo, c.gz)) - 1;
-    f.shi = (int)floorf(__fdiv_rn(zhi, c.gz)) + 1;
+    f.slo = (int)floorf(__fdiv_rn(zlo, f.g.gz)) - 1;
+    f.shi = (int)floorf(__fdiv_rn(zhi, f.g.gz)) + 1;
     int tot_near = 0, tot_far = 0;
-    for (int dy = -c.ry; dy <= c.ry; ++dy)
-        for (int dx = -c.rx; dx <= c.rx; ++dx) {
+    for (int dy = -f.g.ry; dy <= f.g.ry; ++dy)
+        for (int dx = -f.g.rx; dx <= f.g.rx; ++dx) {
             int nn, nf;
             // the regions stay apart: near entries below top - tot_far, far above
             cl_column<STORE>(c, f, dy, dx, base + tot_near, top - 1 - tot_far, base + tot_near,
@@ -322,7 +345,7 @@ __device__ int cl_list_one(const View &v, const ClusterSet &c, int cl) {
     const int total = tot_near + tot_far;
     if (!STORE) return total;
     if (total > c.lstride) {
-        set_err(v.err, v.err_any, c.sim, SPH_ECAPACITY);
+        set_err(v.err, v.err_any, sim, SPH_ECAPACITY);
         tot_far = 0;
         tot_near = min(tot_near, c.lstride);
     }
@@ -356,11 +379,17 @@ constexpr bool kPfDensity = false, kPfHeat = false, kPfForce = true;
 // near is the entry's flag, uniform across the warp; flush() after every
 // 16th entry of the list (blocked compensated sums).
 
+// The lattice steps of the warp's simulation and its constants.
+struct PairCtx {
+    const SimDev *S;
+    float wx, wy, gz;
+    float thr_lo, thr_hi;
+};
+
 template <bool PF, typename F, typename G>
-__device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, float thr_lo,
-                                           float thr_hi, int si, int gi, const float4 &pi,
-                                           const int2 *p, int n, int step, int &flushes,
-                                           F body, G flush) {
+__device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, const PairCtx &x,
+                                           int si, int gi, const float4 &pi, const int2 *p, int n,
+                                           int step, int &flushes, F body, G flush) {
     const int jj = (threadIdx.x & 31) >> 3;
     int2 en_n = make_int2(0, 0);
     float4 pj_n = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -384,16 +413,16 @@ __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, f
         }
         const bool near = en.x < 0;
         const int sj = (en.x & 0x7fffffff) * 4 + jj;
-        const float sx = (float)(signed char)(en.y & 0xff) * c.wx;
-        const float sy = (float)(signed char)((en.y >> 8) & 0xff) * c.wy;
-        const float sz = (float)(en.y >> 16) * c.gz;
+        const float sx = (float)(signed char)(en.y & 0xff) * x.wx;
+        const float sy = (float)(signed char)((en.y >> 8) & 0xff) * x.wy;
+        const float sz = (float)(en.y >> 16) * x.gz;
         float d[3];
         d[0] = (pj.x + sx) - pi.x;
         d[1] = (pj.y + sy) - pi.y;
         d[2] = (pj.z + sz) - pi.z;
         const float rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        if (gi >= 0 && rsq <= thr_hi && sj != si &&
-            (rsq < thr_lo || exact_in_set<3>(v.xe_in, &v.one, gi, c.slot_idx[sj]))) {
+        if (gi >= 0 && rsq <= x.thr_hi && sj != si &&
+            (rsq < x.thr_lo || exact_in_set<3>(v.xe_in, x.S, gi, c.slot_idx[sj]))) {
             if (near) body(sj, pj, d, rsq, std::true_type{});
             else body(sj, pj, d, rsq, std::false_type{});
         }
@@ -404,16 +433,44 @@ __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, f
 // The near entries from the front of the i-cluster's region, then (unless
 // NEAR_ONLY) the far ones from its back, in list order.
 template <bool NEAR_ONLY, bool PF, typename F, typename G>
-__device__ __forceinline__ void cl_for_pairs(const View &v, const ClusterSet &c, float thr_lo,
-                                             float thr_hi, int wid, int si, int gi,
-                                             const float4 &pi, F body, G flush) {
+__device__ __forceinline__ void cl_for_pairs(const View &v, const ClusterSet &c, const PairCtx &x,
+                                             int wid, int si, int gi, const float4 &pi, F body,
+                                             G flush) {
     const int2 *region = c.ent + (long long)wid * c.lstride;
     int flushes = 0;
-    cl_segment<PF>(v, c, thr_lo, thr_hi, si, gi, pi, region, c.lnear[wid], 1, flushes, body,
-                   flush);
+    cl_segment<PF>(v, c, x, si, gi, pi, region, c.lnear[wid], 1, flushes, body, flush);
     if (!NEAR_ONLY)
-        cl_segment<PF>(v, c, thr_lo, thr_hi, si, gi, pi, region + c.lstride - 1, c.lfar[wid], -1,
-                       flushes, body, flush);
+        cl_segment<PF>(v, c, x, si, gi, pi, region + c.lstride - 1, c.lfar[wid], -1, flushes,
+                       body, flush);
+}
+
+// The warp's simulation: kernel parameters for a single simulation (ONE),
+// else its table entries.
+template <bool ONE>
+__device__ __forceinline__ const SimDev &cl_sim(const View &v, int sim) {
+    if constexpr (ONE) return v.one;
+    else return v.sims[sim];
+}
+template <bool ONE>
+__device__ __forceinline__ const ClGeom &cl_geom(const ClusterSet &c, int sim) {
+    if constexpr (ONE) return c.g1;
+    else return c.geom[sim];
+}
+template <bool ONE>
+__device__ __forceinline__ int cl_simid(const ClusterSet &c, int wid) {
+    if constexpr (ONE) return c.sim1;
+    else return c.csim[wid];
+}
+
+__device__ __forceinline__ PairCtx pair_ctx(const SimDev &S, const ClGeom &g, float thr_hi) {
+    PairCtx x;
+    x.S = &S;
+    x.wx = g.wx;
+    x.wy = g.wy;
+    x.gz = g.gz;
+    x.thr_lo = S.cf.thr_lo;
+    x.thr_hi = thr_hi;
+    return x;
 }
 
 // Sum over the four lanes that share i (lanes ii, ii + 8, ii + 16, ii + 24),
@@ -429,7 +486,7 @@ __device__ __forceinline__ bool cl_live(const ClusterSet &c, int wid) {
     return wid < c.ncl_max && wid < c.colcl[c.ncol];
 }
 
-template <int K>
+template <int K, bool ONE>
 __global__ void __launch_bounds__(kBlock) k_cl_density(const __grid_constant__ View v,
                                                        const __grid_constant__ ClusterSet c,
                                                        int stage) {
@@ -439,15 +496,16 @@ __global__ void __launch_bounds__(kBlock) k_cl_density(const __grid_constant__ V
     const int si = wid * 8 + ii;
     const float4 pi = c.cpos[si];
     const int gi = c.slot_idx[si];
-    const SimDev &S = v.one;
-    const SimConst<float> &k = S.cf;
+    const int sim = cl_simid<ONE>(c, wid);
+    const SimDev &S = cl_sim<ONE>(v, sim);
+    const PairCtx x = pair_ctx(S, cl_geom<ONE>(c, sim), S.cf.thr_hi);
     const KConst<float> ks = make_kconst<float>(S, 0), kl = make_kconst<float>(S, 1);
     BAcc<float> rs, rl;
     rs.init(0.0f);
     rl.init(0.0f);
     unsigned cnt = 0;
     cl_for_pairs<false, kPfDensity>(
-        v, c, k.thr_lo, k.thr_hi, wid, si, gi, pi,
+        v, c, x, wid, si, gi, pi,
         [&](int, const float4 &pj, const float *, float rsq, auto near) {
             const float r = sqrtf(rsq);
             float w, g;
@@ -465,7 +523,7 @@ __global__ void __launch_bounds__(kBlock) k_cl_density(const __grid_constant__ V
         });
     const double sum_s = quad_sum(rs.get64()), sum_l = quad_sum(rl.get64());
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if (lane == 0) atomicAdd(&v.pair_count[c.sim], (unsigned long long)cnt);
+    if (lane == 0) atomicAdd(&v.pair_count[sim], (unsigned long long)cnt);
     if (jj != 0 || gi < 0) return;
     // EOS in FP64, as in the cell-window density pass (k_density)
     const double rho = S.ws0 + S.sig_s * sum_s;
@@ -492,10 +550,10 @@ __global__ void __launch_bounds__(kBlock) k_cl_density(const __grid_constant__ V
     const float4 vi = ((const float4 *)v.pk_vel_in)[gi];
     c.cfv[si] = make_float4(vi.x, vi.y, vi.z, (float)fs);
     if (!isfinite((float)p) || !isfinite((float)rho) || !isfinite((float)rhol))
-        set_err(v.err, v.err_any, c.sim, SPH_ENAN);
+        set_err(v.err, v.err_any, sim, SPH_ENAN);
 }
 
-template <int K>
+template <int K, bool ONE>
 __global__ void __launch_bounds__(kBlock) k_cl_heat(const __grid_constant__ View v,
                                                     const __grid_constant__ ClusterSet c) {
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -504,8 +562,11 @@ __global__ void __launch_bounds__(kBlock) k_cl_heat(const __grid_constant__ View
     const int si = wid * 8 + ii;
     const float4 pi = c.cpos[si];
     const int gi = c.slot_idx[si];
-    const SimDev &S = v.one;
+    const int sim = cl_simid<ONE>(c, wid);
+    const SimDev &S = cl_sim<ONE>(v, sim);
     const SimConst<float> &k = S.cf;
+    // only the short kernel enters q: the pair test stops at its support
+    const PairCtx x = pair_ctx(S, cl_geom<ONE>(c, sim), k.thr_s);
     const KConst<float> ks = make_kconst<float>(S, 0);
     const float4 fi = c.cf[si];
     BAcc<float> q[3];
@@ -514,7 +575,7 @@ __global__ void __launch_bounds__(kBlock) k_cl_heat(const __grid_constant__ View
     q[2].init(0.0f);
     // only the short kernel enters q: entries beyond its support are skipped
     cl_for_pairs<true, kPfHeat>(
-        v, c, k.thr_lo, k.thr_s, wid, si, gi, pi,
+        v, c, x, wid, si, gi, pi,
         [&](int sj, const float4 &pj, const float *d, float rsq, auto) {
             const float r = fsqrt<float>(rsq);
             const float g = kernel_g<K, float>(ks, r);
@@ -542,8 +603,11 @@ __global__ void __launch_bounds__(kBlock) k_cl_heat(const __grid_constant__ View
     c.cq[si] = make_float4(qq[0] * ir2, qq[1] * ir2, qq[2] * ir2, 0.0f);
 }
 
-template <int K, int VH>
-__global__ void __launch_bounds__(kBlock, 4) k_cl_force(const __grid_constant__ View v,
+// Register caps: 64 for a single simulation (constants in the kernel
+// parameters); 85 for several, whose constants come from the table (64
+// spilled 168 bytes).
+template <int K, int VH, bool ONE>
+__global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_cl_force(const __grid_constant__ View v,
                                                      const __grid_constant__ ClusterSet c) {
     constexpr bool visc = (VH & 1) != 0;
     constexpr bool heat = (VH & 2) != 0;
@@ -553,8 +617,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_cl_force(const __grid_constant__ 
     const int si = wid * 8 + ii;
     const float4 pi = c.cpos[si];
     const int gi = c.slot_idx[si];
-    const SimDev &S = v.one;
+    const int sim = cl_simid<ONE>(c, wid);
+    const SimDev &S = cl_sim<ONE>(v, sim);
     const SimConst<float> &sc = S.cf;
+    const PairCtx x = pair_ctx(S, cl_geom<ONE>(c, sim), sc.thr_hi);
     const KConst<float> ks = make_kconst<float>(S, 0), kl = make_kconst<float>(S, 1);
     const float hs = sc.hs, eps_h2 = sc.eps_h2, alpha_c = sc.alpha_c, beta = sc.beta;
     const float pl2 = sc.pl2;
@@ -568,7 +634,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_cl_force(const __grid_constant__ 
     ud.init(0.0f);
     // the pair terms of k_force (forces.py:338-405, c_forces.pyx:96-111, 163-178, 224-237)
     cl_for_pairs<false, kPfForce>(
-        v, c, sc.thr_lo, sc.thr_hi, wid, si, gi, pi,
+        v, c, x, wid, si, gi, pi,
         [&](int sj, const float4 &pj, const float *d, float rsq, auto near) {
             constexpr bool NEAR = decltype(near)::value;
             const float r = fsqrt<float>(rsq);
@@ -609,7 +675,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_cl_force(const __grid_constant__ 
     if (jj != 0 || gi < 0) return;
     for (int a = 0; a < 3; ++a) ((float *)v.vdot[a])[gi] = vd[a];
     ((float *)v.udot)[gi] = u;
-    if (!isfinite(vd[0]) || !isfinite(u)) set_err(v.err, v.err_any, c.sim, SPH_ENAN);
+    if (!isfinite(vd[0]) || !isfinite(u)) set_err(v.err, v.err_any, sim, SPH_ENAN);
 }
 
 int warp_blocks(const ClusterSet &c) { return nblocks((long long)c.ncl_max * 32, kBlock); }
@@ -639,27 +705,42 @@ void launch_cluster_pack(const View &v, const ClusterSet &c, int stage, cudaStre
     k_cl_pack<<<nblocks(c.slots_max, kBlock), kBlock, 0, s>>>(v, c, stage);
 }
 
-#define SPH_CL_KERNELS(CALL)                                                          \
-    switch (kernel) {                                                                 \
-        case SPH_KERNEL_GAUSSIAN: { constexpr int K = SPH_KERNEL_GAUSSIAN; CALL; break; } \
-        case SPH_KERNEL_LUCY: { constexpr int K = SPH_KERNEL_LUCY; CALL; break; }         \
-        case SPH_KERNEL_DEBRUN: { constexpr int K = SPH_KERNEL_DEBRUN; CALL; break; }     \
-        default: { constexpr int K = SPH_KERNEL_CUBIC; CALL; break; }                     \
+#define SPH_CL_KERNELS(...)                                                                  \
+    switch (kernel) {                                                                        \
+        case SPH_KERNEL_GAUSSIAN: { constexpr int K = SPH_KERNEL_GAUSSIAN; __VA_ARGS__; break; } \
+        case SPH_KERNEL_LUCY: { constexpr int K = SPH_KERNEL_LUCY; __VA_ARGS__; break; }         \
+        case SPH_KERNEL_DEBRUN: { constexpr int K = SPH_KERNEL_DEBRUN; __VA_ARGS__; break; }     \
+        default: { constexpr int K = SPH_KERNEL_CUBIC; __VA_ARGS__; break; }                     \
     }
 
 void launch_cluster_density(const View &v, const ClusterSet &c, int kernel, int stage,
                             cudaStream_t s) {
-    SPH_CL_KERNELS((k_cl_density<K><<<warp_blocks(c), kBlock, 0, s>>>(v, c, stage)));
+    if (v.one_sim) {
+        SPH_CL_KERNELS(k_cl_density<K, true><<<warp_blocks(c), kBlock, 0, s>>>(v, c, stage));
+    } else {
+        SPH_CL_KERNELS(k_cl_density<K, false><<<warp_blocks(c), kBlock, 0, s>>>(v, c, stage));
+    }
 }
 
 void launch_cluster_heat(const View &v, const ClusterSet &c, int kernel, cudaStream_t s) {
-    SPH_CL_KERNELS((k_cl_heat<K><<<warp_blocks(c), kBlock, 0, s>>>(v, c)));
+    if (v.one_sim) {
+        SPH_CL_KERNELS(k_cl_heat<K, true><<<warp_blocks(c), kBlock, 0, s>>>(v, c));
+    } else {
+        SPH_CL_KERNELS(k_cl_heat<K, false><<<warp_blocks(c), kBlock, 0, s>>>(v, c));
+    }
 }
 
 void launch_cluster_force(const View &v, const ClusterSet &c, int kernel, int viscosity, int heat,
                           cudaStream_t s) {
     const int vh = (viscosity ? 1 : 0) | (heat ? 2 : 0);
-#define SPH_CL_FORCE(VH_) SPH_CL_KERNELS((k_cl_force<K, VH_><<<warp_blocks(c), kBlock, 0, s>>>(v, c)))
+#define SPH_CL_FORCE(VH_)                                                                \
+    do {                                                                                 \
+        if (v.one_sim) {                                                                 \
+            SPH_CL_KERNELS(k_cl_force<K, VH_, true><<<warp_blocks(c), kBlock, 0, s>>>(v, c));  \
+        } else {                                                                         \
+            SPH_CL_KERNELS(k_cl_force<K, VH_, false><<<warp_blocks(c), kBlock, 0, s>>>(v, c)); \
+        }                                                                                \
+    } while (0)
     switch (vh) {
         case 0: SPH_CL_FORCE(0); break;
         case 1: SPH_CL_FORCE(1); break;

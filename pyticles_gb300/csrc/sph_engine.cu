@@ -123,6 +123,8 @@ struct sph_engine {
     bool one_sim = false;          // exactly one live simulation (one_dev)
     SimDev one_dev;
     ClusterSet cl = {};            // tuning.pair_scheme = 1 (sph_cluster.cu)
+    ClGeom *cl_geom_d = nullptr;   // per simulation slot
+    int cl_geom_cap = 0;
     int64_t cl_np = 0, cl_fine = 0, cl_col = 0, cl_ncl = 0;  // allocated sizes
     long long cl_ent = 0;
     int cl_need = 0;               // list entries per i-cluster last measured (x margin)
@@ -406,7 +408,7 @@ void cluster_free(sph_engine *e) {
     void *ptrs[] = {c.fcount, c.fstart,  c.fkey,    c.frank, c.ford, c.scan_tmp, c.colcnt,
                     c.colcl,  c.slot_idx, c.slot_of, c.cref,  c.ibox, c.jbox,     c.lnear,
                     c.lfar,   c.ent,     c.cpos,    c.cfv,   c.cf,   c.cq,       c.crho,
-                    c.maxfill};
+                    c.maxfill, c.colsim, c.csim};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     c = ClusterSet{};
@@ -414,62 +416,84 @@ void cluster_free(sph_engine *e) {
     e->cl_ent = 0;
 }
 
-// Cluster geometry of the engine's single 3D simulation (tuning.pair_scheme
-// = 1): columns about 8 particles wide (the cube root of the volume of 8 at
-// the mean density), slabs a quarter of that, the column reach of the cutoff
-// plus twice the allowed drift, and the buffers.  Leaves c.on = 0 (the cell
-// scheme runs) where the scheme does not apply.
+// Cluster geometry of every live 3D simulation (tuning.pair_scheme = 1):
+// columns about 8 particles wide (the cube root of the volume of 8 at the
+// simulation's mean density), slabs a quarter of that, the column reach of
+// the cutoff plus twice the allowed drift, each simulation's range in the
+// flattened column and fine-cell tables, and the buffers.  Leaves c.on = 0
+// (the cell scheme runs) where the scheme does not apply to every
+// simulation.
 int cluster_setup(sph_engine *e) {
     ClusterSet &c = e->cl;
     c.on = 0;
-    if (e->tune.pair_scheme != 1 || !e->one_sim || e->dim != 3 || e->precision != SPH_MIXED ||
+    if (e->tune.pair_scheme != 1 || e->dim != 3 || e->precision != SPH_MIXED ||
         e->group.collision != SPH_COLLIDE_OFF || e->np_b < 8)
         return SPH_OK;
-    int sid = -1;
-    for (int s = 0; s < (int)e->sims.size(); ++s)
-        if (e->sims[s].active) sid = s;
-    const Sim &S = e->sims[sid];
-    const SimDev &d = e->one_dev;
-    const double *L = S.prm.box;
-    const double vol = L[0] * L[1] * L[2];
-    const double wt = std::cbrt(8.0 * vol / (double)S.n);
-    const int ncx = std::max(1, (int)std::floor(L[0] / wt));
-    const int ncy = std::max(1, (int)std::floor(L[1] / wt));
-    const int nslab = std::max(1, (int)std::floor(L[2] / (0.25 * wt)));
-    const double wx = L[0] / ncx, wy = L[1] / ncy, gz = L[2] / nslab;
-    const double rc = std::sqrt(d.thr);
-    double drift[3];
-    for (int a = 0; a < 3; ++a) {
-        drift[a] = 2.0 * d.slack_half[a];
-        if (!(drift[a] < 0.25 * L[a])) return SPH_OK;   // single-cell axis or no slack room
+    std::vector<ClGeom> geom(e->cap_s);
+    std::vector<int> colsim;
+    int64_t ncol = 0, nfine = 0, ncl_max = 0, np = 0;
+    double per_est = 64.0;
+    for (int sid = 0; sid < (int)e->sims.size(); ++sid) {
+        const Sim &S = e->sims[sid];
+        memset(&geom[sid], 0, sizeof(ClGeom));
+        if (!S.active) continue;
+        const SimDev d = make_simdev(e, S);
+        const double *L = S.prm.box;
+        const double vol = L[0] * L[1] * L[2];
+        const double wt = std::cbrt(8.0 * vol / (double)S.n);
+        const int ncx = std::max(1, (int)std::floor(L[0] / wt));
+        const int ncy = std::max(1, (int)std::floor(L[1] / wt));
+        const int nslab = std::max(1, (int)std::floor(L[2] / (0.25 * wt)));
+        const double wx = L[0] / ncx, wy = L[1] / ncy, gz = L[2] / nslab;
+        const double rc = std::sqrt(d.thr);
+        double drift[3];
+        for (int a = 0; a < 3; ++a) {
+            drift[a] = 2.0 * d.slack_half[a];
+            if (!(drift[a] < 0.25 * L[a])) return SPH_OK;   // single-cell axis or no slack room
+        }
+        // a column dx over lies at least (|dx| - 1) widths away
+        const int rx = (int)std::ceil((rc + drift[0] + 1e-3) / wx);
+        const int ry = (int)std::ceil((rc + drift[1] + 1e-3) / wy);
+        // every column and every z image within reach must be distinct
+        if (2 * rx + 1 > ncx || 2 * ry + 1 > ncy || rx > 100 || ry > 100) return SPH_OK;
+        if (L[2] < 2.0 * (rc + drift[2]) + 4.0 * gz || nslab > 30000) return SPH_OK;
+        const int64_t sfine = (int64_t)ncx * ncy * nslab;
+        if (sfine > std::max<int64_t>(int64_t(1) << 16, 16 * S.n)) return SPH_OK;
+        ClGeom &g = geom[sid];
+        g.ncx = ncx;
+        g.ncy = ncy;
+        g.nslab = nslab;
+        g.rx = rx;
+        g.ry = ry;
+        g.col_off = (int)ncol;
+        g.fine_off = (int)nfine;
+        g.wxd = wx;
+        g.wyd = wy;
+        g.gzd = gz;
+        g.wx = (float)wx;
+        g.wy = (float)wy;
+        g.gz = (float)gz;
+        for (int a = 0; a < 3; ++a) g.drift2[a] = (float)drift[a];
+        for (int k = 0; k < ncx * ncy; ++k) colsim.push_back(sid);
+        ncol += (int64_t)ncx * ncy;
+        nfine += sfine;
+        ncl_max += S.n / 8 + (int64_t)ncx * ncy + 1;
+        np += S.n;
+        // list length before any measurement: 2.6 times the mean of a uniform
+        // fluid (the j-halves in the box of an i-cluster grown by the reach)
+        const double rho_n = (double)S.n / vol;
+        const double R = rc + std::max(drift[0], std::max(drift[1], drift[2]));
+        const double hz = 8.0 / (rho_n * wx * wy) + gz;
+        const double box = (2 * wx + 2 * R) * (2 * wy + 2 * R) * (2 * hz + 2 * R);
+        per_est = std::max(per_est, std::ceil(rho_n * box / 4.0));
     }
-    // a column dx over lies at least (|dx| - 1) widths away
-    const int rx = (int)std::ceil((rc + drift[0] + 1e-3) / wx);
-    const int ry = (int)std::ceil((rc + drift[1] + 1e-3) / wy);
-    // every column and every z image within reach must be distinct
-    if (2 * rx + 1 > ncx || 2 * ry + 1 > ncy || rx > 100 || ry > 100) return SPH_OK;
-    if (L[2] < 2.0 * (rc + drift[2]) + 4.0 * gz || nslab > 30000) return SPH_OK;
-    const int64_t nfine = (int64_t)ncx * ncy * nslab;
-    if (nfine > std::max<int64_t>(int64_t(1) << 16, 16 * S.n) || nfine > (int64_t(1) << 30))
-        return SPH_OK;
-    const int64_t ncol = (int64_t)ncx * ncy;
-    const int64_t ncl_max = S.n / 8 + ncol + 1;
-    if (8 * ncl_max > (int64_t(1) << 30)) return SPH_OK;
-    // list capacity: the j-halves in the box of an i-cluster grown by the reach
-    const double rho_n = (double)S.n / vol;
-    const double R = rc + std::max(drift[0], std::max(drift[1], drift[2]));
-    const double hz = 8.0 / (rho_n * wx * wy) + gz;
-    const double box = (2 * wx + 2 * R) * (2 * wy + 2 * R) * (2 * hz + 2 * R);
-    // before any measurement 2.6 times the mean list length of a uniform
-    // fluid; afterwards what the longest list measured needs (cluster_measure)
-    const int per = e->cl_need > 0
-                        ? e->cl_need
-                        : (int)std::min(65536.0, std::max(64.0, std::ceil(rho_n * box / 4.0)));
+    if (nfine > (int64_t(1) << 30) || 8 * ncl_max > (int64_t(1) << 30)) return SPH_OK;
+    // afterwards what the longest list measured needs (cluster_measure)
+    const int per = e->cl_need > 0 ? e->cl_need : (int)std::min(65536.0, per_est);
     const long long cap = (long long)per * ncl_max;
-    if (S.n > e->cl_np || nfine > e->cl_fine || ncol > e->cl_col || ncl_max > e->cl_ncl ||
-        cap > e->cl_ent || (long long)e->cl_ent < (long long)per * e->cl_ncl) {
+    if (np > e->cl_np || nfine > e->cl_fine || ncol > e->cl_col || ncl_max > e->cl_ncl ||
+        cap > e->cl_ent) {
         cluster_free(e);
-        const int64_t np = std::max<int64_t>(S.n, 1);
         const int64_t scan = std::max(nfine, ncol) / 4096 + 2;
         TRY(dalloc(&c.fcount, nfine));
         TRY(dalloc(&c.fstart, nfine + 1));
@@ -479,6 +503,8 @@ int cluster_setup(sph_engine *e) {
         TRY(dalloc(&c.scan_tmp, scan));
         TRY(dalloc(&c.colcnt, ncol));
         TRY(dalloc(&c.colcl, ncol + 1));
+        TRY(dalloc(&c.colsim, ncol));
+        TRY(dalloc(&c.csim, ncl_max));
         TRY(dalloc(&c.slot_idx, 8 * ncl_max));
         TRY(dalloc(&c.slot_of, np));
         TRY(dalloc(&c.cref, ncl_max));
@@ -500,21 +526,25 @@ int cluster_setup(sph_engine *e) {
         e->cl_ncl = ncl_max;
         e->cl_ent = cap;
     }
-    c.sim = sid;
-    c.ncx = ncx;
-    c.ncy = ncy;
-    c.nslab = nslab;
+    if (!e->cl_geom_d || e->cl_geom_cap < e->cap_s) {
+        cudaFree(e->cl_geom_d);
+        e->cl_geom_d = nullptr;
+        TRY(dalloc(&e->cl_geom_d, e->cap_s));
+        e->cl_geom_cap = e->cap_s;
+    }
+    CK(cudaMemcpy(e->cl_geom_d, geom.data(), sizeof(ClGeom) * e->cap_s, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c.colsim, colsim.data(), sizeof(int) * ncol, cudaMemcpyHostToDevice));
+    c.geom = e->cl_geom_d;
+    c.sim1 = -1;
+    memset(&c.g1, 0, sizeof(ClGeom));
+    if (e->one_sim)
+        for (int sid = 0; sid < (int)e->sims.size(); ++sid)
+            if (e->sims[sid].active) {
+                c.sim1 = sid;
+                c.g1 = geom[sid];
+            }
     c.ncol = (int)ncol;
     c.nfine = (int)nfine;
-    c.rx = rx;
-    c.ry = ry;
-    c.wxd = wx;
-    c.wyd = wy;
-    c.gzd = gz;
-    c.wx = (float)wx;
-    c.wy = (float)wy;
-    c.gz = (float)gz;
-    for (int a = 0; a < 3; ++a) c.drift2[a] = (float)drift[a];
     c.ncl_max = (int)ncl_max;
     c.slots_max = (int)(8 * ncl_max);
     c.lstride = per;
@@ -1170,6 +1200,8 @@ void free_all(sph_engine *e) {
     for (void *p : cp)
         if (p) cudaFree(p);
     cluster_free(e);
+    if (e->cl_geom_d) cudaFree(e->cl_geom_d);
+    e->cl_geom_d = nullptr;
     if (e->cl_fill_host) cudaFreeHost(e->cl_fill_host);
     if (e->cl_fill_ev) cudaEventDestroy(e->cl_fill_ev);
     e->cl_fill_host = nullptr;

@@ -151,30 +151,41 @@ struct CollideSet {
     int *info;                      // [4]: count, overflow, max level, solver status
 };
 
-// Cluster-pair scheme (tuning.pair_scheme = 1, sph_cluster.cu): one
+// Cluster-pair scheme (tuning.pair_scheme = 1, sph_cluster.cu): each 3D
 // simulation's particles are binned into columns (x, y) of about eight
 // particles' width and thin z slabs, ordered by slab within a column and cut
 // into clusters of 8 consecutive particles (padded slots at a column's end).
 // Each cluster keeps its positions relative to a lattice point of its own
 // (column centre, slab floor), so a cluster pair's shift is an integer
 // lattice offset.  A list per i-cluster (8 particles) names the j-clusters
-// (halves of 4) whose bounding boxes lie within the cutoff plus the allowed
-// drift; a warp evaluates 8 i x 4 j pairs per list entry.  Lists live in
-// fixed regions of lstride entries, built in one pass.
-struct ClusterSet {
-    int on;                       // the scheme runs for this layout
-    int sim;                      // the simulation's slot
-    int ncx, ncy, nslab, ncol, nfine;
+// (halves of 4) of the same simulation whose bounding boxes lie within the
+// cutoff plus the allowed drift; a warp evaluates 8 i x 4 j pairs per list
+// entry.  Lists live in fixed regions of lstride entries, built in one pass.
+// Per simulation: its lattice and its ranges in the flattened column and
+// fine-cell tables.
+struct ClGeom {
+    int ncx, ncy, nslab;          // columns per axis, slabs per column
     int rx, ry;                   // +-columns searched per axis
+    int col_off, fine_off;        // first column / fine cell of the simulation
     float wx, wy, gz;             // lattice steps
     double wxd, wyd, gzd;
     float drift2[3];              // twice the allowed drift per axis (list margin)
+};
+
+struct ClusterSet {
+    int on;                       // the scheme runs for this layout
+    int ncol, nfine;              // columns / fine cells of all simulations
     int ncl_max, slots_max;
     int lstride;                  // list entries reserved per i-cluster
+    const ClGeom *geom;           // [simulation slots]
+    ClGeom g1;                    // an engine with one simulation: its lattice,
+    int sim1;                     // and its slot, as kernel parameters
+    int *colsim;                  // [ncol] simulation of each column
+    int *csim;                    // [ncl_max] simulation of each cluster
     int *fcount, *fstart, *fkey, *frank, *ford, *scan_tmp;
     int *colcnt, *colcl;          // [ncol + 1]: clusters per column, prefix
     int *slot_idx, *slot_of;      // slot -> sorted index (-1 padding), inverse
-    int4 *cref;                   // per cluster {kx, ky, kz, column}
+    int4 *cref;                   // per cluster {kx, ky, kz, global column}
     float4 *ibox, *jbox;          // bounding boxes (lo, hi) of clusters / halves
     int *lnear, *lfar;            // [ncl_max] entries within / beyond the short
                                   // support: the near ones from the front of the

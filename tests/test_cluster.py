@@ -143,26 +143,26 @@ def test_cluster_scheme_with_binning_on_demand_and_thermostat():
     assert rel_l2(uu, uo) < MIXED_TOL
 
 
-@pytest.mark.parametrize("what", ["2d", "fp64", "two_sims", "small_box"])
+@pytest.mark.parametrize("what", ["2d", "fp64", "small_box_with_another"])
 def test_cell_scheme_runs_where_clusters_do_not_apply(what):
-    """pair_scheme = 1 leaves a 2D engine, an FP64 engine, an engine with two
-    simulations and a box narrower than five columns on the cell scheme: the
-    same launches and the same bits as pair_scheme = 0."""
+    """pair_scheme = 1 leaves a 2D engine, an FP64 engine and an engine one
+    of whose simulations has a box narrower than five columns on the cell
+    scheme: the same launches and the same bits as pair_scheme = 0."""
     precision = "mixed"
     if what == "2d":
         prm, r, v, m, T0 = workloads.config_2d(48, 3130)
-    elif what == "small_box":
-        prm, r, v, m, T0 = workloads.config_3d(12, 3131)
     else:
         prm, r, v, m, T0 = workloads.config_3d(20, 3132)
         precision = "fp64" if what == "fp64" else "mixed"
     u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
+    small = workloads.config_3d(12, 3131)
     res = []
     for scheme in (0, 1):
         e, s = engine(prm, r, v, m, u, scheme, precision=precision, cap=2)
         with e:
-            if what == "two_sims":
-                e.add(prm, r, v, m, u)
+            if what == "small_box_with_another":
+                ps, rs, vs, ms, Ts = small
+                e.add(ps, rs, vs, ms, workloads.vdw_energy(np.full(len(rs), 0.7), Ts))
             e.advance(3)
             e.sync()
             res.append((e.kernels_per_step(), e.get_state(s)))
@@ -339,3 +339,55 @@ def test_cluster_scheme_in_a_rectangular_box():
     assert kps[1] != kps[0]
     ro, vo, uo, _ = oracle.advance(prm, r, v, m, u, 3)
     assert rel_l2(rr, ro) < MIXED_TOL and rel_l2(uu, uo) < MIXED_TOL
+
+
+def batch_of_3d():
+    """Three 3D fluids of different size, density and temperature (the same
+    kernel and flags: one engine group)."""
+    sims = []
+    for side, dens, T, seed in ((20, 0.7, 0.6, 3180), (24, 0.55, 0.9, 3181), (18, 0.8, 0.5, 3182)):
+        prm, r, v, m, T0 = workloads.config_3d(side, seed, density=dens, integrator="rk4")
+        sims.append((prm, r, v, m, with_gradient(prm, r, v, m, T)))
+    return sims
+
+
+def test_cluster_scheme_batched_equals_alone():
+    """Each simulation's columns, clusters and lists are its own, and its
+    sums follow them alone: a simulation gives the same bits in a batch of
+    three as alone."""
+    sims = batch_of_3d()
+    total = sum(len(x[1]) for x in sims)
+    with Engine(sims[0][0], "mixed", max_particles=total, max_sims=3) as e:
+        ids = [e.add(*x) for x in sims]
+        e.set_tuning(pair_scheme=1, steps_per_graph=4)
+        ks = e.kernels_per_step()
+        e.advance(8)
+        e.sync()
+        batched = [e.get_state(i) for i in ids]
+    with Engine(sims[0][0], "mixed", max_particles=total, max_sims=3) as e0:
+        for x in sims:
+            e0.add(*x)
+        assert e0.kernels_per_step() != ks           # the cluster passes ran
+    for x, got in zip(sims, batched):
+        e, s = engine(*x, 1, steps_per_graph=4)
+        with e:
+            e.advance(8)
+            e.sync()
+            alone = e.get_state(s)
+        for a, b in zip(got, alone):
+            assert np.array_equal(a, b)
+
+
+def test_cluster_scheme_batch_matches_oracle():
+    sims = batch_of_3d()
+    total = sum(len(x[1]) for x in sims)
+    with Engine(sims[0][0], "mixed", max_particles=total, max_sims=3) as e:
+        ids = [e.add(*x) for x in sims]
+        e.set_tuning(pair_scheme=1)
+        derivs = [e.derivatives(i) for i in ids]
+        e.sync()
+        assert e.last_pair_total() == sum(oracle.derivatives(*x)["nip"] for x in sims)
+    for x, d in zip(sims, derivs):
+        ref = oracle.derivatives(*x)
+        for k in ("rho", "vdot", "udot"):
+            assert rel_l2(d[k], ref[k]) < MIXED_TOL, k
