@@ -2,9 +2,9 @@
 
 Knobs (struct sph_tuning): threads per block of the pair passes, the
 cell-edge / cutoff ratio (1 -> cells of the cutoff and a 3^d window, 1/2 ->
-5^d, 1/3 -> 7^d, cells beyond the cutoff culled per particle) and, for a
-single 3D simulation in mixed precision, the pair scheme (cell windows or
-cluster pairs; the cluster scheme has its own fixed launch shape).  A candidate is
+5^d, 1/3 -> 7^d, cells beyond the cutoff culled per particle) and, for 3D
+simulations in mixed precision, the pair scheme (cell windows or cluster
+pairs; the cluster scheme has its own fixed launch shape).  A candidate is
 timed with CUDA events over a few graph-captured steps on a clone of the
 simulations (same parameters, same current states), so tuning neither
 advances the live simulations nor shifts their thermostat schedules.  Results
@@ -30,10 +30,9 @@ def signature(group, precision, counts):
 
 
 def cluster_candidate(group, precision, sims):
-    """Whether the cluster-pair scheme can apply: one 3D simulation in mixed
-    precision without collisions (the engine itself checks the box)."""
-    return (group.dim == 3 and precision == "mixed" and len(sims) == 1
-            and group.collision == 0)
+    """Whether the cluster-pair scheme can apply: 3D simulations in mixed
+    precision without collisions (the engine itself checks the boxes)."""
+    return group.dim == 3 and precision == "mixed" and group.collision == 0
 
 
 def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream, scheme=0):

@@ -205,8 +205,8 @@ class Engine:
         """block_size, use_graph, steps_per_graph, cell_ratio, rebin (1: bin
         into cells only when a particle has used half of the cell slack,
         VerletList.ponder_rebuild's skin reuse; 0: every step) and
-        pair_scheme (0: cell windows; 1: cluster pairs, for one 3D
-        simulation in mixed precision without collisions)."""
+        pair_scheme (0: cell windows; 1: cluster pairs, for 3D simulations
+        in mixed precision without collisions)."""
         cur = self.tuning
         cur.update(kw)
         t = SphTuning(block_size=int(cur["block_size"]), use_graph=int(cur["use_graph"]),

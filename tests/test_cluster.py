@@ -1,6 +1,6 @@
-"""The cluster-pair scheme (tuning pair_scheme = 1): one 3D simulation in
-mixed precision, its pairs evaluated as 8 x 4 blocks of compact particle
-clusters from box-culled lists.  The pair set is the reference's exact set
+"""The cluster-pair scheme (tuning pair_scheme = 1): 3D simulations in
+mixed precision, their pairs evaluated as 8 x 4 blocks of compact particle
+clusters from box-culled lists of each simulation.  The pair set is the reference's exact set
 (neighbour_list.py:168-178), the results meet the mixed-precision bounds
 against the FP64 oracle like the cell-window scheme, runs are deterministic,
 and the cell scheme runs wherever the cluster scheme does not apply."""
