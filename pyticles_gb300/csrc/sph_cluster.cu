@@ -51,6 +51,10 @@ __global__ void k_cl_key(const __grid_constant__ View v, const __grid_constant__
     if (i >= v.np) return;
     const int sim = v.b_sim[i];
     const SimDev &S = v.sims[sim];
+    if (!S.cl_on) {   // on the cell-window passes
+        c.fkey[i] = -1;
+        return;
+    }
     const ClGeom &g = c.geom[sim];
     const double step[3] = {g.wxd, g.wyd, g.gzd};
     const int nk[3] = {g.ncx, g.ncy, g.nslab};
@@ -71,7 +75,9 @@ __global__ void k_cl_key(const __grid_constant__ View v, const __grid_constant__
 __global__ void k_cl_scatter(const __grid_constant__ View v, const __grid_constant__ ClusterSet c) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.np) return;
-    const int dst = c.fstart[c.fkey[i]] + c.frank[i];
+    const int key = c.fkey[i];
+    if (key < 0) return;
+    const int dst = c.fstart[key] + c.frank[i];
     if (SPH_IN_BOUNDS(dst >= 0 && dst < v.np, v.err_any)) c.ford[dst] = i;
 }
 
@@ -108,7 +114,7 @@ __global__ void k_cl_cols(const __grid_constant__ ClusterSet c) {
 
 __global__ void k_cl_slots(const __grid_constant__ View v, const __grid_constant__ ClusterSet c) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= v.np) return;
+    if (p >= c.fstart[c.nfine]) return;   // the particles on cluster pairs
     const int i = c.ford[p];
     const int sim = v.b_sim[i];
     const ClGeom &g = c.geom[sim];

@@ -121,6 +121,8 @@ struct sph_engine {
     unsigned long long *bin_count = nullptr;
     bool bins_valid = false;       // B, its packed copies and the cells match A
     bool one_sim = false;          // exactly one live simulation (one_dev)
+    int n_cell_sims = 0;           // live simulations on the cell-window passes
+    bool cl_disabled = false;      // cluster lists did not fit: cell passes only
     SimDev one_dev;
     ClusterSet cl = {};            // tuning.pair_scheme = 1 (sph_cluster.cu)
     ClGeom *cl_geom_d = nullptr;   // per simulation slot
@@ -416,17 +418,19 @@ void cluster_free(sph_engine *e) {
     e->cl_ent = 0;
 }
 
-// Cluster geometry of every live 3D simulation (tuning.pair_scheme = 1):
+// Cluster geometry of the live 3D simulations (tuning.pair_scheme = 1):
 // columns about 8 particles wide (the cube root of the volume of 8 at the
 // simulation's mean density), slabs a quarter of that, the column reach of
 // the cutoff plus twice the allowed drift, each simulation's range in the
-// flattened column and fine-cell tables, and the buffers.  Leaves c.on = 0
-// (the cell scheme runs) where the scheme does not apply to every
-// simulation.
-int cluster_setup(sph_engine *e) {
+// flattened column and fine-cell tables, and the buffers.  A simulation whose
+// box is too narrow for the columns stays on the cell-window passes (the
+// choice depends on the simulation alone); sd[s].cl_on marks the others.
+// c.on = 0 if none runs on cluster pairs.
+int cluster_setup(sph_engine *e, std::vector<SimDev> &sd) {
     ClusterSet &c = e->cl;
     c.on = 0;
-    if (e->tune.pair_scheme != 1 || e->dim != 3 || e->precision != SPH_MIXED ||
+    for (auto &d : sd) d.cl_on = 0;
+    if (e->tune.pair_scheme != 1 || e->cl_disabled || e->dim != 3 || e->precision != SPH_MIXED ||
         e->group.collision != SPH_COLLIDE_OFF || e->np_b < 8)
         return SPH_OK;
     std::vector<ClGeom> geom(e->cap_s);
@@ -436,8 +440,8 @@ int cluster_setup(sph_engine *e) {
     for (int sid = 0; sid < (int)e->sims.size(); ++sid) {
         const Sim &S = e->sims[sid];
         memset(&geom[sid], 0, sizeof(ClGeom));
-        if (!S.active) continue;
-        const SimDev d = make_simdev(e, S);
+        if (!S.active || S.n < 8) continue;
+        const SimDev &d = sd[sid];
         const double *L = S.prm.box;
         const double vol = L[0] * L[1] * L[2];
         const double wt = std::cbrt(8.0 * vol / (double)S.n);
@@ -447,18 +451,21 @@ int cluster_setup(sph_engine *e) {
         const double wx = L[0] / ncx, wy = L[1] / ncy, gz = L[2] / nslab;
         const double rc = std::sqrt(d.thr);
         double drift[3];
+        bool fits = true;
         for (int a = 0; a < 3; ++a) {
             drift[a] = 2.0 * d.slack_half[a];
-            if (!(drift[a] < 0.25 * L[a])) return SPH_OK;   // single-cell axis or no slack room
+            fits &= drift[a] < 0.25 * L[a];   // not a single-cell axis, slack room
         }
+        if (!fits) continue;
         // a column dx over lies at least (|dx| - 1) widths away
         const int rx = (int)std::ceil((rc + drift[0] + 1e-3) / wx);
         const int ry = (int)std::ceil((rc + drift[1] + 1e-3) / wy);
         // every column and every z image within reach must be distinct
-        if (2 * rx + 1 > ncx || 2 * ry + 1 > ncy || rx > 100 || ry > 100) return SPH_OK;
-        if (L[2] < 2.0 * (rc + drift[2]) + 4.0 * gz || nslab > 30000) return SPH_OK;
+        if (2 * rx + 1 > ncx || 2 * ry + 1 > ncy || rx > 100 || ry > 100) continue;
+        if (L[2] < 2.0 * (rc + drift[2]) + 4.0 * gz || nslab > 30000) continue;
         const int64_t sfine = (int64_t)ncx * ncy * nslab;
-        if (sfine > std::max<int64_t>(int64_t(1) << 16, 16 * S.n)) return SPH_OK;
+        if (sfine > std::max<int64_t>(int64_t(1) << 16, 16 * S.n)) continue;
+        sd[sid].cl_on = 1;
         ClGeom &g = geom[sid];
         g.ncx = ncx;
         g.ncy = ncy;
@@ -487,26 +494,33 @@ int cluster_setup(sph_engine *e) {
         const double box = (2 * wx + 2 * R) * (2 * wy + 2 * R) * (2 * hz + 2 * R);
         per_est = std::max(per_est, std::ceil(rho_n * box / 4.0));
     }
-    if (nfine > (int64_t(1) << 30) || 8 * ncl_max > (int64_t(1) << 30)) return SPH_OK;
+    if (ncol == 0 || nfine > (int64_t(1) << 30) || 8 * ncl_max > (int64_t(1) << 30)) {
+        for (auto &d : sd) d.cl_on = 0;
+        return SPH_OK;
+    }
     // afterwards what the longest list measured needs (cluster_measure)
     const int per = e->cl_need > 0 ? e->cl_need : (int)std::min(65536.0, per_est);
     const long long cap = (long long)per * ncl_max;
-    if (np > e->cl_np || nfine > e->cl_fine || ncol > e->cl_col || ncl_max > e->cl_ncl ||
+    // fkey, frank and slot_of are indexed by the particle's place in the
+    // engine's sorted order, so they hold every live particle, not only the
+    // simulations on cluster pairs
+    const int64_t nall = std::max<int64_t>(e->np_b, np);
+    if (nall > e->cl_np || nfine > e->cl_fine || ncol > e->cl_col || ncl_max > e->cl_ncl ||
         cap > e->cl_ent) {
         cluster_free(e);
         const int64_t scan = std::max(nfine, ncol) / 4096 + 2;
         TRY(dalloc(&c.fcount, nfine));
         TRY(dalloc(&c.fstart, nfine + 1));
-        TRY(dalloc(&c.fkey, np));
-        TRY(dalloc(&c.frank, np));
-        TRY(dalloc(&c.ford, np));
+        TRY(dalloc(&c.fkey, nall));
+        TRY(dalloc(&c.frank, nall));
+        TRY(dalloc(&c.ford, nall));
         TRY(dalloc(&c.scan_tmp, scan));
         TRY(dalloc(&c.colcnt, ncol));
         TRY(dalloc(&c.colcl, ncol + 1));
         TRY(dalloc(&c.colsim, ncol));
         TRY(dalloc(&c.csim, ncl_max));
         TRY(dalloc(&c.slot_idx, 8 * ncl_max));
-        TRY(dalloc(&c.slot_of, np));
+        TRY(dalloc(&c.slot_of, nall));
         TRY(dalloc(&c.cref, ncl_max));
         TRY(dalloc(&c.ibox, 2 * ncl_max));
         TRY(dalloc(&c.jbox, 4 * ncl_max));
@@ -520,7 +534,7 @@ int cluster_setup(sph_engine *e) {
         TRY(dalloc(&c.crho, 8 * ncl_max));
         TRY(dalloc(&c.maxfill, 1));
         CK(cudaMemset(c.maxfill, 0, sizeof(int)));
-        e->cl_np = np;
+        e->cl_np = nall;
         e->cl_fine = nfine;
         e->cl_col = ncol;
         e->cl_ncl = ncl_max;
@@ -724,14 +738,18 @@ int relayout(sph_engine *e) {
         if (s < (int)e->sims.size()) sd[s] = make_simdev(e, e->sims[s]);
         else memset(&sd[s], 0, sizeof(SimDev));
     }
-    CK(cudaMemcpyAsync(e->sims_d, sd.data(), sizeof(SimDev) * e->cap_s, cudaMemcpyHostToDevice, st));
     // a single live simulation: its constants travel as kernel parameters
     int live = 0, last = -1;
     for (int s = 0; s < (int)e->sims.size(); ++s)
         if (e->sims[s].active) ++live, last = s;
     e->one_sim = live == 1;
+    // marks the simulations that run on cluster pairs (SimDev.cl_on)
+    TRY(cluster_setup(e, sd));
+    e->n_cell_sims = 0;
+    for (int s = 0; s < (int)e->sims.size(); ++s)
+        if (e->sims[s].active && !sd[s].cl_on) ++e->n_cell_sims;
     if (e->one_sim) e->one_dev = sd[last];
-    TRY(cluster_setup(e));
+    CK(cudaMemcpyAsync(e->sims_d, sd.data(), sizeof(SimDev) * e->cap_s, cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
     free_graph(e);
     e->layout_dirty = false;
@@ -815,9 +833,12 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
         v.reuse = 1;
         v.rebin_gate = e->rebin_gate;
     }
+    const bool cells = e->n_cell_sims > 0;
     if (e->cl.on) {
-        // cluster pairs: build at the step's first evaluation, repack at the
-        // later ones; the rates pass leaves the stage update to k_integrate
+        // the simulations on cluster pairs: build at the step's first
+        // evaluation, repack at the later ones; their rates pass leaves the
+        // stage update to k_integrate.  The cell-window passes below skip
+        // them (SimDev.cl_on) and run only if some simulation remains.
         const ClusterSet &c = e->cl;
         const int kern = e->group.kernel;
         if (s == 0) {
@@ -828,10 +849,12 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
             ProfScope ps(e, SPH_PASS_DENSITY, st);
             if (s > 0) launch_cluster_pack(v, c, s, st);
             launch_cluster_density(v, c, kern, s, st);
+            if (cells) launch_density(v, e->precision, kern, s, e->tune.block_size, st);
         }
         if (e->group.heat_flux) {
             ProfScope ps(e, SPH_PASS_HEAT, st);
             launch_cluster_heat(v, c, kern, st);
+            if (cells) launch_heat(v, e->precision, kern, e->tune.block_size, st);
         }
         if (mode == 1 && s == e->nstage - 1 && e->any_thermostat) {
             ProfScope ps(e, SPH_PASS_TSUM, st);
@@ -840,7 +863,10 @@ void enqueue_stage(sph_engine *e, int s, int mode, cudaStream_t st) {
         {
             ProfScope ps(e, SPH_PASS_FORCE, st);
             launch_cluster_force(v, c, kern, e->group.viscosity, e->group.heat_flux, st);
-            if (mode == 1) launch_integrate(v, e->precision, e->group.integrator, s, st);
+            if (mode == 1) launch_integrate(v, e->precision, e->group.integrator, s, st, 1);
+            if (cells)
+                launch_force(v, e->precision, kern, e->group.viscosity, e->group.heat_flux,
+                             e->group.integrator, s, mode, e->tune.block_size, st);
         }
         return;
     }
@@ -915,9 +941,11 @@ int cluster_measure(sph_engine *e) {
         st_alloc = dalloc(&c.ent, (int64_t)need * c.ncl_max);
     }
     if (st_alloc != SPH_OK) {
-        // no room for the lists: this layout runs on the cell scheme
+        // no room for the lists: the layout is rebuilt on the cell scheme
         c.on = 0;
         e->cl_ent = 0;
+        e->cl_disabled = true;
+        e->layout_dirty = true;
         return SPH_OK;
     }
     c.lstride = need;
@@ -936,6 +964,7 @@ int cluster_check(sph_engine *e) {
         if (*e->cl_fill_host > 0.8 * c.lstride) e->cl_stale = true;
     }
     if (e->cl_stale) TRY(cluster_measure(e));
+    if (e->layout_dirty) TRY(relayout(e));   // the lists did not fit
     return SPH_OK;
 }
 
@@ -959,9 +988,11 @@ int cluster_note_fill(sph_engine *e) {
 int64_t kernels_per_step(const sph_engine *e) {
     if (e->cl.on) {
         // cluster build; per evaluation density, [heat,] force and the stage
-        // update; the later evaluations' repacking
+        // update; the later evaluations' repacking; the cell-window passes of
+        // the other simulations
         int64_t k = kSortKernels + cluster_build_kernels();
         k += (int64_t)e->nstage * (3 + (e->group.heat_flux ? 1 : 0)) + (e->nstage - 1);
+        if (e->n_cell_sims > 0) k += (int64_t)e->nstage * (2 + (e->group.heat_flux ? 1 : 0));
         if (e->any_thermostat) k += 2;
         if (rebin_on_demand(e)) k += 2;
         return k;
@@ -1556,10 +1587,17 @@ int sph_sim_pair_count(sph_engine *e, int32_t id, int64_t *nip) {
     TRY(check_sim(e, id));
     TRY(ensure_layout(e));
     cudaStream_t st = e->stream;
-    enqueue_prepare(e, st);
-    View v = make_view(e);
-    stage_view(e, v, 0);
-    launch_density(v, e->precision, e->group.kernel, 0, e->tune.block_size, st);
+    if (e->cl.on) {
+        // simulations on cluster pairs count in the cluster density pass
+        TRY(cluster_check(e));
+        enqueue_prepare(e, st);
+        enqueue_stage(e, 0, 0, st);
+    } else {
+        enqueue_prepare(e, st);
+        View v = make_view(e);
+        stage_view(e, v, 0);
+        launch_density(v, e->precision, e->group.kernel, 0, e->tune.block_size, st);
+    }
     unsigned long long c = 0;
     CK(cudaMemcpyAsync(&c, e->pair_count + id, sizeof(c), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1693,7 +1731,10 @@ int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
         t->steps_per_graph < 1 || (t->pair_scheme != 0 && t->pair_scheme != 1))
         return SPH_EINVAL;
     bool regrid = t->cell_ratio != e->tune.cell_ratio;
-    if (t->pair_scheme != e->tune.pair_scheme) e->layout_dirty = true;
+    if (t->pair_scheme != e->tune.pair_scheme) {
+        e->layout_dirty = true;
+        e->cl_disabled = false;
+    }
     e->tune = *t;
     e->tune.reserved = 0;
     free_graph(e);

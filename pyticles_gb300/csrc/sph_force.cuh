@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
     const T4 *__restrict__ Q = (const T4 *)v.pk_q;
     const int s = v.b_sim[ii];
     const SimDev &S = ONE ? v.one : v.sims[s];
+    if (S.cl_on) return;   // evaluated (and integrated) by the cluster passes
     KConst<R> ks = make_kconst<R>(S, 0);
     KConst<R> kl = make_kconst<R>(S, 1);
     const SimConst<R> &sc = sconst<R>(S);
@@ -276,12 +277,12 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
 // of its own, for steps whose velocities change between the force pass and
 // the update (hard collisions).
 template <typename R, int D>
-__global__ void __launch_bounds__(256) k_integrate(View v, int stage, int integ) {
+__global__ void __launch_bounds__(256) k_integrate(View v, int stage, int integ, int cl_only) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.np) return;
     const int s = v.b_sim[i];
     const SimDev &S = v.sims[s];
-    if (!S.active) return;
+    if (!S.active || (cl_only && !S.cl_on)) return;
     R vdr[3] = {0, 0, 0};
     for (int a = 0; a < D; ++a) vdr[a] = ((const R *)v.vdot[a])[i];
     integrate_stage<R, D>(v, S, i, s, stage, integ, vdr, ((const R *)v.udot)[i]);
@@ -315,11 +316,11 @@ void launch_force_t(const View &v, int kernel, int viscosity, int heat, int inte
 }
 
 template <typename R>
-void launch_integrate_t(const View &v, int integrator, int stage, cudaStream_t s) {
+void launch_integrate_t(const View &v, int integrator, int stage, cudaStream_t s, int cl_only) {
     if (v.np <= 0) return;
     int nb = (v.np + 255) / 256;
-    if (v.dim == 2) k_integrate<R, 2><<<nb, 256, 0, s>>>(v, stage, integrator);
-    else k_integrate<R, 3><<<nb, 256, 0, s>>>(v, stage, integrator);
+    if (v.dim == 2) k_integrate<R, 2><<<nb, 256, 0, s>>>(v, stage, integrator, cl_only);
+    else k_integrate<R, 3><<<nb, 256, 0, s>>>(v, stage, integrator, cl_only);
 }
 
 }  // namespace sph

@@ -6,10 +6,10 @@ namespace sph {
 
 extern template void launch_force_t<double>(const View &, int, int, int, int, int, int, int,
                                             cudaStream_t);
-extern template void launch_integrate_t<double>(const View &, int, int, cudaStream_t);
+extern template void launch_integrate_t<double>(const View &, int, int, cudaStream_t, int);
 template void launch_force_t<float>(const View &, int, int, int, int, int, int, int,
                                     cudaStream_t);
-template void launch_integrate_t<float>(const View &, int, int, cudaStream_t);
+template void launch_integrate_t<float>(const View &, int, int, cudaStream_t, int);
 
 void launch_force(const View &v, int precision, int kernel, int viscosity, int heat,
                   int integrator, int stage, int mode, int block, cudaStream_t s) {
@@ -19,9 +19,10 @@ void launch_force(const View &v, int precision, int kernel, int viscosity, int h
         launch_force_t<double>(v, kernel, viscosity, heat, integrator, stage, mode, block, s);
 }
 
-void launch_integrate(const View &v, int precision, int integrator, int stage, cudaStream_t s) {
-    if (precision == SPH_MIXED) launch_integrate_t<float>(v, integrator, stage, s);
-    else launch_integrate_t<double>(v, integrator, stage, s);
+void launch_integrate(const View &v, int precision, int integrator, int stage, cudaStream_t s,
+                      int cl_only) {
+    if (precision == SPH_MIXED) launch_integrate_t<float>(v, integrator, stage, s, cl_only);
+    else launch_integrate_t<double>(v, integrator, stage, s, cl_only);
 }
 
 }  // namespace sph

@@ -5,6 +5,6 @@ namespace sph {
 
 template void launch_force_t<double>(const View &, int, int, int, int, int, int, int,
                                      cudaStream_t);
-template void launch_integrate_t<double>(const View &, int, int, cudaStream_t);
+template void launch_integrate_t<double>(const View &, int, int, cudaStream_t, int);
 
 }  // namespace sph

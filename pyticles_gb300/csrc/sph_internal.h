@@ -62,6 +62,8 @@ struct SimDev {
     double T0, T1;          // thermostat ramp ends
     long long ramp;
     int coll_on;            // hard collisions after each evaluation
+    int cl_on;              // the pair passes run on cluster pairs (sph_cluster.cu);
+                            // the cell-window passes skip this simulation
     int coll_win[3];        // +-cells searched for collision partners
     double coll_c2;         // collision_cutoff^2 (Force.cutoffsq, forces.py:33)
     SimConst<float> cf;
@@ -226,8 +228,10 @@ void launch_collide_levels(const CollideSet &c, cudaStream_t s);
 void launch_collide_apply(const CollideSet &c, int dim, Vec3Ref vel, Vec3Ref pos,
                           const double *m, double push_cut, void *pk_vel, int precision,
                           int *err, int *err_any, int nsims, cudaStream_t s);
-// Engine path: the integrator stage from the stored rates (collisions on).
-void launch_integrate(const View &v, int precision, int integrator, int stage, cudaStream_t s);
+// Engine path: the integrator stage from the stored rates (collisions on;
+// with cl_only, the simulations on cluster pairs alone).
+void launch_integrate(const View &v, int precision, int integrator, int stage, cudaStream_t s,
+                      int cl_only = 0);
 
 // ---- launch wrappers (sph_sort.cu) ----
 void launch_bin(const View &v, int np_a, cudaStream_t s);

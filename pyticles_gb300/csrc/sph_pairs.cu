@@ -21,6 +21,7 @@ __global__ void __launch_bounds__(256, ONE ? 5 : 4) k_density(const __grid_const
     const T4 *__restrict__ P = (const T4 *)v.pk_pos_in;
     const int s = v.b_sim[ii];
     const SimDev &S = ONE ? v.one : v.sims[s];
+    if (S.cl_on) return;   // evaluated by the cluster passes
     KConst<R> ks = make_kconst<R>(S, 0);
     KConst<R> kl = make_kconst<R>(S, 1);
     BAcc<R> rs, rl;
@@ -95,6 +96,7 @@ __global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v)
     const T4 *__restrict__ F = (const T4 *)v.pk_f;
     const int s = v.b_sim[ii];
     const SimDev &S = ONE ? v.one : v.sims[s];
+    if (S.cl_on) return;   // evaluated by the cluster passes
     KConst<R> ks = make_kconst<R>(S, 0);
     const T4 fi = F[ii];
     BAcc<R> q[3];

@@ -37,12 +37,18 @@ from .workloads import lattice_system, rng_for, vdw_energy
 # ids and sort scratch, seven packed vectors (positions and velocities of two
 # stages, force factors, heat factors, the force pass's neighbour record),
 # staging.
-def bytes_per_particle(precision="mixed", integrator="ieuler"):
+def bytes_per_particle(precision="mixed", integrator="ieuler", cluster=False):
     rs = 4 if precision == "mixed" else 8
     v4 = 4 * rs
     b = 3 * 8 * 8 + 9 * rs + 5 * 8 + 9 * 4 + 7 * v4 + 10 * rs + 8 * 8
     if integrator == "rk4":
         b += 7 * 8
+    if cluster and precision == "mixed":
+        # cluster pairs (csrc/sph_cluster.cu): slot records (72 B a slot),
+        # sort scratch (16 B), cluster boxes and references (16 B), and the
+        # lists: 1.25 times the longest, about 370 entries of 8 B per cluster
+        # of 8 in a fluid at n = 0.7 (denser fluids need proportionally more)
+        b += 72 + 16 + 16 + 400
     return b
 
 
@@ -116,13 +122,13 @@ class Group:
     """One engine (one dimension group) and its jobs."""
 
     def __init__(self, dim, params, capacity, max_sims, precision, chunk, engine_factory,
-                 stream):
+                 stream, pair_scheme=0):
         self.dim = dim
         self.capacity = int(capacity)
         self.max_sims = max_sims
         self.chunk = chunk
         self.engine = engine_factory(params, precision, self.capacity, max_sims, stream)
-        self.engine.set_tuning(steps_per_graph=chunk, use_graph=1)
+        self.engine.set_tuning(steps_per_graph=chunk, use_graph=1, pair_scheme=pair_scheme)
         self.active = {}          # sim id -> job
         self.live = 0
         self.peak = 0
@@ -207,19 +213,24 @@ class Server:
 
     def __init__(self, hbm_budget_bytes, precision="mixed", chunk=25, max_sims=256,
                  share_2d=0.6, engine_factory=default_engine_factory, clock=time.perf_counter,
-                 streams=None, group_params=None):
+                 streams=None, group_params=None, pair_scheme_3d=1):
+        """pair_scheme_3d: the 3D group's pair scheme (1: cluster pairs, whose
+        tables and lists count against the group's share of the budget)."""
         self.precision = precision
         self.chunk = chunk
         self.clock = clock
         self.hbm_budget = float(hbm_budget_bytes)
-        bpp = bytes_per_particle(precision)
-        caps = {2: hbm_budget_bytes * share_2d / bpp, 3: hbm_budget_bytes * (1 - share_2d) / bpp}
+        self.bpp = {2: bytes_per_particle(precision),
+                    3: bytes_per_particle(precision, cluster=pair_scheme_3d == 1)}
+        caps = {2: hbm_budget_bytes * share_2d / self.bpp[2],
+                3: hbm_budget_bytes * (1 - share_2d) / self.bpp[3]}
         if group_params is None:
             group_params = {2: make_job(0, 0.0, 2, 256, 1, 1).params,
                             3: make_job(0, 0.0, 3, 1000, 1, 2).params}
         streams = streams or {2: None, 3: None}
+        schemes = {2: 0, 3: pair_scheme_3d}
         self.groups = {d: Group(d, group_params[d], caps[d], max_sims, precision, chunk,
-                                engine_factory, streams[d]) for d in (2, 3)}
+                                engine_factory, streams[d], schemes[d]) for d in (2, 3)}
         self.rejected = []
 
     def run(self, jobs, realtime=True, time_limit=None):
@@ -283,12 +294,11 @@ class Server:
         service = np.array([j.finished - j.admitted for j in ok]) if ok else np.zeros(1)
         work = sum(j.work for j in completed)
         window = max(j.arrival for j in jobs) if jobs else 0.0
-        bpp = bytes_per_particle(self.precision)
         return {
             "hbm_budget_bytes": self.hbm_budget,
             "capacity_particles": {d: g.capacity for d, g in self.groups.items()},
             "peak_particles": {d: g.peak for d, g in self.groups.items()},
-            "peak_hbm_bytes": sum(g.peak for g in self.groups.values()) * bpp,
+            "peak_hbm_bytes": sum(g.peak * self.bpp[d] for d, g in self.groups.items()),
             "jobs": len(jobs), "completed": len(ok),
             "failed": len([j for j in completed if j.error]), "rejected": len(self.rejected),
             "latency_p50_s": float(np.percentile(lat, 50)),

@@ -143,26 +143,24 @@ def test_cluster_scheme_with_binning_on_demand_and_thermostat():
     assert rel_l2(uu, uo) < MIXED_TOL
 
 
-@pytest.mark.parametrize("what", ["2d", "fp64", "small_box_with_another"])
+@pytest.mark.parametrize("what", ["2d", "fp64", "small_box"])
 def test_cell_scheme_runs_where_clusters_do_not_apply(what):
-    """pair_scheme = 1 leaves a 2D engine, an FP64 engine and an engine one
-    of whose simulations has a box narrower than five columns on the cell
-    scheme: the same launches and the same bits as pair_scheme = 0."""
+    """pair_scheme = 1 leaves a 2D engine, an FP64 engine and a simulation
+    whose box is narrower than five columns on the cell scheme: the same
+    launches and the same bits as pair_scheme = 0."""
     precision = "mixed"
     if what == "2d":
         prm, r, v, m, T0 = workloads.config_2d(48, 3130)
+    elif what == "small_box":
+        prm, r, v, m, T0 = workloads.config_3d(12, 3131)
     else:
         prm, r, v, m, T0 = workloads.config_3d(20, 3132)
-        precision = "fp64" if what == "fp64" else "mixed"
+        precision = "fp64"
     u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
-    small = workloads.config_3d(12, 3131)
     res = []
     for scheme in (0, 1):
         e, s = engine(prm, r, v, m, u, scheme, precision=precision, cap=2)
         with e:
-            if what == "small_box_with_another":
-                ps, rs, vs, ms, Ts = small
-                e.add(ps, rs, vs, ms, workloads.vdw_energy(np.full(len(rs), 0.7), Ts))
             e.advance(3)
             e.sync()
             res.append((e.kernels_per_step(), e.get_state(s)))
@@ -391,3 +389,41 @@ def test_cluster_scheme_batch_matches_oracle():
         ref = oracle.derivatives(*x)
         for k in ("rho", "vdot", "udot"):
             assert rel_l2(d[k], ref[k]) < MIXED_TOL, k
+
+
+def test_schemes_side_by_side_keep_each_simulation_alone():
+    """A simulation whose box admits columns runs on cluster pairs, one whose
+    box does not on cell windows, in the same engine and the same steps; each
+    gives the bits it gives alone (where its scheme is the same choice)."""
+    big = workloads.config_3d(20, 3190, integrator="rk4")
+    small = workloads.config_3d(12, 3191, integrator="rk4")
+    sims = []
+    for prm, r, v, m, T0 in (big, small):
+        sims.append((prm, r, v, m, with_gradient(prm, r, v, m, T0)))
+    total = sum(len(x[1]) for x in sims)
+    with Engine(sims[0][0], "mixed", max_particles=total, max_sims=2) as e:
+        ids = [e.add(*x) for x in sims]
+        e.set_tuning(pair_scheme=1, steps_per_graph=3)
+        ks = e.kernels_per_step()
+        d = [e.derivatives(i) for i in ids]
+        e.sync()
+        assert e.last_pair_total() == sum(oracle.derivatives(*x)["nip"] for x in sims)
+        for x, di in zip(sims, d):
+            ref = oracle.derivatives(*x)
+            for k in ("rho", "vdot", "udot"):
+                assert rel_l2(di[k], ref[k]) < MIXED_TOL, k
+        e.advance(6)
+        e.sync()
+        mixed = [e.get_state(i) for i in ids]
+    with Engine(sims[0][0], "mixed", max_particles=total, max_sims=2) as e0:
+        for x in sims:
+            e0.add(*x)
+        assert e0.kernels_per_step() < ks        # both schemes' passes ran
+    for x, got in zip(sims, mixed):
+        e, s = engine(*x, 1, steps_per_graph=3)
+        with e:
+            e.advance(6)
+            e.sync()
+            alone = e.get_state(s)
+        for a, b in zip(got, alone):
+            assert np.array_equal(a, b)

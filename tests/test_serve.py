@@ -139,7 +139,9 @@ def test_malformed_and_refused_jobs_fail_alone():
     assert [j.result[0] for j in good] == [20, 15]
     assert rep["completed"] == 2 and rep["rejected"] == 2 and rep["failed"] == 1
     assert rep["peak_particles"][2] == 100 and rep["peak_particles"][3] == 60
-    assert rep["peak_hbm_bytes"] == 160 * serve.bytes_per_particle("mixed")
+    # the 3D group on cluster pairs counts their tables and lists too
+    assert rep["peak_hbm_bytes"] == (100 * serve.bytes_per_particle("mixed")
+                                     + 60 * serve.bytes_per_particle("mixed", cluster=True))
 
 
 def test_latency_accounting_uses_arrival_times():
@@ -177,15 +179,20 @@ def test_poisson_workload_shape():
 # ---- on the GPU ----
 
 def small_jobs(seed=77):
-    specs = [(2, 900, 30), (3, 1000, 20), (2, 1600, 45), (2, 400, 15), (3, 1331, 25),
-             (2, 2500, 35)]
+    # the 3D jobs: one too small for columns (cell windows), two on cluster
+    # pairs, sharing the 3D engine
+    specs = [(2, 900, 30), (3, 1000, 20), (2, 1600, 45), (2, 400, 15), (3, 8000, 25),
+             (2, 2500, 35), (3, 10648, 12)]
     return [make_job(k, 0.01 * k, d, n, s, seed + k) for k, (d, n, s) in enumerate(specs)]
 
 
 def run_alone(job, precision="mixed"):
+    """The job in an engine of its own, on the pair scheme of its server
+    group (cluster pairs for 3D)."""
     from pyticles_gb300 import Engine
     with Engine(job.params, precision, max_particles=job.n) as e:
         s = e.add(job.params, job.r, job.v, job.m, job.u)
+        e.set_tuning(pair_scheme=1 if job.dim == 3 else 0)
         e.advance(job.steps)
         e.sync()
         return e.get_state(s)
