@@ -207,14 +207,15 @@ typedef struct sph_tuning {
     int32_t pair_scheme;      /* 0: cell windows, a particle per lane.
                                  1: cluster pairs -- clusters of 8 compact
                                  particles against listed clusters of 4, 8 x 4
-                                 pairs per warp step.  Applies to a 3D engine
-                                 in mixed precision without collisions whose
-                                 simulations' boxes each span at least five
-                                 columns of about 8 particles per axis;
-                                 otherwise the cell scheme runs.  Lists are
-                                 built every step, per simulation (a
+                                 pairs per warp step, for each simulation of
+                                 a 3D mixed-precision engine without
+                                 collisions whose box spans at least five
+                                 columns of about 8 particles per axis; the
+                                 other simulations stay on cell windows in
+                                 the same steps.  The choice and the lists
+                                 (built every step) are per simulation, so a
                                  simulation gives the same bits alone or in a
-                                 batch); same pair set, rounding differs from
+                                 batch; same pair set, rounding differs from
                                  scheme 0                                     */
     int32_t reserved;         /* 0 */
 } sph_tuning;
