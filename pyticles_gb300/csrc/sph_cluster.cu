@@ -49,6 +49,7 @@ int nblocks(long long n, int block) { return (int)std::max<long long>(1, (n + bl
 __global__ void k_cl_key(const __grid_constant__ View v, const __grid_constant__ ClusterSet c) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.np) return;
+    if (!SPH_IN_BOUNDS(i < c.nall, v.err_any)) return;
     const int sim = v.b_sim[i];
     const SimDev &S = v.sims[sim];
     if (!S.cl_on) {   // on the cell-window passes
@@ -68,6 +69,7 @@ __global__ void k_cl_key(const __grid_constant__ View v, const __grid_constant__
         k[a] = q;
     }
     const int key = g.fine_off + (k[1] * g.ncx + k[0]) * g.nslab + k[2];
+    if (!SPH_IN_BOUNDS(key >= 0 && key < c.nfine, v.err_any)) return;
     c.fkey[i] = key;
     c.frank[i] = atomicAdd(&c.fcount[key], 1);
 }
@@ -75,6 +77,7 @@ __global__ void k_cl_key(const __grid_constant__ View v, const __grid_constant__
 __global__ void k_cl_scatter(const __grid_constant__ View v, const __grid_constant__ ClusterSet c) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.np) return;
+    if (!SPH_IN_BOUNDS(i < c.nall, v.err_any)) return;
     const int key = c.fkey[i];
     if (key < 0) return;
     const int dst = c.fstart[key] + c.frank[i];
@@ -115,13 +118,16 @@ __global__ void k_cl_cols(const __grid_constant__ ClusterSet c) {
 __global__ void k_cl_slots(const __grid_constant__ View v, const __grid_constant__ ClusterSet c) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= c.fstart[c.nfine]) return;   // the particles on cluster pairs
+    if (!SPH_IN_BOUNDS(p < c.nall, v.err_any)) return;
     const int i = c.ford[p];
+    if (!SPH_IN_BOUNDS(i >= 0 && i < v.np && i < c.nall, v.err_any)) return;
     const int sim = v.b_sim[i];
     const ClGeom &g = c.geom[sim];
     const int local = c.fkey[i] - g.fine_off;
     const int lcol = local / g.nslab;
     const int col = g.col_off + lcol;
     const int q = p - c.fstart[g.fine_off + lcol * g.nslab];
+    if (!SPH_IN_BOUNDS(col >= 0 && col < c.ncol, v.err_any)) return;
     const int cl = c.colcl[col] + (q >> 3);
     const int slot = cl * 8 + (q & 7);
     if (!SPH_IN_BOUNDS(cl >= 0 && cl < c.ncl_max, v.err_any)) return;
@@ -419,6 +425,7 @@ __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, c
         }
         const bool near = en.x < 0;
         const int sj = (en.x & 0x7fffffff) * 4 + jj;
+        if (!SPH_IN_BOUNDS(sj < c.slots_max, v.err_any)) continue;
         const float sx = (float)(signed char)(en.y & 0xff) * x.wx;
         const float sy = (float)(signed char)((en.y >> 8) & 0xff) * x.wy;
         const float sz = (float)(en.y >> 16) * x.gz;

@@ -561,6 +561,7 @@ int cluster_setup(sph_engine *e, std::vector<SimDev> &sd) {
     c.nfine = (int)nfine;
     c.ncl_max = (int)ncl_max;
     c.slots_max = (int)(8 * ncl_max);
+    c.nall = (int)e->cl_np;
     c.lstride = per;
     c.on = 1;
     e->cl_stale = true;

@@ -178,6 +178,7 @@ struct ClusterSet {
     int on;                       // the scheme runs for this layout
     int ncol, nfine;              // columns / fine cells of all simulations
     int ncl_max, slots_max;
+    int nall;                     // particle slots of the per-particle arrays
     int lstride;                  // list entries reserved per i-cluster
     const ClGeom *geom;           // [simulation slots]
     ClGeom g1;                    // an engine with one simulation: its lattice,

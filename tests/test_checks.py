@@ -2,7 +2,8 @@
 pair and collision kernels test every cell and particle index they derive
 and report SPH_EBOUNDS instead of accessing out of range.  Ordinary
 workloads -- batched, 2D and 3D, binning on demand, collisions, small
-single-cell boxes -- run clean under it and give the release build's bits.
+single-cell boxes, cluster pairs beside cell windows -- run clean under it
+and give the release build's bits.
 The library is loaded in a child process (PYTICLES_CHECKS=1)."""
 import os
 import subprocess
@@ -50,6 +51,19 @@ with Engine(p3, "mixed", max_particles=len(r3)) as e:
     e.advance(6)
     e.sync()
     out.append(e.get_state(s)[0].sum())
+# cluster pairs beside cell windows: a box too small for columns, a larger one
+p5, r5, v5, m5, T5 = workloads.config_3d(12, 7004, integrator="rk4")
+p4, r4, v4, m4, T4 = workloads.config_3d(20, 7003, integrator="rk4")
+with Engine(p4, "mixed", max_particles=len(r5) + len(r4), max_sims=2) as e:
+    ids = [e.add(p5, r5, v5, m5, workloads.vdw_energy(np.full(len(r5), 0.7), T5)),
+           e.add(p4, r4, v4, m4, workloads.vdw_energy(np.full(len(r4), 0.7), T4))]
+    e.set_tuning(pair_scheme=1, steps_per_graph=3)
+    e.advance(6)
+    e.sync()
+    for s in ids:
+        e.derivatives(s)
+        out.append(e.get_state(s)[0].sum())
+    e.sync()
 print(repr([float(x) for x in out]))
 """
 
