@@ -388,8 +388,9 @@ constexpr bool kPfDensity = false, kPfHeat = false, kPfForce = true;
 // takes no pairs: two padding slots lie at the same far point), j = the
 // lane's quarter (lane >> 3) of each listed j-cluster.  body(sj, pj, d, rsq,
 // near) for every pair of the exact set (FP32 test, FP64 in the guard band);
-// near is the entry's flag, uniform across the warp; flush() after every
-// 16th entry of the list (blocked compensated sums).
+// near is NEAR, the segment's kind (the front of a list holds its entries
+// within the short support, the back the others); flush() after every 16th
+// entry of the list (blocked compensated sums).
 
 // The lattice steps of the warp's simulation and its constants.
 struct PairCtx {
@@ -398,7 +399,7 @@ struct PairCtx {
     float thr_lo, thr_hi;
 };
 
-template <bool PF, typename F, typename G>
+template <bool PF, bool NEAR, typename F, typename G>
 __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, const PairCtx &x,
                                            int si, int gi, const float4 &pi, const int2 *p, int n,
                                            int step, int &flushes, F body, G flush) {
@@ -423,7 +424,6 @@ __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, c
             en = *p;
             pj = c.cpos[(en.x & 0x7fffffff) * 4 + jj];
         }
-        const bool near = en.x < 0;
         const int sj = (en.x & 0x7fffffff) * 4 + jj;
         if (!SPH_IN_BOUNDS(sj < c.slots_max, v.err_any)) continue;
         const float sx = (float)(signed char)(en.y & 0xff) * x.wx;
@@ -436,8 +436,7 @@ __device__ __forceinline__ void cl_segment(const View &v, const ClusterSet &c, c
         const float rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (gi >= 0 && rsq <= x.thr_hi && sj != si &&
             (rsq < x.thr_lo || exact_in_set<3>(v.xe_in, x.S, gi, c.slot_idx[sj]))) {
-            if (near) body(sj, pj, d, rsq, std::true_type{});
-            else body(sj, pj, d, rsq, std::false_type{});
+            body(sj, pj, d, rsq, std::integral_constant<bool, NEAR>{});
         }
         if ((++flushes & 15) == 0) flush();
     }
@@ -451,10 +450,11 @@ __device__ __forceinline__ void cl_for_pairs(const View &v, const ClusterSet &c,
                                              G flush) {
     const int2 *region = c.ent + (long long)wid * c.lstride;
     int flushes = 0;
-    cl_segment<PF>(v, c, x, si, gi, pi, region, c.lnear[wid], 1, flushes, body, flush);
+    // a list's front holds exactly its entries within the short support
+    cl_segment<PF, true>(v, c, x, si, gi, pi, region, c.lnear[wid], 1, flushes, body, flush);
     if (!NEAR_ONLY)
-        cl_segment<PF>(v, c, x, si, gi, pi, region + c.lstride - 1, c.lfar[wid], -1, flushes,
-                       body, flush);
+        cl_segment<PF, false>(v, c, x, si, gi, pi, region + c.lstride - 1, c.lfar[wid], -1,
+                              flushes, body, flush);
 }
 
 // The warp's simulation: kernel parameters for a single simulation (ONE),
