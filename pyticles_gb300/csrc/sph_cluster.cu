@@ -558,7 +558,8 @@ __global__ void __launch_bounds__(kBlock) k_cl_density(const __grid_constant__ V
         ((float *)v.pres0)[gi] = (float)p;
         ((float *)v.pco0)[gi] = (float)pco;
     }
-    c.cf[si] = make_float4((float)fs, (float)rho, Th, (float)(T - (double)Th));
+    // the heat pass reads 1/rho (rounded once from FP64, no reciprocal per pair)
+    c.cf[si] = make_float4((float)fs, (float)recip64<float>(rho), Th, (float)(T - (double)Th));
     c.crho[si] = (float)rho;
     const float4 vi = ((const float4 *)v.pk_vel_in)[gi];
     c.cfv[si] = make_float4(vi.x, vi.y, vi.z, (float)fs);
@@ -590,11 +591,12 @@ __global__ void __launch_bounds__(kBlock) k_cl_heat(const __grid_constant__ View
     cl_for_pairs<true, kPfHeat>(
         v, c, x, wid, si, gi, pi,
         [&](int sj, const float4 &pj, const float *d, float rsq, auto) {
-            const float r = fsqrt<float>(rsq);
-            const float g = kernel_g<K, float>(ks, r);
-            const float4 fj = c.cf[sj];
+            const float ir = rsqrt0(rsq);
+            const float r = rsq * ir;
+            const float g = kernel_g_ir<K>(ks, r, ir);
+            const float4 fj = c.cf[sj];   // {p/rho^2, 1/rho, T_hi, T_lo}
             const float dT = (fj.z - fi.z) + (fj.w - fi.w);
-            const float f = pj.w * rrcp<float>(fj.y) * dT * g;
+            const float f = pj.w * fj.y * dT * g;
             q[0].add(f * d[0]);
             q[1].add(f * d[1]);
             q[2].add(f * d[2]);
@@ -607,7 +609,7 @@ __global__ void __launch_bounds__(kBlock) k_cl_heat(const __grid_constant__ View
     double s[3];
     for (int a = 0; a < 3; ++a) s[a] = quad_sum(q[a].get64());
     if (jj != 0 || gi < 0) return;
-    const float ir2 = 1.0f / (fi.y * fi.y);
+    const float ir2 = fi.y * fi.y;   // 1/rho^2
     float qq[3];
     for (int a = 0; a < 3; ++a) {
         qq[a] = k.kappa * (float)s[a];
@@ -650,13 +652,14 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_cl_force(const __grid_c
         v, c, x, wid, si, gi, pi,
         [&](int sj, const float4 &pj, const float *d, float rsq, auto near) {
             constexpr bool NEAR = decltype(near)::value;
-            const float r = fsqrt<float>(rsq);
-            const float gl = kernel_g<K, float>(kl, r);
+            const float ir = rsqrt0(rsq);
+            const float r = rsq * ir;
+            const float gl = kernel_g_ir<K>(kl, r, ir);
             const float4 fvj = c.cfv[sj];
             const float dvdx = (fvj.x - fvi.x) * d[0] + (fvj.y - fvi.y) * d[1] + (fvj.z - fvi.z) * d[2];
             float gsum = pl2 * gl, gs = 0.0f;
             if constexpr (NEAR) {
-                gs = kernel_g<K, float>(ks, r);
+                gs = kernel_g_ir<K>(ks, r, ir);
                 float ps = fvi.w + fvj.w;
                 if (visc && dvdx < 0.0f) {
                     const float rhoj = c.crho[sj];

@@ -224,6 +224,33 @@ __device__ __forceinline__ R kernel_g(const KConst<R> &k, R r) {
     return g;
 }
 
+// (dW/dr)/r given r and ir = 1/r (0 at r = 0) in FP32: the cubic spline's
+// outer branch and Debrun take ir instead of a correctly rounded reciprocal
+// of r; the other kernels are kernel_g.
+template <int K>
+__device__ __forceinline__ float kernel_g_ir(const KConst<float> &k, float r, float ir) {
+    if (K == SPH_KERNEL_CUBIC) {
+        const float q = qof<float>(k, r);
+        float s = 2.0f - q;
+        s = s > 0.0f ? s : 0.0f;
+        const float g_in = k.g0 * (-3.0f + 2.25f * q);
+        const float g_out = k.g0 * (-0.75f * s * s * k.h) * ir;
+        return q < 1.0f ? g_in : g_out;
+    } else if (K == SPH_KERNEL_DEBRUN) {
+        if (r < k.h) {
+            const float s = k.h - r;
+            return k.g0 * s * s * ir;
+        }
+        return 0.0f;
+    } else {
+        return kernel_g<K, float>(k, r);
+    }
+}
+
+// 1/sqrt(x) by the MUFU approximation, 0 at x = 0 (r = x * ir is then the
+// same as fsqrt's x * rsqrt(x))
+__device__ __forceinline__ float rsqrt0(float x) { return x > 0.0f ? rsqrtf(x) : 0.0f; }
+
 __device__ __forceinline__ void set_err(int *err, int *err_any, int s, int code) {
     atomicCAS(&err[s], 0, code);
     atomicCAS(err_any, 0, code);

@@ -197,7 +197,7 @@ struct ClusterSet {
     int2 *ent;                    // {j half | near << 31, lattice offset dx|dy<<8|dz<<16}
     int *maxfill;                 // longest list since the host last read it
     float4 *cpos, *cfv, *cf, *cq; // per slot: {x, y, z, m} local, {v, p/rho^2},
-                                  // {p/rho^2, rho, T_hi, T_lo}, {q/rho^2, 0}
+                                  // {p/rho^2, 1/rho, T_hi, T_lo}, {q/rho^2, 0}
     float *crho;
 };
 
