@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(128) k_cl_list(const __grid_constant__ View v,
 
 // Prefetching the next entry and its j record, per pass: measured faster
 // for the force pass only (3D, N = 2,097,152: force 15.26 -> 14.65 ms per
-// step; density 8.47 -> 10.03 and heat 3.31 -> 3.48 with it).
+// step; density 8.29 -> 8.98 and heat 2.47 -> 2.63 with it).
 constexpr bool kPfDensity = false, kPfHeat = false, kPfForce = true;
 
 // Pairs of one lane over n entries from p (step +1 or -1): i = slot si (lane
