@@ -22,17 +22,21 @@
 //                            each cluster's lattice reference point
 //   k_cl_pack              : cluster-local FP32 positions (every evaluation)
 //   k_cl_bbox, k_cl_list   : boxes of the clusters and of their halves; per
-//                            i-cluster the j-halves within the cutoff plus twice the
-//                            allowed drift, with the shift between the two
-//                            lattice points and a flag for the short
-//                            kernel's support (those entries first)
+//                            i-cluster the j-halves of the same simulation
+//                            within the cutoff plus twice the allowed drift,
+//                            with the shift between the two lattice points,
+//                            the entries within the short kernel's support in
+//                            front, into a region of lstride entries (sized
+//                            by the engine from a measured build)
 // Passes: k_cl_density (+ EOS), k_cl_heat, k_cl_force (rates; the integrator
-// stage runs as k_integrate).
+// stage runs as k_integrate).  Simulations whose boxes are too narrow for
+// the columns stay on the cell-window passes in the same steps.
 //
 // Each particle sums its pairs in list order (j-clusters in a fixed order
-// derived from the step's state), each lane over its quarter of every
+// derived from its simulation's state), each lane over its quarter of every
 // j-cluster, and the four quarters are added in a fixed tree, so the results
-// are deterministic; they differ from the cell scheme's in rounding only.
+// are deterministic and the same alone or in a batch; they differ from the
+// cell scheme's in rounding only.
 #include <type_traits>
 
 #include "sph_pairs.cuh"
