@@ -935,12 +935,11 @@ int cluster_measure(sph_engine *e) {
     const int need = std::max(64, (int)std::ceil(1.25 * fill) + 8);
     if (need == c.lstride) return SPH_OK;
     free_graph(e);
-    int st_alloc = SPH_ENOMEM;
-    if ((long long)need * c.ncl_max <= 2147483000LL) {
-        cudaFree(c.ent);
-        c.ent = nullptr;
-        st_alloc = dalloc(&c.ent, (int64_t)need * c.ncl_max);
-    }
+    // regions are addressed with 64-bit offsets: the buffer may exceed 2^31
+    // entries (a simulation of tens of millions of particles)
+    cudaFree(c.ent);
+    c.ent = nullptr;
+    const int st_alloc = dalloc(&c.ent, (int64_t)need * c.ncl_max);
     if (st_alloc != SPH_OK) {
         // no room for the lists: the layout is rebuilt on the cell scheme
         c.on = 0;
