@@ -146,8 +146,9 @@ def gpu_initial_energy(prm, r, v, m, T0, stream):
 
 def run_timed(prm, r, v, m, u, precision, steps, warmup, torch, stream, profile=True,
               knobs=None, sims=None):
-    """Device time of `steps` steps captured in one graph, with per-pass
-    CUDA events recorded inside the graph.  `sims` [(params, r, v, m, u)]
+    """Device time of `steps` graph-captured steps (one graph; with cluster
+    pairs, graphs of 20 steps each captured on fresh event slots), with
+    per-pass CUDA events recorded inside the graphs.  `sims` [(params, r, v, m, u)]
     replaces the single simulation for batched runs."""
     from pyticles_gb300 import Engine
     sims = sims or [(prm, r, v, m, u)]
@@ -364,7 +365,7 @@ def main():
     ap.add_argument("--batched-sims", type=int, default=512)
     ap.add_argument("--batched-steps", type=int, default=100)
     ap.add_argument("--side3d", type=int, default=128)
-    ap.add_argument("--steps3d", type=int, default=20)
+    ap.add_argument("--steps3d", type=int, default=200)
     ap.add_argument("--serve-jobs", type=int, default=12)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--accuracy-steps", type=int, default=1000,

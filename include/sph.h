@@ -155,7 +155,12 @@ int sph_sim_steps(sph_engine *e, int32_t sim_id, int64_t *steps);
 int sph_sim_set_steps(sph_engine *e, int32_t sim_id, int64_t steps);
 
 /* Advances every simulation by nsteps steps of its integrator, applying
- * the periodic box after each step and the thermostat when enabled. */
+ * the periodic box after each step and the thermostat when enabled.
+ * Asynchronous except with cluster pairs on (sph_tuning.pair_scheme), where
+ * steps run in chunks of 20 and the call returns once all but the last
+ * chunk finished: each chunk's longest pair list is checked before the
+ * chunk after next is queued, and the lists are re-measured in between
+ * when one filled its region past 80%. */
 int sph_advance(sph_engine *e, int32_t nsteps);
 
 /* One derivative evaluation f(x) of every simulation at its current state

@@ -145,6 +145,7 @@ struct sph_engine {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_steps = 0;
+    bool graph_launched = false;   // its event slots hold a launch's profile
     bool props_valid = false;
 };
 
@@ -403,6 +404,7 @@ void free_graph(sph_engine *e) {
     e->graph_exec = nullptr;
     e->graph = nullptr;
     e->graph_steps = 0;
+    e->graph_launched = false;
 }
 
 void cluster_free(sph_engine *e) {
@@ -908,12 +910,12 @@ void enqueue_step(sph_engine *e, cudaStream_t st) {
 }
 
 // Measures the longest pair list of the current state (a binning and a
-// list build that only counts) and sizes the list regions to 1.25 times it,
+// list build that only counts) and sizes the list regions to 1.4 times it,
 // growing or shrinking the entry buffer.  Runs before an advance or an
 // evaluation whenever the state was set from outside or the layout changed,
-// and when the previous advance filled a region past 80% (a fluid that
-// condensed into denser regions): an overflow inside an advance is then
-// unlikely, and still reported (SPH_ECAPACITY) if it happens.  Lists that
+// and within an advance once a chunk of steps filled a region past 80% (a
+// fluid condensing into denser regions): the chunk already queued then has
+// 25% of headroom left, and an overflow is still reported (SPH_ECAPACITY).  Lists that
 // do not fit in device memory leave the layout on the cell scheme.
 int cluster_measure(sph_engine *e) {
     ClusterSet &c = e->cl;
@@ -932,7 +934,8 @@ int cluster_measure(sph_engine *e) {
     CK(cudaMemsetAsync(c.maxfill, 0, sizeof(int), st));
     CK(cudaStreamSynchronize(st));
     e->cl_stale = false;
-    const int need = std::max(64, (int)std::ceil(1.25 * fill) + 8);
+    e->cl_fill_pending = false;   // read of the old regions: superseded
+    const int need = std::max(64, (int)std::ceil(1.4 * fill) + 8);
     if (need == c.lstride) return SPH_OK;
     free_graph(e);
     // regions are addressed with 64-bit offsets: the buffer may exceed 2^31
@@ -1016,8 +1019,12 @@ int ensure_prof_pool(sph_engine *e, size_t need) {
     return SPH_OK;
 }
 
+// Captures `per` steps as the engine's graph, unless that graph exists.
+// With profiling on, a graph already launched is captured again on fresh
+// event slots, so every launch's passes are timed (not only the last one).
 int build_graph(sph_engine *e, int per) {
-    if (e->graph_exec && e->graph_steps == per) return SPH_OK;
+    if (e->graph_exec && e->graph_steps == per && !(e->prof_on && e->graph_launched))
+        return SPH_OK;
     free_graph(e);
     if (e->prof_on) {
         TRY(ensure_prof_pool(e, e->prof_used + (size_t)per * 2 * (1 + 4 * e->nstage) + 8));
@@ -1492,44 +1499,88 @@ int sph_sim_set_steps(sph_engine *e, int32_t id, int64_t steps) {
     return SPH_OK;
 }
 
-int sph_advance(sph_engine *e, int32_t nsteps) {
-    if (!e || nsteps < 0) return SPH_EINVAL;
-    if (nsteps == 0) return SPH_OK;
-    TRY(ensure_layout(e));
-    if (e->np_b == 0) return SPH_OK;
-    TRY(cluster_check(e));
+// Steps per graph launch with cluster pairs: a long advance runs in chunks,
+// and the longest list of each chunk is checked while the next one runs.
+constexpr int kClChunk = 20;
+
+// Between two chunks of an advance with cluster pairs: waits for the longest
+// list of the chunk before the one just queued (finished by now; the queued
+// chunk keeps the device busy), queues the read of the one just queued, and
+// reports whether a region was filled past 80% (re-measure before more steps).
+int cluster_between(sph_engine *e, bool *over) {
+    if (e->cl_fill_pending) {
+        CK(cudaEventSynchronize(e->cl_fill_ev));
+        e->cl_fill_pending = false;
+        if (*e->cl_fill_host > 0.8 * e->cl.lstride) e->cl_stale = true;
+    }
+    TRY(cluster_note_fill(e));
+    *over = e->cl_stale;
+    return SPH_OK;
+}
+
+// Steps per graph launch of an advance.
+int graph_chunk(const sph_engine *e) {
+    const int per = std::max(1, e->tune.steps_per_graph);
+    return e->cl.on ? std::min(per, kClChunk) : per;
+}
+
+// Queues up to n steps in the current layout; stops early (*ran < n) when a
+// cluster list region needs re-measuring before further steps.
+int advance_span(sph_engine *e, int n, int *ran) {
     cudaStream_t st = e->stream;
-    int per = std::max(1, e->tune.steps_per_graph);
+    const bool cl = e->cl.on;
+    const int per = graph_chunk(e);
     int done = 0;
-    // The binning pass covers A's used extent.  After simulations joined or
-    // left, A holds dropped or unsorted particles beyond the live count;
-    // that first step runs eagerly, after which A is compact (extent == live).
-    if (e->prof_on) TRY(ensure_prof_pool(e, e->prof_used + (size_t)nsteps * 2 * (1 + 4 * e->nstage) + 8));
+    *ran = 0;
+    if (e->prof_on) TRY(ensure_prof_pool(e, e->prof_used + (size_t)n * 2 * (1 + 4 * e->nstage) + 8));
     if (rebin_on_demand(e) && !e->bins_valid) {
         // the state or the layout changed since the last step: bin first
         launch_fill_int(e->rebin_gate, 1, 1, st);
         e->bins_valid = true;
     }
+    // The binning pass covers A's used extent.  After simulations joined or
+    // left, A holds dropped or unsorted particles beyond the live count;
+    // that first step runs eagerly, after which A is compact (extent == live).
     if (e->a_extent != e->np_b) {
         enqueue_step(e, st);
         after_advance(e, 1);
         ++done;
     }
-    if (e->tune.use_graph && nsteps - done >= per) {
-        TRY(build_graph(e, per));
-        while (nsteps - done >= per) {
+    while (done < n) {
+        int k;
+        if (e->tune.use_graph && n - done >= per) {
+            TRY(build_graph(e, per));
             CK(cudaGraphLaunch(e->graph_exec, st));
-            after_advance(e, per);
-            done += per;
+            e->graph_launched = true;
+            k = per;
+        } else {
+            k = cl ? std::min(n - done, per) : n - done;
+            for (int i = 0; i < k; ++i) enqueue_step(e, st);
+        }
+        after_advance(e, k);
+        done += k;
+        if (cl) {
+            bool over = false;
+            TRY(cluster_between(e, &over));
+            if (over) break;
         }
     }
+    *ran = done;
+    return SPH_OK;
+}
+
+int sph_advance(sph_engine *e, int32_t nsteps) {
+    if (!e || nsteps < 0) return SPH_EINVAL;
+    int done = 0;
     while (done < nsteps) {
-        enqueue_step(e, st);
-        after_advance(e, 1);
-        ++done;
+        TRY(ensure_layout(e));
+        if (e->np_b == 0) return SPH_OK;
+        TRY(cluster_check(e));
+        int ran = 0;
+        TRY(advance_span(e, nsteps - done, &ran));
+        done += ran;
     }
     CK(cudaGetLastError());
-    TRY(cluster_note_fill(e));
     return SPH_OK;
 }
 
@@ -1763,7 +1814,7 @@ int sph_prepare(sph_engine *e) {
     if (e->np_b == 0 || !e->tune.use_graph) return SPH_OK;
     TRY(cluster_check(e));
     if (e->a_extent != e->np_b) return SPH_OK;  // first step after a change runs eagerly
-    return build_graph(e, std::max(1, e->tune.steps_per_graph));
+    return build_graph(e, graph_chunk(e));
 }
 
 int sph_profile(sph_engine *e, int32_t enable) {

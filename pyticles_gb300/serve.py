@@ -46,9 +46,9 @@ def bytes_per_particle(precision="mixed", integrator="ieuler", cluster=False):
     if cluster and precision == "mixed":
         # cluster pairs (csrc/sph_cluster.cu): slot records (72 B a slot),
         # sort scratch (16 B), cluster boxes and references (16 B), and the
-        # lists: 1.25 times the longest, about 370 entries of 8 B per cluster
+        # lists: 1.4 times the longest, about 415 entries of 8 B per cluster
         # of 8 in a fluid at n = 0.7 (denser fluids need proportionally more)
-        b += 72 + 16 + 16 + 400
+        b += 72 + 16 + 16 + 440
     return b
 
 

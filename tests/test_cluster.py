@@ -125,6 +125,29 @@ def test_cluster_scheme_is_deterministic():
             assert np.array_equal(a, b)
 
 
+def test_pass_profile_counts_every_chunk_of_an_advance():
+    """With cluster pairs an advance replays its graph chunk by chunk; the
+    pass profile times every launch, so 60 steps count three times the
+    passes of 20 (graphs of 200 steps requested, chunks of 20 run)."""
+    prm, r, v, m, u = case("cubic_heat_8000")
+    launches = {}
+    for steps in (20, 60):
+        e, s = engine(prm, r, v, m, u, 1, steps_per_graph=200)
+        with e:
+            e.advance(2)
+            e.sync()
+            e.profile(True)
+            e.prepare()
+            e.advance(steps)
+            e.sync()
+            passes = e.profile_read()
+            launches[steps] = {k: p["launches"] for k, p in passes.items()}
+            assert all(p["ms"] >= 0.0 for p in passes.values())
+    assert launches[20]["force"] > 0
+    for k, n in launches[20].items():
+        assert launches[60][k] == 3 * n, k
+
+
 def test_cluster_scheme_with_binning_on_demand_and_thermostat():
     prm, r, v, m, T0 = workloads.config_3d(20, 3120, integrator="rk4", dt=2e-3)
     prm.thermostat = 1
@@ -273,6 +296,35 @@ def test_cluster_lists_follow_a_state_that_condenses():
         rr, vv, uu = e.get_state(s)
     ro, vo, uo, _ = oracle.advance(prm, rd, vd, md, ud, 4)
     assert rel_l2(rr, ro) < MIXED_TOL and rel_l2(uu, uo) < MIXED_TOL
+
+
+def test_cluster_lists_grow_within_one_advance():
+    """A gas imploding towards the box centre (v = -(r - c)): over 200 steps
+    in one call the densest lists grow by more than the 1.4 times headroom of
+    a measurement, so the call must re-measure between its chunks of steps.
+    It runs without SPH_ECAPACITY, gives the bits of the same steps taken in
+    calls of 10, and its final state has the oracle's pair set."""
+    spatial = pytest.importorskip("scipy.spatial")
+    prm, r, v, m, u = droplet(gas=True)
+    L = prm.box[0]
+    v = v - (r - 0.5 * L)
+    rc = prm.cutoff
+    counts0 = spatial.cKDTree(r, boxsize=L).query_ball_point(r, rc, return_length=True)
+    out = []
+    for calls in ((200,), (10,) * 20):
+        e, s = engine(prm, r, v, m, u, 1, steps_per_graph=200)
+        with e:
+            for n in calls:
+                e.advance(n)
+            e.sync()                         # no SPH_ECAPACITY
+            out.append(e.get_state(s) + (e.pair_count(s),))
+    for a, b in zip(out[0][:3], out[1][:3]):
+        assert np.array_equal(a, b)
+    rr, vv, uu, npairs = out[0]
+    counts1 = spatial.cKDTree(np.mod(rr, L), boxsize=L).query_ball_point(
+        np.mod(rr, L), rc, return_length=True)
+    assert counts1.max() > 1.5 * counts0.max()
+    assert npairs == oracle.derivatives(prm, rr, vv, m, uu)["nip"]
 
 
 def test_particle_system_with_cluster_pairs():
