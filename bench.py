@@ -286,8 +286,15 @@ def accuracy_track(prm, r, v, m, u, steps, every, stream, knobs=None):
             rs, vs, us = e.get_state(s)
             g = e.derivatives(s)
             e.sync()
+            t0 = time.perf_counter()
             ref = oracle.derivatives(prm, rs, vs, m, us)
-            row = {"step": done}
+            t_ref = time.perf_counter() - t0
+            row = {"step": done,
+                   # the same evaluation on the host cores: the CPU baseline
+                   # of this workload (one evaluation = its pair count)
+                   "oracle_eval": {"value": ref["nip"] / t_ref, "unit": UNIT,
+                                   "seconds": t_ref, "cores": oracle.threads(),
+                                   "kind": "port"}}
             for k in ("rho", "vdot", "udot"):
                 row[k] = float(np.linalg.norm(g[k] - ref[k]) / np.linalg.norm(ref[k]))
             out.append(row)
@@ -443,6 +450,10 @@ def main():
         if not args.no_cpu:
             acc3 = accuracy_track(*w3[0], args.steps3d, args.steps3d, stream,
                                   knobs=extras["fluid3d"]["tuning"])
+            extras["fluid3d"]["cpu_baseline"] = dict(
+                acc3[-1].pop("oracle_eval"),
+                sample="one FP64 oracle evaluation (pair search, density, heat flux, force) "
+                       "of the 128^3 state after the timed steps")
             extras["fluid3d"]["accuracy"] = {
                 "what": "relative L2 of the mixed-precision evaluation against the FP64 "
                         "oracle at the GPU state after the timed steps",
@@ -453,6 +464,8 @@ def main():
     if rank == 0 and not args.no_cpu and args.accuracy_steps > 0:
         accuracy = accuracy_track(prm, r, v, m, u, args.accuracy_steps,
                                   max(1, min(100, args.accuracy_steps)), stream)
+        for row in accuracy:
+            row.pop("oracle_eval")
 
     cpu = None
     if rank == 0 and not args.no_cpu:
