@@ -48,7 +48,8 @@ enum sph_status {
     SPH_ECUDA = 6,           /* a CUDA runtime call failed                       */
     SPH_ESKIN = 7,           /* a particle moved further within one step than the
                                 cell slack allows (cell list would miss pairs)   */
-    SPH_ECAPACITY = 8,       /* engine particle / simulation capacity exceeded  */
+    SPH_ECAPACITY = 8,       /* engine particle / simulation capacity exceeded,
+                                or a cluster pair list outgrew its region       */
     SPH_ENOTFOUND = 9,       /* unknown simulation id                           */
     SPH_EBOUNDS = 10         /* an index check failed and the access was
                                 skipped: the checking build's checks, and in
@@ -157,10 +158,11 @@ int sph_sim_set_steps(sph_engine *e, int32_t sim_id, int64_t steps);
 /* Advances every simulation by nsteps steps of its integrator, applying
  * the periodic box after each step and the thermostat when enabled.
  * Asynchronous except with cluster pairs on (sph_tuning.pair_scheme), where
- * steps run in chunks of 20 and the call returns once all but the last
- * chunk finished: each chunk's longest pair list is checked before the
- * chunk after next is queued, and the lists are re-measured in between
- * when one filled its region past 80%. */
+ * steps run in graph chunks of steps_per_graph steps (at most 32; a longer
+ * setting is split into even chunks of about 20) and the call returns once
+ * all but its last chunk finished: each chunk's longest pair list is
+ * checked before the chunk after next is queued, and the lists are
+ * re-measured in between when one filled its region past 80%. */
 int sph_advance(sph_engine *e, int32_t nsteps);
 
 /* One derivative evaluation f(x) of every simulation at its current state

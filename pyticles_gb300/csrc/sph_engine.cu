@@ -1499,9 +1499,11 @@ int sph_sim_set_steps(sph_engine *e, int32_t id, int64_t steps) {
     return SPH_OK;
 }
 
-// Steps per graph launch with cluster pairs: a long advance runs in chunks,
-// and the longest list of each chunk is checked while the next one runs.
-constexpr int kClChunk = 20;
+// Steps per graph launch with cluster pairs: a long advance runs in chunks
+// of at most kClMaxChunk steps (a longer graph is split into even chunks of
+// about kClChunk), and the longest list of each chunk is checked while the
+// next one runs.
+constexpr int kClChunk = 20, kClMaxChunk = 32;
 
 // Between two chunks of an advance with cluster pairs: waits for the longest
 // list of the chunk before the one just queued (finished by now; the queued
@@ -1521,7 +1523,9 @@ int cluster_between(sph_engine *e, bool *over) {
 // Steps per graph launch of an advance.
 int graph_chunk(const sph_engine *e) {
     const int per = std::max(1, e->tune.steps_per_graph);
-    return e->cl.on ? std::min(per, kClChunk) : per;
+    if (!e->cl.on || per <= kClMaxChunk) return per;
+    const int n = (per + kClChunk - 1) / kClChunk;
+    return (per + n - 1) / n;
 }
 
 // Queues up to n steps in the current layout; stops early (*ran < n) when a
