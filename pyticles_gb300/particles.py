@@ -7,7 +7,9 @@ host state to libsph, runs one integrator step on the GPU (density ->
 EOS -> forces/rates -> integrator -> periodic wrap -> thermostat) and copies
 the state and properties back, with the reference's post-update semantics
 (particles.py:459-494, 496-542).  run(dt, nsteps) advances several steps
-with a single upload and download.
+with a single upload and download.  gather_state / scatter_state /
+gather_derivatives and create_particle keep the reference's state-vector
+interface for callers that drive their own integrator or add particles.
 
 The engine configuration is derived from the attached objects:
   box      PeriodicBox (box.py:28-47) -> periodic extents
@@ -44,6 +46,11 @@ KBDASH = 1.0
 class ParticleSystem:
     """Particles with basic mechanical properties (particles.py:69-195)."""
 
+    # Rows of the state vector x: m, r (3 rows), v (3 rows); the reference
+    # lays them out for 3D (particles.py:198-233), and a 2D system leaves the
+    # z rows at zero so that every row keeps its number.
+    N_VARIABLES = 7
+
     def __init__(self, n, d=3, maxn=125, controllers=(), xmax=XMAX, ymax=YMAX, zmax=ZMAX,
                  vmax=VMAX, simbox=None, mass=1.0, rinit=None, source=None, side=(5, 5, 5),
                  integrator="rk4", spacing=0.1):
@@ -69,6 +76,9 @@ class ParticleSystem:
                                       "netCDF modules; set p.r directly")
         self.m[:] = mass
         self.colour = 1.0, 0.0, 0.0
+        # state vectors of the integrators (particles.py:151-154)
+        self.x = np.zeros([self.N_VARIABLES, self.maxn])
+        self.xdot = np.zeros([self.N_VARIABLES, self.maxn])
         self.nlists = []
         self.forces = []
         self.controllers = list(controllers)
@@ -79,6 +89,40 @@ class ParticleSystem:
         for nl in self.nlists:
             if nl.rebuild_list:
                 nl.build()
+
+    def create_particle(self, r, v=None):
+        """Appends a particle at index n with the mass of particle n - 1
+        (particles.py:171-178); v defaults to rest."""
+        if self.n >= self.maxn:
+            raise ValueError(f"the system holds maxn = {self.maxn} particles already")
+        self.r[self.n] = r
+        self.m[self.n] = self.m[self.n - 1]
+        self.v[self.n] = 0.0 if v is None else v
+        self.n += 1
+        self.rebuild_lists()
+
+    def gather_state(self):
+        """The state vector x of the first n particles (particles.py:200-210)."""
+        n, d = self.n, self.dim
+        self.x[0, :n] = self.m[:n]
+        self.x[1:1 + d, :n] = self.r[:n].T
+        self.x[4:4 + d, :n] = self.v[:n].T
+        return self.x
+
+    def scatter_state(self, x):
+        """Particle arrays from the state vector x (particles.py:212-221)."""
+        n, d = self.n, self.dim
+        self.m[:n] = x[0, :n]
+        self.r[:n] = x[1:1 + d, :n].T
+        self.v[:n] = x[4:4 + d, :n].T
+
+    def gather_derivatives(self):
+        """The rates xdot of the state vector (particles.py:223-233)."""
+        n, d = self.n, self.dim
+        self.xdot[0, :n] = self.mdot[:n]
+        self.xdot[1:1 + d, :n] = self.rdot[:n].T
+        self.xdot[4:4 + d, :n] = self.vdot[:n].T
+        return self.xdot
 
 
 class SmoothParticleSystem(ParticleSystem):
@@ -94,6 +138,8 @@ class SmoothParticleSystem(ParticleSystem):
                  in mixed precision, 1.5x faster; elsewhere the cell scheme
                  runs); same pair set, rounding differs
     """
+
+    N_VARIABLES = 11   # + rho, p, pco, u (particles.py:355-358)
 
     def __init__(self, n, d=3, maxn=100, controllers=(), xmax=XMAX, ymax=YMAX, zmax=ZMAX,
                  vmax=VMAX, rinit=None, side=None, mass=1.0, spacing=None, temperature=1.0,
@@ -283,6 +329,31 @@ class SmoothParticleSystem(ParticleSystem):
         self._download(e.properties)
         self.steps += nsteps
         self.timing["update time"] = time.time() - t1
+
+    def gather_state(self):
+        """x with the smooth particle rows rho, p, pco, u (particles.py:496-511)."""
+        n = self.n
+        ParticleSystem.gather_state(self)
+        for row, a in zip(range(7, 11), (self.rho, self.p, self.pco, self.u)):
+            self.x[row, :n] = a[:n]
+        return self.x
+
+    def scatter_state(self, x):
+        """The inverse of gather_state (particles.py:513-526)."""
+        n = self.n
+        ParticleSystem.scatter_state(self, x)
+        for row, a in zip(range(7, 11), (self.rho, self.p, self.pco, self.u)):
+            a[:n] = x[row, :n]
+
+    def gather_derivatives(self):
+        """xdot with rhodot, zero rates for p and pco, and udot
+        (particles.py:528-542)."""
+        n = self.n
+        ParticleSystem.gather_derivatives(self)
+        self.xdot[7, :n] = self.rhodot[:n]
+        self.xdot[8:10, :n] = 0.0
+        self.xdot[10, :n] = self.udot[:n]
+        return self.xdot
 
     def apply_thermostat(self, target_temp):
         """Scaling thermostat on the host arrays (particles.py:450-457); the

@@ -38,6 +38,69 @@ def test_ponder_rebuild_host_logic():
     assert nl.rebuild_list is True
 
 
+def _filled_system(d, n=5, maxn=7, seed=11):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = SmoothParticleSystem(n, d=d, maxn=maxn)
+    for a in (p.r, p.v, p.m, p.rho, p.p, p.pco, p.u, p.vdot, p.udot, p.rhodot):
+        a[...] = rng.uniform(0.5, 2.0, a.shape)
+    p.rdot = p.v
+    return p
+
+
+@pytest.mark.parametrize("d", [2, 3])
+def test_state_vector_rows_follow_the_reference(d):
+    """gather_state / gather_derivatives fill the reference's 11 rows
+    (particles.py:496-511, 528-542): m, x, y, z, vx, vy, vz, rho, p, pco, u
+    and mdot, rdot, vdot, rhodot, 0, 0, udot; a 2D system leaves the z rows
+    at zero."""
+    p = _filled_system(d)
+    n = p.n
+    x = p.gather_state()
+    assert x.shape == (11, p.maxn)
+    assert np.array_equal(x[0, :n], p.m[:n])
+    for a in range(3):
+        want_r = p.r[:n, a] if a < d else np.zeros(n)
+        want_v = p.v[:n, a] if a < d else np.zeros(n)
+        assert np.array_equal(x[1 + a, :n], want_r)
+        assert np.array_equal(x[4 + a, :n], want_v)
+    for row, arr in zip(range(7, 11), (p.rho, p.p, p.pco, p.u)):
+        assert np.array_equal(x[row, :n], arr[:n])
+    assert not x[:, n:].any()                  # rows beyond n stay untouched
+    xd = p.gather_derivatives()
+    assert np.array_equal(xd[0, :n], p.mdot[:n])
+    for a in range(d):
+        assert np.array_equal(xd[1 + a, :n], p.v[:n, a])
+        assert np.array_equal(xd[4 + a, :n], p.vdot[:n, a])
+    assert np.array_equal(xd[7, :n], p.rhodot[:n])
+    assert not xd[8:10].any()
+    assert np.array_equal(xd[10, :n], p.udot[:n])
+
+
+@pytest.mark.parametrize("d", [2, 3])
+def test_scatter_state_inverts_gather_state(d):
+    p = _filled_system(d)
+    x = p.gather_state().copy()
+    x[:, :p.n] *= 3.0
+    q = _filled_system(d, seed=12)
+    q.scatter_state(x)
+    assert np.array_equal(q.gather_state(), x)
+    assert np.array_equal(q.r[:q.n], 3.0 * p.r[:p.n])
+    assert np.array_equal(q.u[:q.n], 3.0 * p.u[:p.n])
+
+
+def test_create_particle_appends_with_the_last_mass():
+    """particles.py:171-178: the new particle takes index n and the mass of
+    particle n - 1; the system refuses more than maxn particles."""
+    p = _filled_system(3, n=5, maxn=6)
+    p.create_particle((1.0, 2.0, 3.0))
+    assert p.n == 6
+    assert np.array_equal(p.r[5], [1.0, 2.0, 3.0])
+    assert p.m[5] == p.m[4]
+    assert not p.v[5].any()
+    with pytest.raises(ValueError):
+        p.create_particle((0.0, 0.0, 0.0))
+
+
 def test_periodic_box_teleports():
     r = np.array([[5.5, -0.1], [0.0, 5.0], [-2.0, 7.0]])
     wrap_teleport(r, (5.0, 5.0))
