@@ -3,9 +3,10 @@
 The force objects describe which terms the GPU derivative evaluation
 computes; the arithmetic runs in libsph's force pass:
 
-* SpamForce + CohesiveSpamForce (forces.py:321-405): van der Waals
-  repulsive pressure on the short smoothing length and cohesive pressure on
-  the long one, energy rate du = a.dv/2 per pair.
+* SpamForce + CohesiveSpamForce (forces.py:321-405), and their 2D forms
+  SpamForce2d + CohesiveSpamForce2d (:246-318): van der Waals repulsive
+  pressure on the short smoothing length and cohesive pressure on the long
+  one, energy rate du = a.dv/2 per pair.
 * SpamComplete (spam_complete_force.py:19-183): the same plus artificial
   viscosity (eta, zeta) and optionally the heat flux, in one call.
 * SpamConduction (c_forces.pyx:185-239): adds the heat-flux energy term.
@@ -49,6 +50,18 @@ class CohesiveSpamForce(Force):
 
     def __init__(self, particles, neighbour_list, cutoff=10.0):
         Force.__init__(self, particles, neighbour_list, cutoff=cutoff)
+
+
+class SpamForce2d(SpamForce):
+    """The 2D form of SpamForce (forces.py:246-274): the same terms, which
+    the engine evaluates in the system's dimension."""
+
+
+class CohesiveSpamForce2d(CohesiveSpamForce):
+    """The 2D cohesive force (forces.py:277-318).  The reference's active body
+    repeats the repulsive pressure term (p / rho^2, :300-318) and keeps the
+    cohesive one (pco / rho^2) commented out (:286-298); the engine computes
+    the cohesive term, as CohesiveSpamForce does in 3D."""
 
 
 class SpamConduction(Force):

@@ -188,8 +188,9 @@ class SmoothParticleSystem(ParticleSystem):
             raise RuntimeError("attach a neighbour list (p.nlists / p.nl_default)")
         return nl
 
-    def engine_params(self, dt):
-        """sph_params for the attached box, neighbour list and forces."""
+    def engine_params(self, dt, thermostat=None):
+        """sph_params for the attached box, neighbour list and forces
+        (thermostat overrides the system's own switch)."""
         if not isinstance(self.box, PeriodicBox):
             raise NotImplementedError("the GB300 engine needs a PeriodicBox "
                                       f"(got {type(self.box).__name__})")
@@ -201,23 +202,27 @@ class SmoothParticleSystem(ParticleSystem):
         cutoff, tol = nl._cutoff_tol()
         kw = dict(dim=self.dim, box=self.box.extents, h_short=float(hs[0]),
                   h_long=float(hl[0]), cutoff=cutoff, tolerance=tol, dt=float(dt),
-                  integrator=self.integrator, thermostat=bool(self.thermostat),
+                  integrator=self.integrator,
+                  thermostat=bool(self.thermostat if thermostat is None else thermostat),
                   thermostat_temp=float(self.thermostat_temp), adash=ADASH, bdash=BDASH,
                   kbdash=KBDASH)
         comp = [f for f in self.forces if isinstance(f, SpamComplete)]
-        kinds = {type(f) for f in self.forces}
+
+        def has(cls):
+            return any(isinstance(f, cls) for f in self.forces)
+
         if comp:
             f = comp[0]
             kw.update(kernel=f.kernel, adash=f.adash, bdash=f.bdash, kbdash=f.kbdash,
                       viscosity=(f.eta != 0.0 or f.zeta != 0.0), visc_alpha=f.eta,
                       visc_beta=f.zeta, visc_eps=f.visc_eps, sound_speed=f.sound_speed,
                       heat_flux=bool(f.heat_flux), thermalk=f.thermalk)
-        elif SpamForce in kinds and CohesiveSpamForce in kinds:
+        elif has(SpamForce) and has(CohesiveSpamForce):
             kw.update(kernel="lucy", viscosity=False)
         else:
             raise NotImplementedError("the GB300 engine evaluates SpamComplete or the "
                                       "SpamForce + CohesiveSpamForce pair")
-        if SpamConduction in kinds:
+        if has(SpamConduction):
             kw["heat_flux"] = True
         kw["collision_cutoff"] = self._collision_cutoff(cutoff, tol)
         return _abi.make_params(**kw)
@@ -252,8 +257,8 @@ class SmoothParticleSystem(ParticleSystem):
             raise NotImplementedError("collision range beyond the neighbour list's pairs")
         return float(f.cutoff)
 
-    def _ensure_engine(self, dt):
-        prm = self.engine_params(dt)
+    def _ensure_engine(self, dt, thermostat=None):
+        prm = self.engine_params(dt, thermostat)
         key = (repr(sorted(_abi.params_dict(prm).items())), self.n, self.precision)
         n = self.n
         if self._engine is None or self._engine_key != key:
@@ -317,18 +322,22 @@ class SmoothParticleSystem(ParticleSystem):
     def run(self, dt, nsteps):
         """nsteps integrator steps with one upload and one download."""
         t1 = time.time()
-        self.dt = dt
         t = time.time()
         self.rebuild_lists()
         self.timing["nlist rebuild time"] = time.time() - t
-        e = self._ensure_engine(dt)
+        self._advance(dt, nsteps)
+        self.steps += nsteps
+        self.timing["update time"] = time.time() - t1
+
+    def _advance(self, dt, nsteps, thermostat=None):
+        """nsteps engine steps from the host arrays back into them."""
+        self.dt = dt
+        e = self._ensure_engine(dt, thermostat)
         t = time.time()
         e.advance(nsteps)
         e.sync()
         self.timing["integrate time"] = time.time() - t
         self._download(e.properties)
-        self.steps += nsteps
-        self.timing["update time"] = time.time() - t1
 
     def gather_state(self):
         """x with the smooth particle rows rho, p, pco, u (particles.py:496-511)."""

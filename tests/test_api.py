@@ -7,9 +7,10 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from pyticles_gb300 import (CohesiveSpamForce, MirrorBox, NeighbourList, ParticleSystem,
-                            PeriodicBox, SmoothParticleSystem, SortedVerletList, SpamComplete,
-                            SpamForce, VerletList, workloads)
+from pyticles_gb300 import (CohesiveSpamForce, CohesiveSpamForce2d, MirrorBox, NeighbourList,
+                            ParticleSystem, PeriodicBox, SmoothParticleSystem, SortedVerletList,
+                            SpamComplete, SpamForce, SpamForce2d, VerletList, integrator,
+                            workloads)
 from pyticles_gb300.box import wrap_teleport
 from tests.golden_cases import load, params_of, rel_l2, sort_pairs
 
@@ -131,6 +132,27 @@ def test_engine_params_from_reference_objects():
     assert (prm.h_short, prm.h_long, prm.dt, prm.thermostat_temp) == (3.0, 6.0, 2e-3, 0.4)
     p.forces = [SpamForce(p, nl), CohesiveSpamForce(p, nl)]
     assert p.engine_params(1e-3).viscosity == 0
+    # the 2D classes (forces.py:246-318) configure the same evaluation
+    p.forces = [SpamForce2d(p, nl), CohesiveSpamForce2d(p, nl)]
+    prm2 = p.engine_params(1e-3)
+    assert (prm2.kernel, prm2.viscosity, prm2.heat_flux) == (2, 0, 0)
+    assert p.engine_params(1e-3, thermostat=False).thermostat == 0
+
+
+def test_integrator_takes_only_a_systems_own_methods():
+    """integrator.euler/imp_euler/rk4 run the engine step for the system
+    whose gather_state, derivatives, gather_derivatives and scatter_state
+    they get; anything else has no host integrator to fall back on."""
+    p = SmoothParticleSystem(4, d=2, maxn=4)
+    q = SmoothParticleSystem(4, d=2, maxn=4)
+    own = (p.gather_state, p.derivatives, p.gather_derivatives, p.scatter_state)
+    assert integrator._system(*own) is p
+    mixed = (p.gather_state, q.derivatives, p.gather_derivatives, p.scatter_state)
+    swapped = (p.gather_state, p.derivatives, p.gather_state, p.scatter_state)
+    for fns in (mixed, swapped, (lambda: None,) + own[1:]):
+        for step in (integrator.euler, integrator.imp_euler, integrator.rk4):
+            with pytest.raises(NotImplementedError):
+                step(*fns, 1e-3)
 
 
 # ---- evaluation (GPU) ----
@@ -266,3 +288,41 @@ def test_spam_properties_matches_reference():
     for k in ("rho", "p", "pco", "u", "t"):
         a, b = getattr(p, k)[:n], g[k]
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-12, k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,fn", [("ieuler", integrator.imp_euler), ("rk4", integrator.rk4),
+                                     ("euler", integrator.euler)])
+def test_integrator_functions_run_the_engine_step(name, fn):
+    """integrator.<fn>(p.gather_state, p.derivatives, p.gather_derivatives,
+    p.scatter_state, dt) followed by the box wrap gives the bits of update(dt)
+    on a twin system set to that integrator (particles.py:485-488)."""
+    g = load("lucy2d_400")
+    twins = []
+    for integ in ("ieuler", name):
+        box = PeriodicBox(xmax=float(g["box"][0]), ymax=float(g["box"][1]), zmax=1)
+        n = len(g["r0"])
+        p = SmoothParticleSystem(n, d=2, maxn=n, hshort=float(g["h_short"]),
+                                 hlong=float(g["h_long"]), simbox=box, integrator=integ,
+                                 precision="fp64")
+        p.r[:] = g["r0"]
+        p.v[:] = g["v0"]
+        p.m[:] = g["m"]
+        p.u[:] = g["u0"]
+        nl = VerletList(p, cutoff=float(g["cutoff"]), tolerance=0.0)
+        p.nlists.append(nl)
+        p.nl_default = nl
+        p.forces.append(SpamComplete(p, nl, eta=0.0, zeta=0.0))
+        twins.append(p)
+    a, b = twins
+    dt = float(g["dt"])
+    for _ in range(3):
+        fn(a.gather_state, a.derivatives, a.gather_derivatives, a.scatter_state, dt)
+        a.box.apply(a)
+        b.update(dt)
+    assert a.integrator == "ieuler"          # the call leaves the system's own choice
+    for k in ("r", "v", "u", "rho", "vdot", "udot"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    a.close()
+    b.close()
+
