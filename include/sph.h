@@ -24,6 +24,7 @@
  *                                       forces.SpamForce/CohesiveSpamForce forces.py:321-405
  *   sph_sim_pair_count / export_pairs   VerletList.build + separations   neighbour_list.py:160-189, 63-83
  *   sph_tuning.rebin, sph_rebin_count   VerletList.compress/ponder_rebuild neighbour_list.py:191-234
+ *   sph_kernel_eval                     spkernel.kernel / lucy_kernel ... spkernel.py:22-153
  *   sph_collide_pairs                   CollisionForce / CollisionForce3d forces.py:87-243
  *                                       FortranCollisionForce            forces.py:454-474
  *                                       Force.apply (cutoff test)        forces.py:38-42
@@ -277,6 +278,18 @@ int sph_splash_map(int32_t mode, int64_t n, const double *r, int32_t r_cols, con
                    const double *rho, const double *a, const double *h, int32_t nx, int32_t ny,
                    const double *x, const double *y, double z, const double *bounds,
                    double cutoff, double *Z, int32_t mem, void *stream);
+
+/* The smoothing kernel of the pair passes at n distances r (spkernel.kernel,
+ * gauss_kernel, lucy_kernel, debrun_kernel, lucy_w, lucy_w3d,
+ * spkernel.py:22-153): w[k] = W(r[k], h) and g[k] = (dW/dr)/r, so that
+ * dwdx = g (r_j - r_i) in Lucy's sign convention for every kernel (the
+ * reference's Gaussian returns -g dx, spkernel.py:51).  kernel: enum
+ * sph_kernel; dim 2 or 3; precision: the arithmetic of the pair passes
+ * (SPH_MIXED evaluates in FP32 on FP32-rounded r).  mem tags r, w and g.
+ * Runs on `stream` (NULL: the default stream) and returns once w and g are
+ * written. */
+int sph_kernel_eval(int32_t kernel, int32_t dim, double h, int32_t precision, int64_t n,
+                    const double *r, double *w, double *g, int32_t mem, void *stream);
 
 /* Hard collisions over a given pair list: Force.apply of CollisionForce
  * (mode SPH_COLLIDE_EXCHANGE, dim 2), FortranCollisionForce (EXCHANGE, the

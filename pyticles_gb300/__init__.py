@@ -12,6 +12,7 @@ Reference-facing API (same names as andrewcharles/pyticles):
     PeriodicBox
     properties.spam_properties, vdw, vdw_energy, vdw_temp
     integrator.euler, imp_euler, rk4         (the engine step of a system)
+    spkernel.kernel, lucy_kernel, gauss_kernel, debrun_kernel, lucy_w, lucy_w3d
 Engine-level API: Engine (many simulations per engine), workloads, serve.
 """
 from ._abi import KERNELS, SphError, SphParams, make_params  # noqa: F401
@@ -22,6 +23,6 @@ from .forces import (CohesiveSpamForce, CohesiveSpamForce2d, CollisionForce,  # 
                      SpamConduction, SpamForce, SpamForce2d)
 from .neighbour_list import NeighbourList, SortedVerletList, VerletList  # noqa: F401
 from .particles import ParticleSystem, SmoothParticleSystem  # noqa: F401
-from . import integrator, properties  # noqa: F401
+from . import integrator, properties, spkernel  # noqa: F401
 
 __version__ = "0.1.0"

@@ -198,6 +198,7 @@ def _declare(lib):
         "sph_derivatives_noalloc": [P(SphParams), c_i32, c_i64] + [vp] * 13,
         "sph_splash_map": [c_i32, c_i64, vp, c_i32, vp, vp, vp, vp, c_i32, c_i32, vp, vp,
                            ctypes.c_double, vp, ctypes.c_double, vp, c_i32, vp],
+        "sph_kernel_eval": [c_i32, c_i32, ctypes.c_double, c_i32, c_i64, vp, vp, vp, c_i32, vp],
         "sph_collide_pairs": [c_i32, c_i32, c_i64, vp, vp, vp, c_i64, vp, vp, vp,
                               ctypes.c_double, c_i32, vp],
         "sph_status_string": [ctypes.c_int],
@@ -219,7 +220,8 @@ def exported_symbols():
             "sph_sim_export_pairs", "sph_last_pair_total", "sph_sim_diagnostics",
             "sph_get_tuning", "sph_set_tuning", "sph_rebin_count", "sph_prepare", "sph_profile",
             "sph_profile_read", "sph_kernels_per_step", "sph_sync", "sph_sim_status",
-            "sph_splash_map", "sph_collide_pairs", "sph_derivatives_noalloc", "sph_status_string", "sph_version"]
+            "sph_splash_map", "sph_kernel_eval", "sph_collide_pairs", "sph_derivatives_noalloc",
+            "sph_status_string", "sph_version"]
 
 
 def lib():

@@ -153,22 +153,6 @@ namespace {
 
 int nstage_of(int integ) { return integ == SPH_EULER ? 1 : (integ == SPH_RK4 ? 4 : 2); }
 
-double kernel_sigma(int kernel, int dim, double h) {
-    const double pi = 3.14159265358979323846;
-    switch (kernel) {
-        case SPH_KERNEL_LUCY:
-            return dim == 2 ? 5.0 / (pi * h * h) : 105.0 / (pi * 16.0 * (h * h * h));
-        case SPH_KERNEL_GAUSSIAN:
-            return 1.0 / (std::pow(h, dim) * std::pow(pi, dim / 2.0));
-        case SPH_KERNEL_DEBRUN: {
-            double h2 = h * h, h6 = h2 * h2 * h2;
-            return dim == 2 ? 10.0 / (pi * h6) : 15.0 / (pi * h6);
-        }
-        default:
-            return dim == 2 ? 10.0 / (7.0 * pi * h * h) : 1.0 / (pi * h * h * h);
-    }
-}
-
 double kernel_w0(int kernel, int dim, double h) {
     double sig = kernel_sigma(kernel, dim, h);
     switch (kernel) {
@@ -311,19 +295,9 @@ void fill_const(SimConst<R> &c, const sph_engine *e, const Sim &S, const SimDev 
                                                : (R)1e30;
     }
     const double hh[2] = {p.h_short, p.h_long}, sg[2] = {d.sig_s, d.sig_l};
-    for (int k = 0; k < 2; ++k) {
-        double h = hh[k], sig = sg[k];
-        c.h[k] = (R)h;
-        c.inv_h[k] = (R)(1.0 / h);
-        c.inv_h_lo[k] = (R)(1.0 / h - (double)c.inv_h[k]);
-        c.sig[k] = (R)sig;
-        switch (p.kernel) {
-            case SPH_KERNEL_LUCY: c.g0[k] = (R)(-12.0 * sig / (h * h)); break;
-            case SPH_KERNEL_GAUSSIAN: c.g0[k] = (R)(-2.0 / (h * h)); break;  // times sig later
-            case SPH_KERNEL_CUBIC: c.g0[k] = (R)(sig / (h * h)); break;
-            default: c.g0[k] = (R)(-3.0 * sig); break;
-        }
-    }
+    for (int k = 0; k < 2; ++k)
+        kernel_consts<R>(p.kernel, hh[k], sg[k], c.h[k], c.inv_h[k], c.inv_h_lo[k], c.sig[k],
+                         c.g0[k]);
     c.hs = (R)p.h_short;
     c.eps_h2 = (R)(p.visc_eps * p.h_short * p.h_short);
     c.alpha_c = (R)(p.visc_alpha * p.sound_speed);
@@ -1880,6 +1854,22 @@ int sph_sim_status(sph_engine *e, int32_t id, int32_t *status) {
 }  // extern "C"
 
 namespace sph {
+
+double kernel_sigma(int kernel, int dim, double h) {
+    const double pi = 3.14159265358979323846;
+    switch (kernel) {
+        case SPH_KERNEL_LUCY:
+            return dim == 2 ? 5.0 / (pi * h * h) : 105.0 / (pi * 16.0 * (h * h * h));
+        case SPH_KERNEL_GAUSSIAN:
+            return 1.0 / (std::pow(h, dim) * std::pow(pi, dim / 2.0));
+        case SPH_KERNEL_DEBRUN: {
+            double h2 = h * h, h6 = h2 * h2 * h2;
+            return dim == 2 ? 10.0 / (pi * h6) : 15.0 / (pi * h6);
+        }
+        default:
+            return dim == 2 ? 10.0 / (7.0 * pi * h * h) : 1.0 / (pi * h * h * h);
+    }
+}
 
 // Host-side tables of one simulation laid out on its own (cell offset 0,
 // particle offset 0): device constants, linear-cell -> Morton map and packed

@@ -34,6 +34,30 @@ template <typename R> struct SimConst {
     R hs, eps_h2, alpha_c, beta, pl2, kappa;
 };
 
+// Normalisation sigma of a smoothing kernel (W = sigma w(q)) in dim 2 or 3:
+// Lucy and Debrun as spkernel.py:86-153, the Gaussian's 1/(h^d pi^(d/2))
+// (spkernel.py:39-52), the M4 cubic spline's 10/(7 pi h^2) and 1/(pi h^3).
+double kernel_sigma(int kernel, int dim, double h);
+
+// Device constants of one smoothing length: h, 1/h as a hi/lo pair, sigma
+// and the gradient factor g0 (Lucy -12 sigma/h^2, Gaussian -2/h^2 with sigma
+// applied in the kernel, cubic sigma/h^2, Debrun -3 sigma).  The pair passes'
+// tables and sph_kernel_eval take them from here alike.
+template <typename R>
+inline void kernel_consts(int kernel, double h, double sig, R &h_r, R &inv_h, R &inv_h_lo,
+                          R &sig_r, R &g0) {
+    h_r = (R)h;
+    inv_h = (R)(1.0 / h);
+    inv_h_lo = (R)(1.0 / h - (double)inv_h);
+    sig_r = (R)sig;
+    switch (kernel) {
+        case SPH_KERNEL_LUCY: g0 = (R)(-12.0 * sig / (h * h)); break;
+        case SPH_KERNEL_GAUSSIAN: g0 = (R)(-2.0 / (h * h)); break;
+        case SPH_KERNEL_CUBIC: g0 = (R)(sig / (h * h)); break;
+        default: g0 = (R)(-3.0 * sig); break;
+    }
+}
+
 // Per-simulation constants on the device.
 struct SimDev {
     double L[3], half_L[3], inv_L[3];
