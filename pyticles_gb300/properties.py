@@ -9,17 +9,33 @@ built list); the velocity gradient tensor p.gradv, which no force uses, is
 not computed.  pyticles' run scripts call it once to initialise u from T.
 
 vdw, vdw_energy, vdw_temp -- the equation-of-state formulas of
-properties.py:38-49 on host arrays, for setting up states.
+properties.py:38-49 on host arrays, for setting up states; ideal_isothermal
+and art_water, the reference's other equations of state (properties.py:
+24-36), likewise (the engine's step uses van der Waals).
+
+hamiltonian(p) -- the total energy sum(m v^2 / 2) + sum(u) of the host
+arrays, printed and returned (properties.py:55-60).
 """
 import numpy as np
 
 from . import _abi
 from .engine import Engine
 
-# properties.py:18-20
+# properties.py:18-21
 ADASH = 2.0
 BDASH = 0.5
 KBDASH = 1.0
+RHONAUGHT = 1.0
+
+
+def ideal_isothermal(rho, t):
+    """Isothermal kinetic pressure rho k_B (properties.py:24-29)."""
+    return rho * KBDASH
+
+
+def art_water(rho, t):
+    """Compressible liquid about the reference density (properties.py:32-36)."""
+    return (rho - RHONAUGHT) * KBDASH
 
 
 def vdw(rho, t):
@@ -38,6 +54,16 @@ def vdw_temp(rho, u):
 
 
 calc_pressure = vdw
+
+
+def hamiltonian(p):
+    """Kinetic plus internal energy of the first p.n particles, the internal
+    energy summed without a mass factor as in properties.py:55-60."""
+    n = p.n
+    v = np.asarray(p.v[:n], dtype=np.float64)
+    h = float(np.sum(0.5 * p.m[:n] * np.sum(v * v, axis=1)) + np.sum(p.u[:n]))
+    print(h)
+    return h
 
 
 def summation_density(p, nl, precision=None):

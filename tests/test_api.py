@@ -102,6 +102,20 @@ def test_create_particle_appends_with_the_last_mass():
         p.create_particle((0.0, 0.0, 0.0))
 
 
+def test_property_formulas(capsys):
+    """properties.py:24-60: the equations of state and the Hamiltonian
+    (kinetic energy plus the unweighted sum of u), printed and returned."""
+    from pyticles_gb300 import properties
+    rho, t = np.array([0.5, 1.5]), np.array([0.6, 1.2])
+    assert np.array_equal(properties.ideal_isothermal(rho, t), rho)
+    assert np.array_equal(properties.art_water(rho, t), rho - 1.0)
+    assert np.allclose(properties.vdw_temp(rho, properties.vdw_energy(rho, t)), t)
+    p = _filled_system(3)
+    want = sum(0.5 * p.m[i] * (p.v[i] @ p.v[i]) + p.u[i] for i in range(p.n))
+    assert properties.hamiltonian(p) == pytest.approx(want, rel=1e-14)
+    assert float(capsys.readouterr().out) == pytest.approx(want, rel=1e-14)
+
+
 def test_periodic_box_teleports():
     r = np.array([[5.5, -0.1], [0.0, 5.0], [-2.0, 7.0]])
     wrap_teleport(r, (5.0, 5.0))
