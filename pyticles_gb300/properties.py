@@ -13,6 +13,8 @@ properties.py:38-49 on host arrays, for setting up states; ideal_isothermal
 and art_water, the reference's other equations of state (properties.py:
 24-36), likewise (the engine's step uses van der Waals).
 
+spam_properties_ls(p, nl) -- the same with rho_lr at the long length.
+
 hamiltonian(p) -- the total energy sum(m v^2 / 2) + sum(u) of the host
 arrays, printed and returned (properties.py:55-60).
 """
@@ -68,6 +70,11 @@ def hamiltonian(p):
 
 def summation_density(p, nl, precision=None):
     """rho at the short smoothing length p.h[0] on the GPU (Lucy kernel)."""
+    return _densities(p, nl, precision)[0]
+
+
+def _densities(p, nl, precision=None):
+    """rho and rho_lr at p.h[0] and p.hlr[0] on the GPU (Lucy kernel)."""
     n = p.n
     cutoff, tol = nl._cutoff_tol()
     prm = _abi.make_params(dim=p.dim, kernel="lucy", box=p.box.extents,
@@ -78,7 +85,7 @@ def summation_density(p, nl, precision=None):
         s = e.add(prm, p.r[:n], p.v[:n], p.m[:n], np.zeros(n))
         out = e.derivatives(s)
         e.sync()
-    return out["rho"]
+    return out["rho"], out["rho_lr"]
 
 
 def spam_properties(p, nl):
@@ -87,6 +94,20 @@ def spam_properties(p, nl):
     n = p.n
     rho = summation_density(p, nl)
     p.rho[:n] = rho
+    p.p[:n], p.pco[:n] = calc_pressure(p.rho[:n], p.t[:n])
+    p.u[:n] = vdw_energy(p.rho[:n], p.t[:n])
+    p.t[:n] = vdw_temp(p.rho[:n], p.u[:n])
+
+
+def spam_properties_ls(p, nl):
+    """properties.spam_properties_ls (properties.py:123-188): spam_properties
+    with the density at the long smoothing length, p.rho_lr, as well (the
+    reference's body names the long length h_lr, which it never defines; it
+    is p.hlr).  Pressures and energies follow the short density, as there."""
+    n = p.n
+    rho, rho_lr = _densities(p, nl)
+    p.rho[:n] = rho
+    p.rho_lr[:n] = rho_lr
     p.p[:n], p.pco[:n] = calc_pressure(p.rho[:n], p.t[:n])
     p.u[:n] = vdw_energy(p.rho[:n], p.t[:n])
     p.t[:n] = vdw_temp(p.rho[:n], p.u[:n])

@@ -302,6 +302,22 @@ def test_spam_properties_matches_reference():
     for k in ("rho", "p", "pco", "u", "t"):
         a, b = getattr(p, k)[:n], g[k]
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-12, k
+    # spam_properties_ls: the same, plus rho_lr at the long length (the
+    # oracle's long density of the same state)
+    q = SmoothParticleSystem(n, d=3, maxn=n, hshort=float(g["h"]), hlong=float(g["hlr"]),
+                             simbox=box)
+    q.r[:] = g["r"]
+    q.v[:] = g["v"]
+    q.m[:] = g["m"]
+    q.t[:] = float(g["T0"])
+    properties.spam_properties_ls(q, nl)
+    for k in ("rho", "p", "pco", "u", "t"):
+        assert np.array_equal(getattr(q, k)[:n], getattr(p, k)[:n]), k
+    prm = params_of({"dim": 3, "kernel": "lucy", "box": [3.3] * 3, "h_short": float(g["h"]),
+                     "h_long": float(g["hlr"]), "cutoff": float(g["cutoff"]), "tolerance": 0.0,
+                     "dt": 1.0, "integrator": "ieuler", "thermostat": 0, "thermostat_temp": 1.0})
+    ref = oracle.derivatives(prm, q.r[:n], q.v[:n], q.m[:n], np.zeros(n))["rho_lr"]
+    assert np.linalg.norm(q.rho_lr[:n] - ref) / np.linalg.norm(ref) < 1e-12
 
 
 @pytest.mark.gpu
