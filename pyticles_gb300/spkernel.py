@@ -6,6 +6,7 @@ The functions keep the reference signatures and return conventions
 r has shape (n,) or is a scalar, dx the matching (n, dim) or (dim,).
 
   lucy_kernel, debrun_kernel -> w, dwdx = (dW/dr) dx / r (0 at r = 0)
+  cubic_kernel               -> the same for the M4 spline
   gauss_kernel               -> w, dwdx = -(dW/dr) dx / r, the reference's
                                 sign (spkernel.py:51)
   kernel(r, dx, h, type)     -> by name ('gaussian', 'lucy', 'debrun', and
@@ -43,8 +44,11 @@ def _with_gradient(kid, r, dx, h, sign, precision):
     if dim not in (2, 3):
         raise NotImplementedError("the engine's kernels are 2D and 3D")
     w, g = evaluate(r, h, kid, dim, precision)
-    # dwdx = g dx; at r = 0 the reference returns 0 for the gradient
-    gg = np.where(np.asarray(r) == 0.0, 0.0, sign * g)
+    # dwdx = g dx; at r = 0 Lucy and Debrun return 0 (spkernel.py:109-110,
+    # 144-145), the Gaussian its finite g dx
+    gg = sign * g
+    if kid in (2, 3):
+        gg = np.where(np.asarray(r) == 0.0, 0.0, gg)
     dwdx = np.asarray(gg)[..., None] * dx
     if np.ndim(r) == 0:
         return float(w), dwdx.reshape(dim)
