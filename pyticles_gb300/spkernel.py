@@ -44,8 +44,8 @@ def _with_gradient(kid, r, dx, h, sign, precision):
     if dim not in (2, 3):
         raise NotImplementedError("the engine's kernels are 2D and 3D")
     w, g = evaluate(r, h, kid, dim, precision)
-    # dwdx = g dx; at r = 0 Lucy and Debrun return 0 (spkernel.py:109-110,
-    # 144-145), the Gaussian its finite g dx
+    # dwdx = g dx; at r = 0 Lucy and Debrun return 0 (spkernel.py:108-109,
+    # 143-144), the Gaussian its finite g dx
     gg = sign * g
     if kid in (2, 3):
         gg = np.where(np.asarray(r) == 0.0, 0.0, gg)
