@@ -136,7 +136,9 @@ int sph_sim_add(sph_engine *e, const sph_params *p, int64_t n, const double *r,
                 const double *v, const double *m, const double *u, int32_t mem,
                 int32_t *sim_id);
 int sph_sim_remove(sph_engine *e, int32_t sim_id);
-/* Replaces the state of an existing simulation (same n). */
+/* Replaces the state of an existing simulation (same n): r, v, m and u
+ * together (all NULL changes nothing; some NULL is SPH_EINVAL, and then
+ * nothing is written). */
 int sph_sim_set_state(sph_engine *e, int32_t sim_id, const double *r, const double *v,
                       const double *m, const double *u, int32_t mem);
 /* Reads the state back in the caller's original particle order.

@@ -1406,15 +1406,15 @@ int sph_sim_remove(sph_engine *e, int32_t id) {
 int sph_sim_set_state(sph_engine *e, int32_t id, const double *r, const double *v,
                       const double *m, const double *u, int32_t mem) {
     TRY(check_sim(e, id));
+    const bool all = r && v && m && u;
+    // the state is given in original order, which holds for a full update
+    // only (checked before anything is written)
+    if (!all && (r || v || m || u)) return SPH_EINVAL;
     Sim &S = e->sims[id];
     // A holds the simulation in slot order a_off + k with id[k]; the caller
     // gives original order, so reset ids to identity for the range.
     TRY(write_state_range(e, S.a_off, S.n, r, v, m, u, mem));
-    if (r && v && m && u) launch_iota_sim(e->a_id + S.a_off, e->a_sim + S.a_off, id, (int)S.n, e->stream);
-    else if (r || v || m || u) {
-        // partial updates need the identity order first
-        return SPH_EINVAL;
-    }
+    if (all) launch_iota_sim(e->a_id + S.a_off, e->a_sim + S.a_off, id, (int)S.n, e->stream);
     CK(cudaStreamSynchronize(e->stream));
     e->props_valid = false;
     e->bins_valid = false;
@@ -1452,6 +1452,7 @@ int sph_sim_get_state(sph_engine *e, int32_t id, double *r, double *v, double *u
 
 int sph_sim_count(sph_engine *e, int32_t id, int64_t *n) {
     TRY(check_sim(e, id));
+    if (!n) return SPH_EINVAL;
     *n = e->sims[id].n;
     return SPH_OK;
 }
@@ -1614,6 +1615,7 @@ int sph_sim_get_properties(sph_engine *e, int32_t id, double *rho, double *rho_l
 
 int sph_sim_pair_count(sph_engine *e, int32_t id, int64_t *nip) {
     TRY(check_sim(e, id));
+    if (!nip) return SPH_EINVAL;
     TRY(ensure_layout(e));
     cudaStream_t st = e->stream;
     if (e->cl.on) {
@@ -1718,6 +1720,7 @@ int sph_last_pair_total(sph_engine *e, int64_t *pairs) {
 
 int sph_sim_diagnostics(sph_engine *e, int32_t id, double out[6]) {
     TRY(check_sim(e, id));
+    if (!out) return SPH_EINVAL;
     const Sim &S = e->sims[id];
     size_t n = (size_t)S.n, d = (size_t)e->dim;
     std::vector<double> v(n * d), u(n), m(n), t(n, 0.0);

@@ -105,10 +105,22 @@ def test_argument_errors_are_reported():
         with pytest.raises(SphError) as ei:
             e.add(bad, r, v, m, u)                          # other kernel than the group
         assert ei.value.status == _abi.SPH_EINVAL
-        e.add(prm, r, v, m, u)
+        s = e.add(prm, r, v, m, u)
         with pytest.raises(SphError) as ei:
             e.add(prm, r, v, m, u)                          # no simulation slot left
         assert ei.value.status == _abi.SPH_ECAPACITY
+        # output pointers that are NULL are refused, not written through
+        lib, h = _abi.lib(), e._h
+        assert lib.sph_sim_count(h, s, None) == _abi.SPH_EINVAL
+        assert lib.sph_sim_pair_count(h, s, None) == _abi.SPH_EINVAL
+        assert lib.sph_sim_diagnostics(h, s, None) == _abi.SPH_EINVAL
+        # a partial state update is refused before anything is written
+        before = e.get_state(s)
+        r2 = np.ascontiguousarray(r + 0.5)
+        assert lib.sph_sim_set_state(h, s, r2.ctypes.data, None, None, None,
+                                     _abi.SPH_HOST) == _abi.SPH_EINVAL
+        for a, b in zip(e.get_state(s), before):
+            assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("dim", [2, 3])
