@@ -167,6 +167,14 @@ def test_integrator_takes_only_a_systems_own_methods():
         for step in (integrator.euler, integrator.imp_euler, integrator.rk4):
             with pytest.raises(NotImplementedError):
                 step(*fns, 1e-3)
+    # a system the engine refuses (no periodic box) keeps its own integrator
+    nl = VerletList(p, cutoff=1.0, tolerance=0.0)
+    p.nlists.append(nl)
+    p.forces.append(SpamComplete(p, nl))
+    for step in (integrator.euler, integrator.rk4):
+        with pytest.raises(NotImplementedError):
+            step(*own, 1e-3)
+        assert p.integrator == "ieuler"
 
 
 # ---- evaluation (GPU) ----
