@@ -56,6 +56,8 @@ def lib():
         L.orc_collide_pairs.argtypes = [ctypes.c_int32, ctypes.c_int32, i64, vp, vp, vp, i64,
                                         vp, vp, vp, ctypes.c_double]
         L.orc_collide_pairs.restype = ctypes.c_int
+        L.orc_set_geometry32.argtypes = [ctypes.c_int]
+        L.orc_set_geometry32.restype = None
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_set_threads.restype = None
         L.orc_get_threads.restype = ctypes.c_int
@@ -99,21 +101,27 @@ def pairs(params, r, brute=False):
     return iap[:cap], rsq[:cap]
 
 
-def derivatives(params, r, v, m, u):
+def derivatives(params, r, v, m, u, geometry32=False):
     """One evaluation f(x).  Returns a dict of rho, rho_lr, t, p, pco, vdot,
-    udot, jq and nip."""
+    udot, jq and nip.  geometry32: each pair's separation and distance
+    rounded to the nearest FP32 numbers (the FP32-geometry error floor;
+    the pair set is unchanged)."""
     r, v, m, u = _c(r), _c(v), _c(m), _c(u)
     n, d = r.shape
     out = {k: np.zeros(n) for k in ("rho", "rho_lr", "t", "p", "pco", "udot")}
     out["vdot"] = np.zeros((n, d))
     out["jq"] = np.zeros((n, d))
     nip = ctypes.c_int64()
-    st = lib().orc_derivatives(ctypes.byref(params), n, r.ctypes.data, v.ctypes.data,
-                               m.ctypes.data, u.ctypes.data, out["rho"].ctypes.data,
-                               out["rho_lr"].ctypes.data, out["t"].ctypes.data,
-                               out["p"].ctypes.data, out["pco"].ctypes.data,
-                               out["vdot"].ctypes.data, out["udot"].ctypes.data,
-                               out["jq"].ctypes.data, ctypes.byref(nip))
+    lib().orc_set_geometry32(1 if geometry32 else 0)
+    try:
+        st = lib().orc_derivatives(ctypes.byref(params), n, r.ctypes.data, v.ctypes.data,
+                                   m.ctypes.data, u.ctypes.data, out["rho"].ctypes.data,
+                                   out["rho_lr"].ctypes.data, out["t"].ctypes.data,
+                                   out["p"].ctypes.data, out["pco"].ctypes.data,
+                                   out["vdot"].ctypes.data, out["udot"].ctypes.data,
+                                   out["jq"].ctypes.data, ctypes.byref(nip))
+    finally:
+        lib().orc_set_geometry32(0)
     assert st == 0, st
     out["nip"] = nip.value
     return out

@@ -90,6 +90,23 @@ typedef struct {
 
 static int g_threads = 0;
 
+/* FP32 pair geometry (orc_set_geometry32): every pair's separation vector
+ * and distance are replaced by the FP32 numbers nearest to them before any
+ * kernel or force term uses them; the pair set and everything else stay
+ * FP64.  The change this makes to a result is the error floor of any
+ * evaluation that carries pair geometry in FP32, however accurate its other
+ * arithmetic: the reference against which the mixed-precision passes are
+ * held on near-lattice systems whose pair forces cancel. */
+static int g_geom32 = 0;
+
+void orc_set_geometry32(int on) { g_geom32 = on ? 1 : 0; }
+
+static inline void geometry32(int dim, double *dr, double *rsq) {
+    for (int a = 0; a < dim; ++a) dr[a] = (double)(float)dr[a];
+    double r = (double)(float)sqrt(*rsq);
+    *rsq = r * r; /* exact: sqrt(*rsq) is then r again */
+}
+
 void orc_set_threads(int n) { g_threads = n; }
 
 int orc_get_threads(void) {
@@ -308,6 +325,7 @@ static int grid_neighbours(const sph_params *p, const grid_t *g, const double *r
                 double dr[3] = {0, 0, 0};                                          \
                 double rsq = pair_rsq((P), &(R)[(I) * (P)->dim], &(R)[j * (P)->dim], dr); \
                 if (!(rsq < _thr)) continue;                                       \
+                if (g_geom32) geometry32((P)->dim, dr, &rsq);                      \
                 __VA_ARGS__                                                        \
             }                                                                      \
         }                                                                          \

@@ -165,3 +165,33 @@ def test_spam_properties_formulas_match_reference():
                      "thermostat_temp": 1.0})
     d = oracle.derivatives(prm, g["r"], g["v"], g["m"], np.zeros(len(rho)))
     assert rel_l2(d["rho"], rho) < EVAL_TOL
+
+
+def test_floors_fixture_is_what_the_oracle_computes():
+    """tests/golden/floors.json (make_floors.py) holds the conditioning floors
+    the mixed-precision parity bounds are built on; recomputing them from the
+    oracle gives the committed numbers."""
+    from tests.golden.make_floors import floors
+    from tests.golden_cases import load_floors
+    committed = load_floors()
+    fresh = floors()
+    assert sorted(committed) == sorted(fresh) == sorted(SYSTEMS)
+    for name in SYSTEMS:
+        for kind in ("position", "geometry"):
+            for k, x in fresh[name][kind].items():
+                assert committed[name][kind][k] == pytest.approx(x, rel=1e-9), (name, kind, k)
+
+
+def test_geometry_floor_only_rounds_the_pair_geometry():
+    """The FP32-geometry mode keeps the pair set and moves the evaluation by
+    FP32-sized amounts, not more."""
+    g = load("lucy2d_400")
+    prm = params_of(g)
+    a = oracle.derivatives(prm, g["r0"], g["v0"], g["m"], g["u0"])
+    b = oracle.derivatives(prm, g["r0"], g["v0"], g["m"], g["u0"], geometry32=True)
+    c = oracle.derivatives(prm, g["r0"], g["v0"], g["m"], g["u0"])
+    assert a["nip"] == b["nip"] == len(g["iap"])
+    assert 0 < rel_l2(b["rho"], a["rho"]) < 1e-7
+    assert 0 < rel_l2(b["vdot"], a["vdot"]) < 1e-5
+    for k in ("rho", "vdot", "udot"):       # the mode is off again afterwards
+        assert np.array_equal(a[k], c[k])
