@@ -20,6 +20,8 @@ CollisionForce3d, p.r) over the neighbour list's pairs on the device
 (sph_collide_pairs); inside SmoothParticleSystem.update the engine applies
 CollisionForce / FortranCollisionForce after every evaluation itself.
 """
+import warnings
+
 import numpy as np
 
 from . import _abi
@@ -72,14 +74,34 @@ class SpamConduction(Force):
         Force.__init__(self, particles, nl)
 
 
+_cgrad_warned = False
+
+
+def _warn_cgrad():
+    global _cgrad_warned
+    if not _cgrad_warned:
+        _cgrad_warned = True
+        warnings.warn("SpamComplete: the density-gradient term (cgrad) of the reference's "
+                      "absent Fortran force is not computed; the evaluation runs without it "
+                      "(pass cgrad=0.0 to silence this warning)", RuntimeWarning, stacklevel=3)
+
+
 class SpamComplete(Force):
     """All smooth-particle properties and forces in one evaluation
     (spam_complete_force.py:19-60).
 
     adash, bdash, kbdash -- van der Waals a, b, k_B
-    sigma, rcoef, cgrad  -- accepted for compatibility; the repulsive core and
-                            density-gradient terms live in the absent Fortran
-                            and are not computed (sigma = rcoef = 0 defaults)
+    sigma, rcoef         -- the repulsive core (spam_complete_force.py:40-41,
+                            55-56) lives in the absent Fortran: non-zero
+                            values raise NotImplementedError
+    cgrad                -- the density-gradient term (spam_complete_force.py:
+                            42, 57) lives in the absent Fortran too and is NOT
+                            computed at any value, its reference default 1.0
+                            included: a non-zero cgrad warns once
+                            (RuntimeWarning) and the evaluation runs without
+                            the term, as the reference's own drivers
+                            configure it (nanobox_quench.py:93 passes
+                            cgrad=0.0)
     eta, zeta            -- artificial viscosity: Monaghan alpha = eta,
                             beta = zeta, sound speed 1 (the reference passes
                             c = 1, :142)
@@ -96,6 +118,8 @@ class SpamComplete(Force):
         if sigma != 0.0 or rcoef != 0.0:
             raise NotImplementedError("the repulsive core (sigma, rcoef) has no source in "
                                       "pyticles and is not implemented")
+        if cgrad != 0.0:
+            _warn_cgrad()
         self.adash, self.bdash, self.kbdash = adash, bdash, kbdash
         self.sigma, self.rcoef, self.cgrad = sigma, rcoef, cgrad
         self.eta, self.zeta = eta, zeta

@@ -177,6 +177,30 @@ def test_integrator_takes_only_a_systems_own_methods():
         assert p.integrator == "ieuler"
 
 
+def test_spam_complete_reports_the_terms_it_does_not_compute():
+    """sigma / rcoef (repulsive core) raise; cgrad (density-gradient term,
+    reference default 1.0) warns once and is not computed; cgrad = 0, as the
+    reference's drivers pass it, is silent."""
+    import warnings
+
+    from pyticles_gb300 import forces
+    p = SmoothParticleSystem(4, d=2, maxn=4)
+    nl = VerletList(p, cutoff=1.0, tolerance=0.0)
+    with pytest.raises(NotImplementedError):
+        SpamComplete(p, nl, sigma=1.0, cgrad=0.0)
+    with pytest.raises(NotImplementedError):
+        SpamComplete(p, nl, rcoef=1.0, cgrad=0.0)
+    forces._cgrad_warned = False
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        SpamComplete(p, nl, cgrad=0.0)
+        assert not w
+        SpamComplete(p, nl)                 # the reference default cgrad = 1.0
+        SpamComplete(p, nl, cgrad=0.5)
+    assert len(w) == 1 and issubclass(w[0].category, RuntimeWarning)
+    assert "cgrad" in str(w[0].message)
+
+
 # ---- evaluation (GPU) ----
 
 @pytest.mark.gpu
