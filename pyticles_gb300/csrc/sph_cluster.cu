@@ -524,13 +524,13 @@ __global__ void __launch_bounds__(kBlock) k_cl_density(const __grid_constant__ V
     cl_for_pairs<false, kPfDensity>(
         v, c, x, wid, si, gi, pi,
         [&](int, const float4 &pj, const float *, float rsq, auto near) {
-            const float r = sqrtf(rsq);
+            const Dist<float> dd = plain_dist<float>(rsq);
             float w, g;
             if constexpr (decltype(near)::value) {
-                kernel_wg<K, float>(ks, r, &w, &g);
+                kernel_wg<K, float>(ks, dd, &w, &g);
                 rs.add(pj.w * w);
             }
-            kernel_wg<K, float>(kl, r, &w, &g);
+            kernel_wg<K, float>(kl, dd, &w, &g);
             rl.add(pj.w * w);
             ++cnt;
         },
@@ -595,9 +595,7 @@ __global__ void __launch_bounds__(kBlock) k_cl_heat(const __grid_constant__ View
     cl_for_pairs<true, kPfHeat>(
         v, c, x, wid, si, gi, pi,
         [&](int sj, const float4 &pj, const float *d, float rsq, auto) {
-            const float ir = rsqrt0(rsq);
-            const float r = rsq * ir;
-            const float g = kernel_g_ir<K>(ks, r, ir);
+            const float g = kernel_g<K, float, true>(ks, make_dist<float>(rsq));
             const float4 fj = c.cf[sj];   // {p/rho^2, 1/rho, T_hi, T_lo}
             const float dT = (fj.z - fi.z) + (fj.w - fi.w);
             const float f = pj.w * fj.y * dT * g;
@@ -656,14 +654,13 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_cl_force(const __grid_c
         v, c, x, wid, si, gi, pi,
         [&](int sj, const float4 &pj, const float *d, float rsq, auto near) {
             constexpr bool NEAR = decltype(near)::value;
-            const float ir = rsqrt0(rsq);
-            const float r = rsq * ir;
-            const float gl = kernel_g_ir<K>(kl, r, ir);
+            const Dist<float> dd = make_dist<float>(rsq);
+            const float gl = kernel_g<K, float, true>(kl, dd);
             const float4 fvj = c.cfv[sj];
             const float dvdx = (fvj.x - fvi.x) * d[0] + (fvj.y - fvi.y) * d[1] + (fvj.z - fvi.z) * d[2];
             float gsum = pl2 * gl, gs = 0.0f;
             if constexpr (NEAR) {
-                gs = kernel_g_ir<K>(ks, r, ir);
+                gs = kernel_g<K, float, true>(ks, dd);
                 float ps = fvi.w + fvj.w;
                 if (visc && dvdx < 0.0f) {
                     const float rhoj = c.crho[sj];

@@ -288,6 +288,7 @@ void fill_const(SimConst<R> &c, const sph_engine *e, const Sim &S, const SimDev 
         c.thr_s = (R)(supp * supp * (1.0 + 1.0 / 1024.0));
     for (int a = 0; a < 3; ++a) {
         c.edge[a] = (R)S.edge[a];
+        c.edge_lo[a] = (R)(S.edge[a] - (double)c.edge[a]);
         c.L[a] = (R)p.box[a];
         c.hL[a] = (R)d.half_L[a];
         // rounded up so no reachable cell is culled; single-cell axes never are
@@ -296,8 +297,8 @@ void fill_const(SimConst<R> &c, const sph_engine *e, const Sim &S, const SimDev 
     }
     const double hh[2] = {p.h_short, p.h_long}, sg[2] = {d.sig_s, d.sig_l};
     for (int k = 0; k < 2; ++k)
-        kernel_consts<R>(p.kernel, hh[k], sg[k], c.h[k], c.inv_h[k], c.inv_h_lo[k], c.sig[k],
-                         c.g0[k]);
+        kernel_consts<R>(p.kernel, hh[k], sg[k], c.h[k], c.h_lo[k], c.inv_h[k], c.inv_h_lo[k],
+                         c.sig[k], c.g0[k], c.g0_h2[k], c.inv_h2[k], c.inv_h2_lo[k]);
     c.hs = (R)p.h_short;
     c.eps_h2 = (R)(p.visc_eps * p.h_short * p.h_short);
     c.alpha_c = (R)(p.visc_alpha * p.sound_speed);

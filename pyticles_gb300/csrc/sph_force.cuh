@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
     ud.init(0);
     auto body = [&](int j, const T4 &pj, const R *d, R rsq, auto near) {
         constexpr bool NEAR = decltype(near)::value;
-        R r = fsqrt<R>(rsq);
-        R gl = kernel_g<K, R>(kl, r);
+        const Dist<R> dd = make_dist<R>(rsq);
+        R gl = kernel_g<K, R, true>(kl, dd);
         const T4 fvj = FV[j];
         R dvdx = (fvj.x - vix) * d[0] + (fvj.y - viy) * d[1];
         if (D == 3) dvdx += (fvj.z - viz) * d[2];
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
         // vanish and gsum = pl2 gl bit for bit
         R gsum = pl2 * gl, gs = (R)0;
         if constexpr (NEAR) {
-            gs = kernel_g<K, R>(ks, r);
+            gs = kernel_g<K, R, true>(ks, dd);
             R ps = fsi + (D == 2 ? fvj.z : fvj.w);
             if (visc && dvdx < (R)0) {
                 // Monaghan viscosity on approaching pairs

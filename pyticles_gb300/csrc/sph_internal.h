@@ -29,8 +29,10 @@ template <typename R> struct SimConst {
     R thr_s;                     // short kernel's support^2 (grown by a margin, at
                                  // most thr_hi): beyond it W_s = grad W_s = 0
     R edge[3], L[3], hL[3];
+    R edge_lo[3];                // edge - (R)edge: cell offsets as a hi/lo pair
     R ext[3];                    // half cell extent + allowed drift (culling)
-    R h[2], inv_h[2], inv_h_lo[2], sig[2], g0[2];
+    R h[2], h_lo[2], inv_h[2], inv_h_lo[2], sig[2], g0[2], g0_h2[2];
+    R inv_h2[2], inv_h2_lo[2];
     R hs, eps_h2, alpha_c, beta, pl2, kappa;
 };
 
@@ -39,14 +41,16 @@ template <typename R> struct SimConst {
 // (spkernel.py:39-52), the M4 cubic spline's 10/(7 pi h^2) and 1/(pi h^3).
 double kernel_sigma(int kernel, int dim, double h);
 
-// Device constants of one smoothing length: h, 1/h as a hi/lo pair, sigma
+// Device constants of one smoothing length: h and 1/h as hi/lo pairs, sigma
 // and the gradient factor g0 (Lucy -12 sigma/h^2, Gaussian -2/h^2 with sigma
 // applied in the kernel, cubic sigma/h^2, Debrun -3 sigma).  The pair passes'
 // tables and sph_kernel_eval take them from here alike.
 template <typename R>
-inline void kernel_consts(int kernel, double h, double sig, R &h_r, R &inv_h, R &inv_h_lo,
-                          R &sig_r, R &g0) {
+inline void kernel_consts(int kernel, double h, double sig, R &h_r, R &h_lo, R &inv_h,
+                          R &inv_h_lo, R &sig_r, R &g0, R &g0_h2, R &inv_h2,
+                          R &inv_h2_lo) {
     h_r = (R)h;
+    h_lo = (R)(h - (double)h_r);
     inv_h = (R)(1.0 / h);
     inv_h_lo = (R)(1.0 / h - (double)inv_h);
     sig_r = (R)sig;
@@ -56,6 +60,9 @@ inline void kernel_consts(int kernel, double h, double sig, R &h_r, R &inv_h, R 
         case SPH_KERNEL_CUBIC: g0 = (R)(sig / (h * h)); break;
         default: g0 = (R)(-3.0 * sig); break;
     }
+    g0_h2 = (R)((double)g0 / (h * h));
+    inv_h2 = (R)(1.0 / (h * h));
+    inv_h2_lo = (R)(1.0 / (h * h) - (double)inv_h2);
 }
 
 // Per-simulation constants on the device.

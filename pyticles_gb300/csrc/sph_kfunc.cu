@@ -17,7 +17,7 @@ __global__ void k_kernel_eval(int64_t n, const double *r, double *w, double *g, 
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     R wv, gv;
-    kernel_wg<K, R>(k, (R)r[i], &wv, &gv);
+    kernel_wg<K, R>(k, dist_of<R>((R)r[i]), &wv, &gv);
     w[i] = sig * (double)wv;
     g[i] = (double)gv;
 }
@@ -27,7 +27,8 @@ void launch_kernel_eval(int kernel, int dim, double h, int64_t n, const double *
                         double *g, cudaStream_t st) {
     const double sig = kernel_sigma(kernel, dim, h);
     KConst<R> k;
-    kernel_consts<R>(kernel, h, sig, k.h, k.inv_h, k.inv_h_lo, k.sig, k.g0);
+    kernel_consts<R>(kernel, h, sig, k.h, k.h_lo, k.inv_h, k.inv_h_lo, k.sig, k.g0,
+                     k.g0_h2, k.inv_h2, k.inv_h2_lo);
     const int block = 256;
     const unsigned grid = (unsigned)((n + block - 1) / block);
     switch (kernel) {

@@ -29,13 +29,13 @@ __global__ void __launch_bounds__(256, ONE ? 5 : 4) k_density(const __grid_const
     rl.init((R)0);
     unsigned cnt = 0;
     auto body = [&](int j, const T4 &pj, const R *d, R rsq, auto near) {
-        R r = rsqrt_<R>(rsq);
+        const Dist<R> dd = plain_dist<R>(rsq);
         R w, g;
         if constexpr (decltype(near)::value) {
-            kernel_wg<K, R>(ks, r, &w, &g);
+            kernel_wg<K, R>(ks, dd, &w, &g);
             rs.add(pj.w * w);
         }
-        kernel_wg<K, R>(kl, r, &w, &g);
+        kernel_wg<K, R>(kl, dd, &w, &g);
         rl.add(pj.w * w);
         ++cnt;
     };
@@ -104,8 +104,7 @@ __global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v)
     q[1].init(0);
     q[2].init(0);
     auto body = [&](int j, const T4 &pj, const R *d, R rsq, auto) {
-        R r = fsqrt<R>(rsq);
-        R g = kernel_g<K, R>(ks, r);
+        R g = kernel_g<K, R, true>(ks, make_dist<R>(rsq));
         T4 fj = F[j];
         R dT = (fj.z - fi.z) + (fj.w - fi.w);
         R f = pj.w * rrcp<R>(fj.y) * dT * g;

@@ -34,6 +34,7 @@ template <typename R, int D>
 struct PairFrame {
     R thr_lo, thr_hi, thr_s;
     R edge[3], L[3], hL[3];
+    R edge_lo[3];   // FP32: the part of the cell edge that (float)edge misses
     R ext[3];       // half extent of a cell including the allowed drift
     int small_mask;
     __device__ __forceinline__ void init(const SimDev &S) {
@@ -44,6 +45,7 @@ struct PairFrame {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             edge[a] = c.edge[a];
+            edge_lo[a] = c.edge_lo[a];
             L[a] = c.L[a];
             hL[a] = c.hL[a];
             ext[a] = c.ext[a];
@@ -131,9 +133,17 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
                 const int gc = S.cell_off + mort[row + x];
                 if (!SPH_IN_BOUNDS(gc >= S.cell_off && gc < S.cell_off + S.ncells, v.err_any))
                     continue;
-                const R ox_ = (R)ox * fr.edge[0] - pi.x;
-                const R oy_ = (R)oy * fr.edge[1] - pi.y;
-                const R oz_ = (D == 3) ? (R)oz * fr.edge[2] - pi.z : (R)0;
+                // offset of the window cell's frame from particle i; in FP32
+                // the cell edge is a hi/lo pair, so that the offset carries one
+                // rounding instead of the edge's rounding times the cell count
+                R ox_ = (R)ox * fr.edge[0] - pi.x;
+                R oy_ = (R)oy * fr.edge[1] - pi.y;
+                R oz_ = (D == 3) ? (R)oz * fr.edge[2] - pi.z : (R)0;
+                if constexpr (std::is_same<R, float>::value) {
+                    ox_ = __fmaf_rn((R)ox, fr.edge_lo[0], ox_);
+                    oy_ = __fmaf_rn((R)oy, fr.edge_lo[1], oy_);
+                    if (D == 3) oz_ = __fmaf_rn((R)oz, fr.edge_lo[2], oz_);
+                }
                 const int jb = v.cell_start[gc], je = v.cell_start[gc + 1];
                 if (!SPH_IN_BOUNDS(jb >= 0 && jb <= je && je <= v.np, v.err_any)) continue;
                 auto scan = [&](auto near, auto self) {

@@ -10,7 +10,7 @@ import pytest
 from oracle import oracle
 from pyticles_gb300 import Engine, SphError, build, make_params, workloads
 from pyticles_gb300._abi import SPH_ESKIN
-from tests.golden_cases import rel_l2
+from tests.golden_cases import position_floor, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -518,10 +518,14 @@ def test_random_3d_systems_match_oracle(seed):
     """Random systems (sparse and dense columns, clusters spread over many
     slabs, z windows wrapping the box, some boxes too small for columns):
     pair counts exact, and the mixed-precision errors against the oracle no
-    larger than the cell scheme's on the same system (uniformly random
-    placements put particles nearly on top of each other, where FP32
-    coordinate differences lose digits in either scheme)."""
+    larger than the cell scheme's on the same system.  Uniformly random
+    placements put particles nearly on top of each other and push local
+    densities past the van der Waals pole (b rho = 1), so on some systems
+    FP32 rounding of the positions alone moves the FP64 forces by 1e-5 to
+    3e-4 (the position floor): there both schemes' errors are that floor
+    times a random factor, and the bound is a small multiple of it."""
     prm, r, v, m, u = random_system(4000 + seed)
+    floor = position_floor(prm, r, v, m, u)
     ref = oracle.derivatives(prm, r, v, m, u)
     ro, vo, uo, _ = oracle.advance(prm, r, v, m, u, 3)
     errs = {}
@@ -536,6 +540,6 @@ def test_random_3d_systems_match_oracle(seed):
             rr, vv, uu = e.get_state(s)
         errs[scheme] = {k: rel_l2(d[k], ref[k]) for k in ("rho", "vdot", "udot")}
         errs[scheme].update(r3=rel_l2(rr, ro), u3=rel_l2(uu, uo))
-    print(seed, errs)
+    print(seed, errs, {k: floor[k] for k in ("rho", "vdot", "udot")})
     for k, err in errs[1].items():
-        assert err < 2 * max(errs[0][k], MIXED_TOL), (k, errs)
+        assert err < 2 * max(errs[0][k], 3 * floor.get(k, 0.0), MIXED_TOL), (k, errs, floor)

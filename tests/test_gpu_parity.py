@@ -13,20 +13,45 @@ import pytest
 from oracle import oracle
 from pyticles_gb300 import Engine, build, workloads
 from pyticles_gb300._abi import SPH_ENAN, SPH_ESKIN, SphError
-from tests.golden_cases import SYSTEMS, load, params_of, rel_l2, sort_pairs
+from tests.golden_cases import SYSTEMS, load, load_floors, params_of, rel_l2, sort_pairs
 
 pytestmark = pytest.mark.gpu
 
 EVAL_TOL = 1e-12
 STEP_TOL = 1e-10
 MIXED_TOL = 1e-6
-# Pure pressure forces (no viscosity) on near-lattice systems cancel to a
-# net force far below the individual pair terms, and T = (u + a rho)/k_B
-# cancels too; a density error at the FP32 floor (~5e-8) then reaches the
-# net force amplified ~30x.  These systems are held to 5e-6 on vdot/udot;
-# every quantity of the viscous workloads (the benchmarked ones) to 1e-6.
-PRESSURE_ONLY_TOL = 5e-6
+# Pure pressure forces (no viscosity) on the near-lattice golden systems
+# cancel to a net force far below the individual pair terms, so the net
+# force carries the FP32 rounding of every term.  Carrying the pair
+# geometry alone in FP32 (separation and distance rounded once, all else
+# FP64: floor B, tests/golden/floors.json) already moves vdot by 0.4-1.1e-6
+# on these systems, so no FP32 pair pass meets 1e-6 on all of them.  Their
+# mixed vdot is held to FLOOR_FACTOR times each system's own floor B
+# (measured on GB300: 1.6-2.5 times); every other quantity, and every
+# quantity of the viscous workloads, to 1e-6.
+FLOOR_FACTOR = 3.0
+JQ_TOL = 5e-6
+FLOORS = load_floors()
 KEYS = ("rho", "rho_lr", "t", "p", "pco", "vdot", "udot")
+
+
+def record(test, case, precision, errs, bounds=None):
+    """Appends one line of measured errors to $PYTICLES_PARITY_LOG (JSON
+    lines), so that a run's per-system errors are kept, not only printed."""
+    import json
+    import os
+    path = os.environ.get("PYTICLES_PARITY_LOG")
+    print(case, precision, errs)
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps({"test": test, "case": case, "precision": precision,
+                                "errors": errs, "bounds": bounds}) + "\n")
+
+
+def mixed_bound(name, k):
+    if k == "vdot":
+        return FLOOR_FACTOR * FLOORS[name]["geometry"][k]
+    return MIXED_TOL
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -49,13 +74,10 @@ def test_evaluation_matches_reference(name, precision):
         d = e.derivatives(s)
         e.sync()
         errs = {k: rel_l2(d[k], g["ev_" + k]) for k in KEYS}
-        print(name, precision, errs)
+        bounds = {k: EVAL_TOL if precision == "fp64" else mixed_bound(name, k) for k in KEYS}
+        record("evaluation", name, precision, errs, bounds)
         for k, err in errs.items():
-            if precision == "fp64":
-                tol = EVAL_TOL
-            else:
-                tol = PRESSURE_ONLY_TOL if k in ("vdot", "udot") else MIXED_TOL
-            assert err < tol, (k, err)
+            assert err < bounds[k], (k, err, bounds[k])
         assert e.pair_count(s) == len(g["iap"])
 
 
@@ -121,9 +143,15 @@ def test_mixed_steps_track_reference(name):
         e.advance(int(g["steps"]))
         e.sync()
         r, v, u = e.get_state(s)
-        assert rel_l2(r, g["r_final"]) < MIXED_TOL
-        assert rel_l2(v, g["v_final"]) < PRESSURE_ONLY_TOL
-        assert rel_l2(u, g["u_final"]) < MIXED_TOL
+        errs = {"r": rel_l2(r, g["r_final"]), "v": rel_l2(v, g["v_final"]),
+                "u": rel_l2(u, g["u_final"])}
+        # the velocity change over the steps is dt x vdot, so it carries
+        # vdot's bound; r and u are held to 1e-6
+        bounds = {"r": MIXED_TOL, "u": MIXED_TOL,
+                  "v": max(MIXED_TOL, mixed_bound(name, "vdot"))}
+        record("steps", name, "mixed", errs, bounds)
+        for k, err in errs.items():
+            assert err < bounds[k], (k, err, bounds[k])
 
 
 def with_gradient(prm, r, v, m, T0):
@@ -155,15 +183,14 @@ def test_full_physics_vs_oracle(case, precision):
         e.sync()
         keys = KEYS + (("jq",) if prm.heat_flux else ())
         errs = {k: rel_l2(d[k], ref[k]) for k in keys}
-        print(case, precision, errs)
+        # jq sums temperature differences T_j - T_i, each carrying the
+        # density error times a/k_B, over a near-uniform temperature field:
+        # held to JQ_TOL
+        bounds = {k: EVAL_TOL if precision == "fp64" else (JQ_TOL if k == "jq" else MIXED_TOL)
+                  for k in keys}
+        record("full_physics", case, precision, errs, bounds)
         for k, err in errs.items():
-            if precision == "fp64":
-                tol = EVAL_TOL
-            else:
-                # jq sums temperature differences T_j - T_i, each carrying the
-                # density error times a/k_B: held to the pressure-only bound
-                tol = PRESSURE_ONLY_TOL if k == "jq" else MIXED_TOL
-            assert err < tol, (k, err)
+            assert err < bounds[k], (k, err, bounds[k])
         assert e.pair_count(s) == ref["nip"]
         e.advance(5)
         e.sync()
