@@ -354,6 +354,30 @@ def reference_arm(args):
     return 0
 
 
+def profile_case(args):
+    """A few eager (non-graph) steps of one workload for profilers: each step
+    launches the binning kernels, then per integrator stage k_density,
+    [k_heat,] k_force; with --steps 2 the second step's launches are the ones
+    to capture.  2D: the fluid of the bench line at --side^2; 3D: the fluid at
+    density 0.7 at --side^3 (cubic spline, viscosity, heat flux)."""
+    from pyticles_gb300 import Engine, build, workloads
+    build.build()
+    if args.profile_case == "2d":
+        prm, r, v, m, T0 = workloads.config_2d(args.side, 1000, viscosity=True)
+        u = workloads.vdw_energy(np.ones(len(r)), T0)
+    else:
+        prm, r, v, m, T0 = workloads.config_3d(args.side, 3000)
+        u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
+    with Engine(prm, args.precision, max_particles=len(r)) as e:
+        e.add(prm, r, v, m, u)
+        e.set_tuning(use_graph=0, pair_scheme=args.pair_scheme)
+        e.advance(args.steps)
+        e.sync()
+        print(f"{args.profile_case} n={len(r)} steps={args.steps} "
+              f"pairs/eval={e.last_pair_total()} tuning={e.tuning}")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -380,7 +404,14 @@ def main():
     ap.add_argument("--rebin", type=int, default=1, choices=[0, 1],
                     help="single-simulation workloads: 1 bins into cells on demand "
                          "(tuning.rebin), 0 every step")
+    ap.add_argument("--profile-case", choices=["2d", "3d"], default=None,
+                    help="profiling driver: --steps eager steps of one workload "
+                         "(--side, --precision, --pair-scheme), no timing")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--pair-scheme", type=int, default=0, choices=[0, 1])
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -432,12 +463,19 @@ def main():
     bpp = opcount.force_bytes_per_step_average(2, 4, reuse=bool(args.rebin))
     achieved = bpp * n / (avg_ms * 1e-3) / 1e9
     trafpp = committed_traffic("k_force_2d_mixed.md")
-    # issue roofline: the launch's warp instructions (ncu, per particle) over
-    # the live launch time against 152 SMs x 4 schedulers x 1 per cycle
+    # the binding limit, instruction issue: from one ncu launch, its warp
+    # instructions over its own duration and clock against SMs x 4 issue
+    # slots per cycle (both from the same launch); the live figure scales
+    # that launch's instruction count to the bench's in-graph launch time
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
     winst_pp = committed_figure("k_force_2d_mixed.md", "warp_instructions_per_particle")
-    issue_peak = 152 * 4 * sm_max * 1e6
+    ncu_ms = committed_figure("k_force_2d_mixed.md", "launch_ms")
+    ncu_mhz = committed_figure("k_force_2d_mixed.md", "sm_mhz")
+    ncu_issue = None
+    if winst_pp is not None and ncu_ms and ncu_mhz:
+        ncu_issue = winst_pp * n / (sms * 4 * ncu_mhz * 1e6 * ncu_ms * 1e-3)
     flops = opcount.FLOPS_FORCE[2] * pairs / (avg_ms * 1e-3) / 1e12
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
     total_pass_ms = sum(p["ms"] for p in passes.values())
 
     extras = {}
@@ -497,22 +535,29 @@ def main():
             "pass_ms_per_step": {k: p["ms"] / args.steps for k, p in passes.items()},
         },
         "roofline": {
-            "bound": "hbm", "kernel": "k_force<float,2,lucy> (force + energy rate + integrator)",
+            # the HBM roofline of the dominant pass, as the metric asks; the
+            # pass is bound by instruction issue (FP32 pair arithmetic), whose
+            # fraction is `binding`
+            "bound": "issue",
+            "kernel": "k_force<float,2,lucy> (force + energy rate + integrator)",
             "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "peak_kind": peak_kind,
             "bytes_per_particle": bpp,
             "traffic": None if trafpp is None else trafpp * n,
+            "binding": None if winst_pp is None else {
+                "limit": "instruction issue (FP32 pair arithmetic)",
+                "frac": ncu_issue,
+                "frac_live": winst_pp * n / (avg_ms * 1e-3) / (sms * 4 * sm_max * 1e6),
+                "warp_instructions_per_particle": winst_pp,
+                "sms": sms,
+                "note": "frac: warp instructions of one ncu launch over that launch's own "
+                        "duration x SMs x 4 issue slots x its SM clock; frac_live: the same "
+                        "instruction count over the live in-graph launch time at the maximum "
+                        "clock"},
             "fp32_pipe": {"achieved_tflops": flops, "peak_tflops": fp32_peak,
                           "frac": flops / fp32_peak,
-                          "note": "algorithmic flops of the force pass; peak = 152 SMs x 128 "
-                                  "FP32 lanes x 2 x max SM clock (nominal)"},
-            "issue": None if winst_pp is None else {
-                "achieved_warp_inst_per_s": winst_pp * n / (avg_ms * 1e-3),
-                "peak_warp_inst_per_s": issue_peak,
-                "frac": winst_pp * n / (avg_ms * 1e-3) / issue_peak,
-                "note": "the binding limit: warp instructions of one force launch from the "
-                        "committed ncu summary over the live launch time; peak = 152 SMs x 4 "
-                        "issue slots x max SM clock"},
+                          "note": "algorithmic flops of the force pass over SMs x 128 FP32 "
+                                  "lanes x 2 x max SM clock (SM count from the device)"},
             "force_share_of_step": f["ms"] / total_pass_ms if total_pass_ms > 0 else None,
         },
         "cpu_baseline": cpu,
