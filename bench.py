@@ -196,6 +196,72 @@ def batched_workload(nsims, ramp_steps=500):
     return sims
 
 
+def batched_arm(sims, steps, torch, stream, dist=None):
+    """The batched workload timed with one thread per particle and as
+    persistent launches (tuning.persistent) over the flattened table, after
+    autotuning the other knobs on a sample; the faster is the arm's value.
+    Under torchrun each rank runs its round-robin share of the simulations
+    (replicas.shard); the work adds up over the slowest rank's time."""
+    from pyticles_gb300 import replicas
+    from pyticles_gb300 import autotune
+    knobs, _ = autotune.tune(sims[0][0], "mixed", autotune.sample_sims(sims, 1 << 20), steps=3,
+                             warmup=2)
+    variants = {}
+    for persistent in (0, 1):
+        k = dict(knobs, rebin=0, persistent=persistent)
+        ms, pairs, passes, kps = run_timed(None, None, None, None, None, "mixed", steps, 3,
+                                           torch, stream, knobs=k, sims=sims)
+        ms, pairs = replicas.combine(ms, pairs, dist, device="cuda")
+        variants["persistent" if persistent else "grid"] = {
+            "ms_per_step": ms / steps, "value": pairs * 2 * steps / (ms * 1e-3),
+            "pass_ms_per_step": {kk: p["ms"] / steps for kk, p in passes.items()},
+            "pairs_per_eval": pairs}
+    best = min(variants, key=lambda name: variants[name]["ms_per_step"])
+    b = variants[best]
+    nall = replicas.combine(0.0, sum(len(x[1]) for x in sims), dist, device="cuda")[1]
+    sall = replicas.combine(0.0, len(sims), dist, device="cuda")[1]
+    return {"sims": int(sall), "n": int(nall), "steps": steps,
+            "ms_per_step": b["ms_per_step"], "pairs_per_eval": b["pairs_per_eval"],
+            "value": b["value"], "unit": UNIT, "tuning": dict(knobs, persistent=int(best == "persistent")),
+            "launch": best, "variants": variants,
+            "pass_ms_per_step": b["pass_ms_per_step"]}
+
+
+def batched_accuracy(sims, steps, stream, knobs):
+    """Mixed precision against the FP64 oracle for the smallest, median and
+    largest simulation of the batch, each advanced `steps` steps from the
+    same initial state (the quench included): relative L2 of r, v, u after
+    the steps, and of rho, vdot, udot of one evaluation at the GPU's final
+    state.  A simulation gives the same bits alone as in the batch, so the
+    three run in their own engine."""
+    from oracle import oracle
+    from pyticles_gb300 import Engine
+    order = sorted(range(len(sims)), key=lambda k: len(sims[k][1]))
+    picks = {"smallest": order[0], "median": order[len(order) // 2], "largest": order[-1]}
+    group = [sims[k] for k in picks.values()]
+    total = sum(len(x[1]) for x in group)
+    out = {}
+    with Engine(group[0][0], "mixed", max_particles=total, max_sims=len(group),
+                stream=stream.cuda_stream) as e:
+        ids = [e.add(*st) for st in group]
+        e.set_tuning(**dict(knobs, rebin=0, steps_per_graph=min(steps, 100)))
+        e.advance(steps)
+        e.sync()
+        states = [e.get_state(i) for i in ids]
+        evals = [e.derivatives(i) for i in ids]
+        e.sync()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    for (name, k), (prm, r, v, m, u), (rr, vv, uu), g in zip(picks.items(), group, states, evals):
+        t0 = time.perf_counter()
+        r1, v1, u1, _ = oracle.advance(prm, r, v, m, u, steps)
+        ref = oracle.derivatives(prm, rr, vv, m, uu)
+        out[name] = {"sim": k, "n": len(r), "oracle_s": time.perf_counter() - t0,
+                     "r": rel(rr, r1), "v": rel(vv, v1), "u": rel(uu, u1),
+                     "rho": rel(g["rho"], ref["rho"]), "vdot": rel(g["vdot"], ref["vdot"]),
+                     "udot": rel(g["udot"], ref["udot"])}
+    return out
+
+
 def fluid3d_workload(side):
     """3D fluid at number density 0.7 (side^3 particles), cubic spline with
     support radii 2.735 / 5.148 (about 60 / 400 neighbours), viscosity, heat
@@ -223,21 +289,30 @@ def timed_workload(sims, steps, warmup, torch, stream, tune=True, rebin=0):
             "pass_ms_per_step": {k: p["ms"] / steps for k, p in passes.items()}}
 
 
-def serve_window(njobs, time_limit, seed=5000):
+def serve_window(njobs, time_limit, budget_gb, seed=5000, dist=None):
     """A fixed Poisson arrival window of the served workload (20 jobs/s, 70%
     2D, N log-uniform in [1e3, 1e6], steps uniform in [100, 5000]), served in
-    real time within an HBM budget; jobs still running at the time limit are
-    reported as unfinished."""
-    from pyticles_gb300 import serve
+    real time within an HBM budget small enough that admission queues.  The
+    offered load (about 1.5e12 pair-interactions/s) exceeds one GPU, so the
+    run stops at the time limit: jobs still running or still waiting then
+    are reported as unfinished, and the work they did counts toward the
+    achieved load.  Offered load counts each job's pairs from the fluid's
+    density (56.5 unordered pairs per particle in 2D, about 200 in 3D) x 2
+    evaluations x its steps, over the arrival window."""
+    from pyticles_gb300 import replicas, serve
     jobs = serve.poisson_jobs(njobs, seed=seed)
+    if dist is not None and dist.is_initialized():
+        # each rank serves its round-robin share of the one arrival stream
+        jobs = replicas.shard(jobs, dist.get_rank(), dist.get_world_size())
     offered = sum(j.n * (56.5 if j.dim == 2 else 200.0) * 2 * j.steps for j in jobs)
-    srv = serve.Server(60e9, chunk=25, max_sims=256)
+    srv = serve.Server(budget_gb * 1e9, chunk=25, max_sims=256)
     rep = srv.run(jobs, realtime=True, time_limit=time_limit)
     rep["job_records"] = srv.job_records(jobs)
     srv.close()
     rep["offered_pair_interactions_per_s"] = offered / max(rep["arrival_window_s"], 1e-9)
+    rep["offered_pair_interactions"] = offered
     rep["time_limit_s"] = time_limit
-    return rep
+    return replicas.merge_served(replicas.gather(rep, dist))
 
 
 def run_e2e(prm, r, v, m, u, steps, torch, stream):
@@ -394,10 +469,13 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched, 3D and served sub-workloads")
     ap.add_argument("--batched-sims", type=int, default=512)
-    ap.add_argument("--batched-steps", type=int, default=100)
+    ap.add_argument("--batched-steps", type=int, default=500,
+                    help="steps of the batched workload (its quench ramps over 500)")
     ap.add_argument("--side3d", type=int, default=128)
     ap.add_argument("--steps3d", type=int, default=200)
-    ap.add_argument("--serve-jobs", type=int, default=12)
+    ap.add_argument("--serve-jobs", type=int, default=200)
+    ap.add_argument("--serve-budget-gb", type=float, default=3.0,
+                    help="HBM budget of the served workload's engines")
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--accuracy-steps", type=int, default=1000,
                     help="trajectory length of the mixed-vs-FP64 accuracy report (0: skip)")
@@ -479,13 +557,24 @@ def main():
     total_pass_ms = sum(p["ms"] for p in passes.values())
 
     extras = {}
-    if rank == 0 and not args.no_extras:
-        extras["batched"] = timed_workload(batched_workload(args.batched_sims),
-                                           args.batched_steps, 3, torch, stream)
+    if not args.no_extras:
+        # every rank: the batched and served arms split their simulations and
+        # jobs over the ranks; the 3D fluid runs as a replica per rank
+        bsims = batched_workload(args.batched_sims)
+        extras["batched"] = batched_arm(replicas.shard(bsims, rank, world), args.batched_steps,
+                                        torch, stream, dist)
+        if rank == 0 and not args.no_cpu:
+            extras["batched"]["accuracy"] = batched_accuracy(
+                bsims, args.batched_steps, stream, extras["batched"]["tuning"])
         w3 = fluid3d_workload(args.side3d)
         extras["fluid3d"] = timed_workload(w3, args.steps3d, 3, torch, stream,
                                            rebin=args.rebin)
-        if not args.no_cpu:
+        f3 = extras["fluid3d"]
+        ms3, work3 = replicas.combine(f3["ms_per_step"] * f3["steps"],
+                                      f3["pairs_per_eval"] * 2 * f3["steps"], dist, device="cuda")
+        f3["value"] = work3 / (ms3 * 1e-3)
+        f3["replicas"] = world
+        if rank == 0 and not args.no_cpu:
             acc3 = accuracy_track(*w3[0], args.steps3d, args.steps3d, stream,
                                   knobs=extras["fluid3d"]["tuning"])
             extras["fluid3d"]["cpu_baseline"] = dict(
@@ -496,7 +585,8 @@ def main():
                 "what": "relative L2 of the mixed-precision evaluation against the FP64 "
                         "oracle at the GPU state after the timed steps",
                 **acc3[-1]}
-        extras["serve"] = serve_window(args.serve_jobs, args.serve_seconds)
+        extras["serve"] = serve_window(args.serve_jobs, args.serve_seconds, args.serve_budget_gb,
+                                       dist=dist)
 
     accuracy = None
     if rank == 0 and not args.no_cpu and args.accuracy_steps > 0:

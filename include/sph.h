@@ -185,9 +185,15 @@ int sph_sim_pair_count(sph_engine *e, int32_t sim_id, int64_t *nip);
 int sph_sim_export_pairs(sph_engine *e, int32_t sim_id, int64_t cap, int64_t *iap,
                          double *drij, double *rsq, double *dv, int64_t *nip, int32_t mem);
 
-/* Sum over all simulations of the pair-set size seen by the last
- * evaluation pass (the metric's unit of work). */
+/* Sum over all simulations of the pair-set size (unordered pairs) of one
+ * evaluation: the first evaluation of the last step, or of the last
+ * derivative call (the metric's unit of work per evaluation). */
 int sph_last_pair_total(sph_engine *e, int64_t *pairs);
+
+/* The same per simulation: counts[sim_id] for sim_id < cap (0 for empty
+ * slots).  No counterpart in the reference; the job server attributes
+ * each job's work from it. */
+int sph_last_pair_counts(sph_engine *e, int64_t *counts, int32_t cap);
 
 /* Per-simulation diagnostics of the current state, FP64 reductions:
  * out[0] kinetic energy, out[1] internal energy, out[2..4] momentum,
@@ -227,7 +233,14 @@ typedef struct sph_tuning {
                                  simulation gives the same bits alone or in a
                                  batch; same pair set, rounding differs from
                                  scheme 0                                     */
-    int32_t reserved;         /* 0 */
+    int32_t persistent;       /* 0: the cell-window density, heat-flux and
+                                 force passes launch one thread per particle.
+                                 1: each launches only the blocks the device
+                                 holds at once (SMs x resident blocks), which
+                                 walk the flattened particle table grid-
+                                 stride: one persistent launch per pass over
+                                 all simulations.  Each particle's sums are
+                                 the same either way (same bits)           */
 } sph_tuning;
 int sph_get_tuning(sph_engine *e, sph_tuning *t);
 int sph_set_tuning(sph_engine *e, const sph_tuning *t);

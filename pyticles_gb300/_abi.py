@@ -90,7 +90,7 @@ class SphTuning(ctypes.Structure):
         ("rebin", ctypes.c_int32),
         ("cell_ratio", ctypes.c_double),
         ("pair_scheme", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("persistent", ctypes.c_int32),
     ]
 
 
@@ -185,6 +185,7 @@ def _declare(lib):
         "sph_sim_pair_count": [vp, c_i32, P(c_i64)],
         "sph_sim_export_pairs": [vp, c_i32, c_i64, vp, vp, vp, vp, P(c_i64), c_i32],
         "sph_last_pair_total": [vp, P(c_i64)],
+        "sph_last_pair_counts": [vp, P(c_i64), c_i32],
         "sph_sim_diagnostics": [vp, c_i32, P(ctypes.c_double)],
         "sph_get_tuning": [vp, P(SphTuning)],
         "sph_set_tuning": [vp, P(SphTuning)],
@@ -217,7 +218,8 @@ def exported_symbols():
     return ["sph_engine_create", "sph_engine_destroy", "sph_sim_add", "sph_sim_remove",
             "sph_sim_set_state", "sph_sim_get_state", "sph_sim_get_properties",
             "sph_sim_count", "sph_sim_steps", "sph_sim_set_steps", "sph_advance", "sph_sim_derivatives", "sph_sim_pair_count",
-            "sph_sim_export_pairs", "sph_last_pair_total", "sph_sim_diagnostics",
+            "sph_sim_export_pairs", "sph_last_pair_total", "sph_last_pair_counts",
+            "sph_sim_diagnostics",
             "sph_get_tuning", "sph_set_tuning", "sph_rebin_count", "sph_prepare", "sph_profile",
             "sph_profile_read", "sph_kernels_per_step", "sph_sync", "sph_sim_status",
             "sph_splash_map", "sph_kernel_eval", "sph_collide_pairs", "sph_derivatives_noalloc",

@@ -539,8 +539,11 @@ __global__ void __launch_bounds__(kBlock) k_cl_density(const __grid_constant__ V
             rl.flush();
         });
     const double sum_s = quad_sum(rs.get64()), sum_l = quad_sum(rl.get64());
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if (lane == 0) atomicAdd(&v.pair_count[sim], (unsigned long long)cnt);
+    // the pair set of one evaluation: counted at the step's first one only
+    if (stage == 0) {
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+        if (lane == 0) atomicAdd(&v.pair_count[sim], (unsigned long long)cnt);
+    }
     if (jj != 0 || gi < 0) return;
     // EOS in FP64, as in the cell-window density pass (k_density)
     const double rho = S.ws0 + S.sig_s * sum_s;

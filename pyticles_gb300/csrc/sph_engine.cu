@@ -568,6 +568,7 @@ View make_view(const sph_engine *e) {
     View v;
     memset(&v, 0, sizeof(v));
     v.np = e->np_b;
+    v.persist = e->tune.persistent;
     v.dim = e->dim;
     v.sims = e->sims_d;
     for (int a = 0; a < 3; ++a) {
@@ -1302,7 +1303,7 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->tune.use_graph = 1;
     e->tune.steps_per_graph = 1;
     e->tune.pair_scheme = 0;
-    e->tune.reserved = 0;
+    e->tune.persistent = 0;
     if (stream) {
         e->stream = (cudaStream_t)stream;
     } else {
@@ -1719,6 +1720,19 @@ int sph_last_pair_total(sph_engine *e, int64_t *pairs) {
     return SPH_OK;
 }
 
+int sph_last_pair_counts(sph_engine *e, int64_t *counts, int32_t cap) {
+    if (!e || !counts || cap < 0) return SPH_EINVAL;
+    std::vector<unsigned long long> c(e->cap_s);
+    CK(cudaMemcpyAsync(c.data(), e->pair_count, sizeof(unsigned long long) * e->cap_s,
+                       cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    for (int s = 0; s < cap; ++s) {
+        const bool live = s < (int)e->sims.size() && e->sims[s].active;
+        counts[s] = live ? (int64_t)(c[s] / 2) : 0;
+    }
+    return SPH_OK;
+}
+
 int sph_sim_diagnostics(sph_engine *e, int32_t id, double out[6]) {
     TRY(check_sim(e, id));
     if (!out) return SPH_EINVAL;
@@ -1761,7 +1775,8 @@ int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
     if (!e || !t) return SPH_EINVAL;
     if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) ||
         !(t->cell_ratio >= 0.2 && t->cell_ratio <= 4.0) || (t->rebin != 0 && t->rebin != 1) ||
-        t->steps_per_graph < 1 || (t->pair_scheme != 0 && t->pair_scheme != 1))
+        t->steps_per_graph < 1 || (t->pair_scheme != 0 && t->pair_scheme != 1) ||
+        (t->persistent != 0 && t->persistent != 1))
         return SPH_EINVAL;
     bool regrid = t->cell_ratio != e->tune.cell_ratio;
     if (t->pair_scheme != e->tune.pair_scheme) {
@@ -1769,7 +1784,6 @@ int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
         e->cl_disabled = false;
     }
     e->tune = *t;
-    e->tune.reserved = 0;
     free_graph(e);
     if (regrid) {
         for (auto &S : e->sims)

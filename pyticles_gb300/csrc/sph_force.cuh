@@ -186,11 +186,9 @@ __device__ __forceinline__ void integrate_stage(const View &v, const SimDev &S, 
 // single 2D simulation, with its constants out of registers, runs best at 51
 // (5 blocks), 3D at 64.
 template <typename R, int D, int K, int VH, bool ONE>
-__global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __grid_constant__ View v, int stage,
-                                                  int mode, int integ) {
+__device__ __forceinline__ void force_one(const View &v, int stage, int mode, int integ, int i) {
     constexpr bool visc = (VH & 1) != 0;
     constexpr bool heat = (VH & 2) != 0;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
     using T4 = typename V4<R>::T;
@@ -273,6 +271,19 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
     integrate_stage<R, D>(v, S, i, s, stage, integ, vdr, udr);
 }
 
+// One thread per particle; PERSIST: the resident blocks of pass_grid walk
+// the particles grid-stride (the same per-particle work, the same bits).
+template <typename R, int D, int K, int VH, bool ONE, bool PERSIST>
+__global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __grid_constant__ View v, int stage,
+                                                  int mode, int integ) {
+    if constexpr (PERSIST) {
+        for (int base = blockIdx.x * blockDim.x; base < v.np; base += gridDim.x * blockDim.x)
+            force_one<R, D, K, VH, ONE>(v, stage, mode, integ, base + threadIdx.x);
+    } else {
+        force_one<R, D, K, VH, ONE>(v, stage, mode, integ, blockIdx.x * blockDim.x + threadIdx.x);
+    }
+}
+
 // Integrator stage from the stored rates: the epilogue of k_force as a pass
 // of its own, for steps whose velocities change between the force pass and
 // the update (hard collisions).
@@ -288,15 +299,26 @@ __global__ void __launch_bounds__(256) k_integrate(View v, int stage, int integ,
     integrate_stage<R, D>(v, S, i, s, stage, integ, vdr, ((const R *)v.udot)[i]);
 }
 
+// the persistent form for the mixed-precision pass only (see density_launch)
+template <typename R, int D, int K, int VH, bool ONE>
+void force_launch(const View &v, int stage, int mode, int integ, int block, cudaStream_t s) {
+    if (std::is_same<R, float>::value && v.persist) {
+        auto *fn = k_force<R, D, K, VH, ONE, std::is_same<R, float>::value>;
+        fn<<<pass_grid(v, fn, block), block, 0, s>>>(v, stage, mode, integ);
+    } else {
+        k_force<R, D, K, VH, ONE, false>
+            <<<(v.np + block - 1) / block, block, 0, s>>>(v, stage, mode, integ);
+    }
+}
+
 template <typename R>
 void launch_force_t(const View &v, int kernel, int viscosity, int heat, int integrator, int stage,
                     int mode, int block, cudaStream_t s) {
     if (v.np <= 0) return;
-    int nb = (v.np + block - 1) / block;
     const int vh = (viscosity ? 1 : 0) | (heat ? 2 : 0);
-#define SPH_FORCE(VH_)                                                                  \
-    (v.one_sim ? k_force<R, D, K, VH_, true><<<nb, block, 0, s>>>(v, stage, mode, integrator) \
-               : k_force<R, D, K, VH_, false><<<nb, block, 0, s>>>(v, stage, mode, integrator))
+#define SPH_FORCE(VH_)                                                                   \
+    (v.one_sim ? force_launch<R, D, K, VH_, true>(v, stage, mode, integrator, block, s)  \
+               : force_launch<R, D, K, VH_, false>(v, stage, mode, integrator, block, s))
 #define SPH_FORCE_VH                                                                     \
     switch (vh) {                                                                        \
         case 0: SPH_FORCE(0); break;                                                     \

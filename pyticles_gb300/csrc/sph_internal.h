@@ -155,6 +155,9 @@ struct View {
     // sims[that id]); the pair kernels then read its constants from the
     // kernel parameters instead of holding them in registers
     int one_sim;
+    // persist: the pair passes launch pass_grid()'s resident blocks, which
+    // walk the particles grid-stride (tuning.persistent)
+    int persist;
     SimDev one;
 };
 

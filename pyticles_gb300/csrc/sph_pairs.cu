@@ -5,6 +5,10 @@
 //               properties.py:77-91), fused EOS epilogue (T from u, clamp,
 //               p, pco: properties.py:38-49, spam_complete_force.py:134-152)
 //   k_heat    : Fourier heat flux q_i (f_properties.py:129-130 restated)
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "sph_pairs.cuh"
 
 namespace sph {
@@ -13,8 +17,7 @@ namespace sph {
 // for_pairs would otherwise take 80 and cost 5-20% in occupancy; 51 for a
 // single simulation (its constants are kernel parameters), 3% faster again.
 template <typename R, int D, int K, bool ONE>
-__global__ void __launch_bounds__(256, ONE ? 5 : 4) k_density(const __grid_constant__ View v, int stage) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void density_one(const View &v, int stage, int i) {
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
     using T4 = typename V4<R>::T;
@@ -82,13 +85,26 @@ __global__ void __launch_bounds__(256, ONE ? 5 : 4) k_density(const __grid_const
                                 : make_v4<R>(vi.x, vi.y, vi.z, (R)fs);
     if (!isfinite((R)p) || !isfinite((R)rho) || !isfinite((R)rhol))
         set_err(v.err, v.err_any, s, SPH_ENAN);
-    add_pair_count(v.pair_count, s, cnt);
+    // the pair set of one evaluation: counted at the step's first one only
+    // (the counters are cleared once per step)
+    if (stage == 0) add_pair_count(v.pair_count, s, cnt);
+}
+
+// One thread per particle; PERSIST: the resident blocks of pass_grid walk
+// the particles grid-stride (the same per-particle work, the same bits).
+template <typename R, int D, int K, bool ONE, bool PERSIST>
+__global__ void __launch_bounds__(256, ONE ? 5 : 4) k_density(const __grid_constant__ View v, int stage) {
+    if constexpr (PERSIST) {
+        for (int base = blockIdx.x * blockDim.x; base < v.np; base += gridDim.x * blockDim.x)
+            density_one<R, D, K, ONE>(v, stage, base + threadIdx.x);
+    } else {
+        density_one<R, D, K, ONE>(v, stage, blockIdx.x * blockDim.x + threadIdx.x);
+    }
 }
 
 // At most 64 registers (4 blocks of 256 per SM): 8% faster in 3D than 80.
 template <typename R, int D, int K, bool ONE>
-__global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void heat_one(const View &v, int i) {
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
     using T4 = typename V4<R>::T;
@@ -133,25 +149,70 @@ __global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v)
     ((T4 *)v.pk_q)[i] = make_v4<R>(qq[0] * ir2, qq[1] * ir2, qq[2] * ir2, (R)0);
 }
 
+template <typename R, int D, int K, bool ONE, bool PERSIST>
+__global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v) {
+    if constexpr (PERSIST) {
+        for (int base = blockIdx.x * blockDim.x; base < v.np; base += gridDim.x * blockDim.x)
+            heat_one<R, D, K, ONE>(v, base + threadIdx.x);
+    } else {
+        heat_one<R, D, K, ONE>(v, blockIdx.x * blockDim.x + threadIdx.x);
+    }
+}
+
+// The persistent form is instantiated for the mixed-precision passes only;
+// FP64 engines launch one thread per particle whatever tuning.persistent says.
+template <typename R, int D, int K, bool ONE>
+void density_launch(const View &v, int stage, int block, cudaStream_t s) {
+    if (std::is_same<R, float>::value && v.persist) {
+        auto *fn = k_density<R, D, K, ONE, std::is_same<R, float>::value>;
+        fn<<<pass_grid(v, fn, block), block, 0, s>>>(v, stage);
+    } else {
+        k_density<R, D, K, ONE, false><<<(v.np + block - 1) / block, block, 0, s>>>(v, stage);
+    }
+}
+
+template <typename R, int D, int K, bool ONE>
+void heat_launch(const View &v, int block, cudaStream_t s) {
+    if (std::is_same<R, float>::value && v.persist) {
+        auto *fn = k_heat<R, D, K, ONE, std::is_same<R, float>::value>;
+        fn<<<pass_grid(v, fn, block), block, 0, s>>>(v);
+    } else {
+        k_heat<R, D, K, ONE, false><<<(v.np + block - 1) / block, block, 0, s>>>(v);
+    }
+}
+
 void launch_density(const View &v, int precision, int kernel, int stage, int block,
                     cudaStream_t s) {
     if (v.np <= 0) return;
-    int nb = (v.np + block - 1) / block;
     if (v.one_sim)
-        SPH_DISPATCH(precision, v.dim, kernel,
-                     (k_density<R, D, K, true><<<nb, block, 0, s>>>(v, stage)));
+        SPH_DISPATCH(precision, v.dim, kernel, (density_launch<R, D, K, true>(v, stage, block, s)));
     else
-        SPH_DISPATCH(precision, v.dim, kernel,
-                     (k_density<R, D, K, false><<<nb, block, 0, s>>>(v, stage)));
+        SPH_DISPATCH(precision, v.dim, kernel, (density_launch<R, D, K, false>(v, stage, block, s)));
 }
 
 void launch_heat(const View &v, int precision, int kernel, int block, cudaStream_t s) {
     if (v.np <= 0) return;
-    int nb = (v.np + block - 1) / block;
     if (v.one_sim)
-        SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K, true><<<nb, block, 0, s>>>(v)));
+        SPH_DISPATCH(precision, v.dim, kernel, (heat_launch<R, D, K, true>(v, block, s)));
     else
-        SPH_DISPATCH(precision, v.dim, kernel, (k_heat<R, D, K, false><<<nb, block, 0, s>>>(v)));
+        SPH_DISPATCH(precision, v.dim, kernel, (heat_launch<R, D, K, false>(v, block, s)));
+}
+
+int resident_blocks(const void *kernel, int block) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_pair(kernel, block * 64 + dev);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0);
+    const int cap = (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+    cache[key] = cap;
+    return cap;
 }
 
 // ---- thermostat: per-chunk FP64 partial sums of T, then one thread per

@@ -181,6 +181,18 @@ __device__ __forceinline__ void for_pairs(const View &v, const SimDev &S,
     }
 }
 
+// Blocks of a pair-pass launch: one thread per particle, or with v.persist
+// only the blocks the device holds at once (SMs x resident blocks of this
+// kernel at this block size, cached per kernel), which then walk the
+// particles grid-stride.
+int resident_blocks(const void *kernel, int block);
+template <typename F> inline int pass_grid(const View &v, F *kernel, int block) {
+    const int nb = (v.np + block - 1) / block;
+    if (!v.persist) return nb;
+    const int cap = resident_blocks((const void *)kernel, block);
+    return nb < cap ? nb : cap;
+}
+
 // Warp-aggregated per-simulation counter update.
 __device__ __forceinline__ void add_pair_count(unsigned long long *cnt, int s, unsigned c) {
     unsigned act = __activemask();

@@ -183,9 +183,18 @@ class Engine:
         return out
 
     def last_pair_total(self):
+        """Unordered pairs of one evaluation (all simulations): the first
+        evaluation of the last step or derivative call."""
         n = ctypes.c_int64()
         check(self._lib.sph_last_pair_total(self._h, ctypes.byref(n)), "sph_last_pair_total")
         return n.value
+
+    def last_pair_counts(self, nslots):
+        """The same per simulation slot: an int64 array of length nslots."""
+        out = np.zeros(int(nslots), dtype=np.int64)
+        check(self._lib.sph_last_pair_counts(self._h, out.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int64)), int(nslots)), "sph_last_pair_counts")
+        return out
 
     def diagnostics(self, sim):
         out = (ctypes.c_double * 6)()
@@ -199,20 +208,23 @@ class Engine:
         check(self._lib.sph_get_tuning(self._h, ctypes.byref(t)), "sph_get_tuning")
         return {"block_size": t.block_size, "use_graph": t.use_graph,
                 "steps_per_graph": t.steps_per_graph, "rebin": t.rebin,
-                "cell_ratio": t.cell_ratio, "pair_scheme": t.pair_scheme}
+                "cell_ratio": t.cell_ratio, "pair_scheme": t.pair_scheme,
+                "persistent": t.persistent}
 
     def set_tuning(self, **kw):
         """block_size, use_graph, steps_per_graph, cell_ratio, rebin (1: bin
         into cells only when a particle has used half of the cell slack,
         VerletList.ponder_rebuild's skin reuse; 0: every step) and
         pair_scheme (0: cell windows; 1: cluster pairs, for 3D simulations
-        in mixed precision without collisions)."""
+        in mixed precision without collisions) and persistent (1: the
+        cell-window passes as persistent grid-stride launches)."""
         cur = self.tuning
         cur.update(kw)
         t = SphTuning(block_size=int(cur["block_size"]), use_graph=int(cur["use_graph"]),
                       steps_per_graph=int(cur["steps_per_graph"]), rebin=int(cur["rebin"]),
                       cell_ratio=float(cur["cell_ratio"]),
-                      pair_scheme=int(cur["pair_scheme"]))
+                      pair_scheme=int(cur["pair_scheme"]),
+                      persistent=int(cur["persistent"]))
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), "sph_set_tuning")
 
     def rebin_count(self):

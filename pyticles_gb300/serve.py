@@ -166,12 +166,13 @@ class Group:
                 if code:
                     job.error = _abi.STATUS_NAMES.get(code, str(code))
                     failed.add(sim)
-        pairs = self.engine.last_pair_total()
-        total = sum(j.n for j in self.active.values())
+        # each job's own pair set (of the chunk's last step) x 2 evaluations
+        # per step x the chunk's steps
+        counts = self.engine.last_pair_counts(max(self.active) + 1)
         done = []
         for sim, job in list(self.active.items()):
             job.remaining -= steps
-            job.work += 2.0 * steps * pairs * (job.n / total)
+            job.work += 2.0 * steps * float(counts[sim])
             if sim in failed or job.remaining <= 0:
                 if sim not in failed:
                     job.result = self.engine.get_state(sim)
@@ -288,12 +289,28 @@ class Server:
         return self.report(completed, makespan, jobs)
 
     def report(self, completed, makespan, jobs):
+        """Latency (completion - visible), queueing delay (admission -
+        visible) and service time (completion - admission) at p50 / p99 over
+        the jobs that completed; jobs still running or still waiting when a
+        time limit stopped the run are counted as such, and the work they
+        did counts toward the achieved load."""
         ok = [j for j in completed if j.error is None]
-        lat = np.array([j.finished - j.visible for j in ok]) if ok else np.zeros(1)
-        queue = np.array([j.admitted - j.visible for j in ok]) if ok else np.zeros(1)
-        service = np.array([j.finished - j.admitted for j in ok]) if ok else np.zeros(1)
-        work = sum(j.work for j in completed)
+
+        def pct(x):
+            x = np.asarray(x, dtype=np.float64)
+            if len(x) == 0:
+                return {"p50": None, "p99": None, "n": 0}
+            return {"p50": float(np.percentile(x, 50)), "p99": float(np.percentile(x, 99)),
+                    "n": int(len(x))}
+
+        lat = pct([j.finished - j.visible for j in ok])
+        admitted = [j for j in jobs if j.admitted is not None and j.visible is not None]
+        queue = pct([j.admitted - j.visible for j in admitted])
+        service = pct([j.finished - j.admitted for j in ok])
+        work = sum(j.work for j in jobs)
         window = max(j.arrival for j in jobs) if jobs else 0.0
+        running = [j for j in jobs if j.admitted is not None and j.finished is None]
+        waiting = [j for j in jobs if j.admitted is None and j.finished is None]
         return {
             "hbm_budget_bytes": self.hbm_budget,
             "capacity_particles": {d: g.capacity for d, g in self.groups.items()},
@@ -301,11 +318,12 @@ class Server:
             "peak_hbm_bytes": sum(g.peak * self.bpp[d] for d, g in self.groups.items()),
             "jobs": len(jobs), "completed": len(ok),
             "failed": len([j for j in completed if j.error]), "rejected": len(self.rejected),
-            "latency_p50_s": float(np.percentile(lat, 50)),
-            "latency_p99_s": float(np.percentile(lat, 99)),
-            "queue_p50_s": float(np.percentile(queue, 50)),
-            "service_p50_s": float(np.percentile(service, 50)),
+            "unfinished_running": len(running), "unfinished_waiting": len(waiting),
+            "latency_s": lat, "queue_s": queue, "service_s": service,
+            "latency_p50_s": lat["p50"], "latency_p99_s": lat["p99"],
+            "queue_p50_s": queue["p50"], "service_p50_s": service["p50"],
             "makespan_s": makespan, "arrival_window_s": window,
+            "work_pair_interactions": work,
             "achieved_pair_interactions_per_s": work / makespan if makespan > 0 else 0.0,
         }
 

@@ -287,6 +287,36 @@ def run_case(R, name, r, v, m, box_len, dim, hs, hl, cutoff, tol, kname, T0, ste
     print(f"{name}: n={n} nip={ni} steps={steps} {time.time() - t0:.1f}s -> {path}")
 
 
+def trajectory_case(R, name, r, v, m, box_len, dim, hs, hl, cutoff, kname, T0, steps, every,
+                    dt=1e-3, integ="ieuler"):
+    """A long trajectory of SmoothParticleSystem.update (particles.py:459-494):
+    the state every `every` steps and the properties after the last step."""
+    t0 = time.time()
+    n = r.shape[0]
+    u = ref_initial_energy(R, r, v, m, box_len, dim, hs, hl, cutoff, 0.0, kname, T0)
+    p, nl, force = build_system(R, r, v, m, u, box_len, dim, hs, hl, cutoff, 0.0, kname, integ)
+    marks, rs, vs, us = [], [], [], []
+    for s in range(1, steps + 1):
+        p.update(dt)
+        if s % every == 0:
+            marks.append(s)
+            rs.append(p.r[:n, :dim].copy())
+            vs.append(p.v[:n, :dim].copy())
+            us.append(p.u[:n].copy())
+    after = snapshot(p, dim, n)
+    out = dict(name=name, dim=dim, kernel=kname,
+               box=np.array(list(box_len) + [1.0] * (3 - dim)), h_short=hs, h_long=hl,
+               cutoff=cutoff, tolerance=0.0, dt=dt, integrator=integ, thermostat=0,
+               thermostat_temp=1.0, T0=T0, steps=steps, r0=r, v0=v, m=m, u0=u,
+               marks=np.array(marks), r_marks=np.array(rs), v_marks=np.array(vs),
+               u_marks=np.array(us))
+    for k, val in after.items():
+        out["after_" + k] = val
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: n={n} steps={steps} {time.time() - t0:.1f}s -> {path}")
+
+
 def collision_case(R, name, r, v, m, box_len, dim, hs, hl, cutoff, kname, T0, steps, coll,
                    dt=1e-3, integ="ieuler"):
     """SmoothParticleSystem.update with p.forces = [SpamComplete's sequence,
@@ -487,7 +517,9 @@ def splat_maps(R):
 
 
 def main():
-    refdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py REFERENCE_DIR [case ...]")
+    refdir = sys.argv[1]
     which = set(sys.argv[2:])
     tmp, R = load_reference(refdir)
     try:
@@ -524,6 +556,13 @@ def main():
             prm, r, v, m, T0 = workloads.config_2d(32, 1000)
             run_case(R, "lucy2d_1024", r, v, m, (32.0, 32.0), 2, 3.0, 6.0, 6.0, 0.0, "lucy",
                      T0, steps=2)
+        if "traj2d_1024" in which:
+            # the plain small configuration at its own length: the 32^2 fluid
+            # of lucy2d_1024, 100 improved-Euler steps at dt = 1e-3 (no
+            # viscosity: the reference has none); slow, so only on request
+            prm, r, v, m, T0 = workloads.config_2d(32, 1000)
+            trajectory_case(R, "traj2d_1024", r, v, m, (32.0, 32.0), 2, 3.0, 6.0, 6.0, "lucy",
+                            T0, steps=100, every=20)
         if want("gauss2d_256"):
             prm, r, v, m, T0 = workloads.lattice_system(16, 2, spacing=1.0, jitter=0.1,
                                                         temperature=0.6, seed=13)

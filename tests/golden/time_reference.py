@@ -23,7 +23,9 @@ from pyticles_gb300 import workloads  # noqa: E402
 
 
 def main():
-    refdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: time_reference.py REFERENCE_DIR [steps]")
+    refdir = sys.argv[1]
     steps = int(sys.argv[2]) if len(sys.argv) > 2 else 1
     tmp, R = make_golden.load_reference(refdir)
     prm, r, v, m, T0 = workloads.config_2d(32, 1000)

@@ -363,3 +363,63 @@ def test_results_do_not_depend_on_block_size_or_graphs():
             ref = out
         for a, b in zip(out, ref):
             assert np.array_equal(a, b), (block, graph)
+
+
+@pytest.mark.parametrize("heat", [False, True])
+def test_persistent_launch_gives_the_same_bits(heat):
+    """tuning.persistent = 1 (the pair passes as resident blocks walking the
+    flattened table grid-stride) changes which block computes a particle,
+    never its sums: batched and single-simulation engines give the same
+    bits as with one thread per particle."""
+    if heat:
+        sims = [workloads.config_3d(12, 3300 + k) for k in range(2)]
+        sims = [(p, r, v, m, workloads.vdw_energy(np.full(len(r), 0.7), T))
+                for p, r, v, m, T in sims]
+    else:
+        sims = [(p, r, v, m, oracle.initial_energy(p, r, v, m, T))
+                for p, r, v, m, T in workloads.batched_2d(4, seed_base=4400, n_lo=256,
+                                                          n_hi=4096, ramp_steps=20)]
+    for group in (sims, sims[:1]):
+        total = sum(len(s[1]) for s in group)
+        out = []
+        for persistent in (0, 1):
+            with Engine(group[0][0], "mixed", max_particles=total, max_sims=len(group)) as e:
+                ids = [e.add(*st) for st in group]
+                e.set_tuning(persistent=persistent, steps_per_graph=3)
+                assert e.tuning["persistent"] == persistent
+                e.advance(6)
+                e.sync()
+                out.append([e.get_state(i) for i in ids])
+        for a, b in zip(*out):
+            for x, y in zip(a, b):
+                assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("name", ["lucy2d_400", "rk4_2d_144", "euler2d_144"])
+def test_pair_total_is_one_evaluation(name):
+    """The metric's unit of work: after a step (2 evaluations for improved
+    Euler, 4 for RK4) the pair total is the pair set of ONE evaluation, the
+    step's first, i.e. the oracle's pair count at the state the step started
+    from; per simulation the same, and the totals add up."""
+    g = load(name)
+    prm = params_of(g)
+    for precision in ("mixed", "fp64"):
+        e, s = one(prm, g["r0"], g["v0"], g["m"], g["u0"], precision)
+        with e:
+            e.advance(1)
+            e.sync()
+            assert e.last_pair_total() == len(g["iap"])
+            assert e.last_pair_counts(1)[0] == len(g["iap"])
+    sims = [(p, r, v, m, oracle.initial_energy(p, r, v, m, T))
+            for p, r, v, m, T in workloads.batched_2d(3, seed_base=4500, n_lo=256, n_hi=2048,
+                                                      ramp_steps=10)]
+    total = sum(len(x[1]) for x in sims)
+    with Engine(sims[0][0], "mixed", max_particles=total, max_sims=4) as e:
+        ids = [e.add(*x) for x in sims]
+        e.advance(1)
+        e.sync()
+        counts = e.last_pair_counts(4)
+        ref = [oracle.derivatives(*x)["nip"] for x in sims]
+        assert [int(counts[i]) for i in ids] == ref
+        assert counts[3] == 0
+        assert e.last_pair_total() == sum(ref)

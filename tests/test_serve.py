@@ -56,6 +56,13 @@ class FakeEngine:
     def last_pair_total(self):
         return sum(s["n"] for s in self.sims.values()) * 10
 
+    def last_pair_counts(self, nslots):
+        out = np.zeros(nslots, dtype=np.int64)
+        for sid, s in self.sims.items():
+            if sid < nslots:
+                out[sid] = s["n"] * 10
+        return out
+
     def close(self):
         pass
 
@@ -91,6 +98,33 @@ def test_jobs_run_exactly_their_steps_and_leave():
     assert rep["completed"] == 3 and rep["failed"] == 0
     assert [j.result[0] for j in jobs] == [25, 40, 7]
     assert not srv.groups[2].active and srv.groups[2].live == 0
+
+
+def test_each_job_is_credited_its_own_pairs():
+    """A job's work is its own pair count x 2 evaluations x its steps, not a
+    share of the chunk's total (the fake engine's pair set is 10 n)."""
+    srv = fake_server(1000)
+    jobs = [fake_job(0, 0.0, 2, 100, 25), fake_job(1, 0.0, 2, 200, 40),
+            fake_job(2, 0.0, 3, 50, 7)]
+    srv.run(jobs, realtime=False)
+    for j in jobs:
+        assert j.work == 2.0 * j.steps * 10 * j.n
+
+
+def test_time_limit_reports_unfinished_jobs():
+    """A run stopped by its time limit reports the jobs still running and
+    still waiting, counts their partial work, and splits latency, queueing
+    and service time at p50 / p99 over the jobs that finished."""
+    srv = fake_server(300, chunk=5, max_sims=2)
+    jobs = [fake_job(0, 0.0, 2, 100, 5), fake_job(1, 0.0, 2, 200, 10000),
+            fake_job(2, 0.0, 2, 250, 10), fake_job(3, 0.0, 2, 50, 10)]
+    rep = srv.run(jobs, realtime=False, time_limit=0.5)
+    assert rep["completed"] >= 1
+    assert rep["unfinished_running"] >= 1 and rep["unfinished_waiting"] >= 1
+    assert rep["completed"] + rep["unfinished_running"] + rep["unfinished_waiting"] == 4
+    assert rep["work_pair_interactions"] > sum(j.work for j in jobs if j.finished is not None)
+    for k in ("latency_s", "queue_s", "service_s"):
+        assert rep[k]["n"] >= 1 and rep[k]["p99"] >= rep[k]["p50"] >= 0
 
 
 def test_admission_waits_for_capacity_and_slots():
