@@ -423,3 +423,53 @@ def test_pair_total_is_one_evaluation(name):
         assert [int(counts[i]) for i in ids] == ref
         assert counts[3] == 0
         assert e.last_pair_total() == sum(ref)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config1_100_steps_match_reference(precision):
+    """The plain small configuration at its own length against the
+    reference's own SmoothParticleSystem.update: 100 improved-Euler steps of
+    the 32 x 32 fluid at dt = 1e-3 (viscosity off, as the reference has
+    none), state compared every 20 steps, properties after the last."""
+    g = load("traj2d_1024")
+    prm = params_of(g)
+    e, s = one(prm, g["r0"], g["v0"], g["m"], g["u0"], precision)
+    tol = STEP_TOL if precision == "fp64" else MIXED_TOL
+    with e:
+        done = 0
+        for k, mark in enumerate(g["marks"]):
+            e.advance(int(mark) - done)
+            done = int(mark)
+            e.sync()
+            r, v, u = e.get_state(s)
+            errs = {"r": rel_l2(r, g["r_marks"][k]), "v": rel_l2(v, g["v_marks"][k]),
+                    "u": rel_l2(u, g["u_marks"][k])}
+            record("traj100", f"traj2d_1024@{done}", precision, errs)
+            for key, err in errs.items():
+                assert err < tol, (done, key, err)
+        props = e.properties(s)
+        errs = {k: rel_l2(props[k], g["after_" + k]) for k in KEYS}
+        bounds = {k: STEP_TOL if precision == "fp64" else mixed_bound("lucy2d_1024", k)
+                  for k in KEYS}
+        record("traj100", "traj2d_1024@after", precision, errs, bounds)
+        for k, err in errs.items():
+            assert err < bounds[k], (k, err, bounds[k])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_viscous_config1_100_steps_match_oracle(precision):
+    """The same 100 steps with the artificial viscosity on (the plain small
+    configuration as specified), against the oracle's trajectory."""
+    prm, r, v, m, T0 = workloads.config_2d(32, 1000, viscosity=True)
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    e, s = one(prm, r, v, m, u, precision)
+    tol = STEP_TOL if precision == "fp64" else MIXED_TOL
+    with e:
+        e.advance(100)
+        e.sync()
+        rr, vv, uu = e.get_state(s)
+    r1, v1, u1, _ = oracle.advance(prm, r, v, m, u, 100)
+    errs = {"r": rel_l2(rr, r1), "v": rel_l2(vv, v1), "u": rel_l2(uu, u1)}
+    record("traj100", "visc2d_1024@100", precision, errs)
+    for key, err in errs.items():
+        assert err < tol, (key, err)

@@ -195,3 +195,21 @@ def test_geometry_floor_only_rounds_the_pair_geometry():
     assert 0 < rel_l2(b["vdot"], a["vdot"]) < 1e-5
     for k in ("rho", "vdot", "udot"):       # the mode is off again afterwards
         assert np.array_equal(a[k], c[k])
+
+
+def test_oracle_follows_the_reference_for_100_steps():
+    """The plain small configuration at its own length: 100 improved-Euler
+    steps of the 32 x 32 fluid (SmoothParticleSystem.update, particles.py:
+    459-494), compared every 20 steps and in the properties after the last."""
+    g = load("traj2d_1024")
+    prm = params_of(g)
+    r, v, u = g["r0"], g["v0"], g["u0"]
+    done = 0
+    for k, mark in enumerate(g["marks"]):
+        r, v, u, props = oracle.advance(prm, r, v, g["m"], u, int(mark) - done, step0=done)
+        done = int(mark)
+        for got, key in ((r, "r_marks"), (v, "v_marks"), (u, "u_marks")):
+            assert rel_l2(got, g[key][k]) < STEP_TOL, (mark, key)
+    assert done == int(g["steps"]) == 100
+    for key in ("rho", "rho_lr", "t", "p", "pco", "vdot", "udot"):
+        assert rel_l2(props[key], g["after_" + key]) < STEP_TOL, key
