@@ -30,11 +30,20 @@ using namespace sph;
 namespace {
 
 constexpr size_t kAlign = 256;
-// per particle: state A and B (72 B each), sort scratch (20), packed position /
-// velocity / force / heat vectors (4 x 32 in FP64), cell origin (24), nine
-// scalar and six vector-component outputs (120), one output staging column
-// (8); rounded up to 512 B.  Per cell: count, start, Morton rank, coordinates.
+// Per particle, in FP64 (the larger case), what sph_derivatives_noalloc
+// carves below: positions and velocities of states A and B and the cell
+// origins (5 x 3 x 8), the heat-flux and vdot components (2 x 3 x 8), u and m
+// of A and B (4 x 8), ids, simulations and sort scratch (9 x 4), five packed
+// vectors -- position, velocity, force factors, heat factors, neighbour
+// record -- (5 x 32), nine scalar outputs (9 x 8) and one output staging
+// column (8): 476 B, within the 512 B budgeted.  Per cell: count, start,
+// Morton rank, coordinates.  The per-array alignment padding is covered by
+// the 256 KiB added to the total.
+constexpr size_t kBytesUsedPerParticle =
+    5 * 3 * 8 + 2 * 3 * 8 + 4 * 8 + 9 * 4 + 5 * 32 + 9 * 8 + 8;
 constexpr size_t kBytesPerParticle = 512;
+static_assert(kBytesUsedPerParticle <= kBytesPerParticle,
+              "the per-particle carving outgrew the scratch budget");
 constexpr size_t kBytesPerCell = 32;
 constexpr size_t kScratchBytes = (size_t)SPH_NOALLOC_MAX_PARTICLES * kBytesPerParticle +
                                  (size_t)SPH_NOALLOC_MAX_CELLS * kBytesPerCell + (256u << 10);

@@ -15,8 +15,8 @@ import pytest
 
 from oracle import oracle
 from pyticles_gb300 import Engine, build, workloads
-from pyticles_gb300._abi import (NOALLOC_MAX_PARTICLES, SPH_EINVAL, SPH_FP64, SPH_MIXED, lib,
-                                 make_params)
+from pyticles_gb300._abi import (NOALLOC_MAX_PARTICLES, SPH_ECAPACITY, SPH_EINVAL, SPH_FP64,
+                                 SPH_MIXED, lib, make_params)
 
 pytestmark = pytest.mark.gpu
 
@@ -75,6 +75,41 @@ def test_noalloc_matches_engine_twice(case, precision):
         out = noalloc(prm, precision, r, v, m, u)
         for k in KEYS:
             assert rel(out[k], ref[k]) <= TOL, (k, rel(out[k], ref[k]))
+
+
+def test_noalloc_coarser_cells_in_a_sparse_box():
+    """A sparse 2D box that needs more cells than the scratch holds at half
+    the cutoff: the call falls back to coarser cells (up to four times the
+    cutoff) and still gives the oracle's FP64 evaluation; a box too large
+    even for those is refused with SPH_ECAPACITY, twice in a row."""
+    rng = np.random.default_rng(7)
+    n = 3000
+    prm = make_params(dim=2, box=(400.0, 400.0), kernel="lucy", h_short=0.8, h_long=1.0,
+                      cutoff=1.0, viscosity=True)
+    r = rng.uniform(0.0, 400.0, size=(n, 2))
+    # clumps, so that pairs exist at this density
+    r[: n // 2] = (r[: n // 2] % 40.0) + 100.0
+    v = rng.normal(0.0, 0.5, size=(n, 2))
+    m = np.ones(n)
+    u = np.full(n, 0.4)
+    ref = oracle.derivatives(prm, r, v, m, u)
+    assert ref["nip"] > 1000
+    for _ in range(2):
+        out = noalloc(prm, "fp64", r, v, m, u)
+        for k in KEYS:
+            assert rel(out[k], ref[k]) <= TOL, (k, rel(out[k], ref[k]))
+    big = make_params(dim=2, box=(5000.0, 5000.0), kernel="lucy", h_short=0.8, h_long=1.0,
+                      cutoff=1.0)
+    rb = rng.uniform(0.0, 5000.0, size=(200, 2))
+    import torch
+    bufs = [torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda:0")
+            for a in (rb, np.zeros((200, 2)), np.ones(200), np.zeros(200))]
+    outb = torch.zeros(200, dtype=torch.float64, device="cuda:0")
+    for _ in range(2):
+        st = lib().sph_derivatives_noalloc(ctypes.byref(big), SPH_FP64, 200,
+                                           *[b.data_ptr() for b in bufs], outb.data_ptr(),
+                                           *([None] * 7), None)
+        assert st == SPH_ECAPACITY
 
 
 def test_noalloc_rejects_sizes_beyond_its_limit():
