@@ -665,7 +665,7 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_cl_force(const __grid_c
             if constexpr (NEAR) {
                 gs = kernel_g<K, float, true>(ks, dd);
                 float ps = fvi.w + fvj.w;
-                if (visc && dvdx < 0.0f) {
+                if (visc && dvdx < 0.0f && gs != 0.0f) {   // gs = 0: ps does not enter
                     const float rhoj = c.crho[sj];
                     const float mu = fdiv<float>(hs * dvdx, rsq + eps_h2);
                     ps += fdiv<float>(2.0f * (-alpha_c * mu + beta * mu * mu), rhoi + rhoj);

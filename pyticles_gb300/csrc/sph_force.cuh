@@ -229,8 +229,10 @@ __device__ __forceinline__ void force_one(const View &v, int stage, int mode, in
         if constexpr (NEAR) {
             gs = kernel_g<K, R, true>(ks, dd);
             R ps = fsi + (D == 2 ? fvj.z : fvj.w);
-            if (visc && dvdx < (R)0) {
-                // Monaghan viscosity on approaching pairs
+            // Monaghan viscosity on approaching pairs within the short
+            // support (beyond it gs = 0, so ps no longer enters gsum and the
+            // warp skips the block when none of its pairs needs it)
+            if (visc && dvdx < (R)0 && gs != (R)0) {
                 const R rhoj = D == 2 ? fvj.w : RHO[j];
                 R mu = fdiv<R>(hs * dvdx, rsq + eps_h2);
                 ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), rhoi + rhoj);
