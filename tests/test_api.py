@@ -153,20 +153,52 @@ def test_engine_params_from_reference_objects():
     assert p.engine_params(1e-3, thermostat=False).thermostat == 0
 
 
-def test_integrator_takes_only_a_systems_own_methods():
+def test_integrator_runs_any_callbacks_like_the_reference():
     """integrator.euler/imp_euler/rk4 run the engine step for the system
     whose gather_state, derivatives, gather_derivatives and scatter_state
-    they get; anything else has no host integrator to fall back on."""
+    they get; any other callables get the reference's generic scheme
+    (integrator.py:14-103): here a harmonic oscillator x' = v, v' = -x, one
+    step of each against the scheme written out."""
     p = SmoothParticleSystem(4, d=2, maxn=4)
     q = SmoothParticleSystem(4, d=2, maxn=4)
     own = (p.gather_state, p.derivatives, p.gather_derivatives, p.scatter_state)
     assert integrator._system(*own) is p
     mixed = (p.gather_state, q.derivatives, p.gather_derivatives, p.scatter_state)
-    swapped = (p.gather_state, p.derivatives, p.gather_state, p.scatter_state)
-    for fns in (mixed, swapped, (lambda: None,) + own[1:]):
-        for step in (integrator.euler, integrator.imp_euler, integrator.rk4):
-            with pytest.raises(NotImplementedError):
-                step(*fns, 1e-3)
+    assert integrator._system(*mixed) is None
+
+    class Osc:
+        def __init__(self):
+            self.x = np.array([1.0, 0.5])
+            self.calls = 0
+
+        def get_state(self):
+            return self.x.copy()
+
+        def calc(self):
+            self.calls += 1
+            self.rate = np.array([self.x[1], -self.x[0]])
+
+        def get_derivs(self):
+            return self.rate
+
+        def set_state(self, x):
+            self.x = np.asarray(x, dtype=float)
+
+    f = lambda x: np.array([x[1], -x[0]])
+    dt = 0.1
+    x0 = np.array([1.0, 0.5])
+    c1 = f(x0) * dt
+    want = {"euler": x0 + c1,
+            "imp_euler": x0 + (c1 + f(x0 + c1) * dt) / 2}
+    k2 = f(x0 + c1 / 2) * dt
+    k3 = f(x0 + k2 / 2) * dt
+    k4 = f(x0 + k3) * dt
+    want["rk4"] = x0 + (1.0 / 6.0) * (c1 + 2. * k2 + 2. * k3 + k4)
+    for name, evals in (("euler", 1), ("imp_euler", 2), ("rk4", 4)):
+        o = Osc()
+        getattr(integrator, name)(o.get_state, o.calc, o.get_derivs, o.set_state, dt)
+        assert np.array_equal(o.x, want[name]), name
+        assert o.calls == evals
     # a system the engine refuses (no periodic box) keeps its own integrator
     nl = VerletList(p, cutoff=1.0, tolerance=0.0)
     p.nlists.append(nl)
