@@ -420,3 +420,42 @@ def test_integrator_functions_run_the_engine_step(name, fn):
     a.close()
     b.close()
 
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,fn", [("ieuler", integrator.imp_euler), ("rk4", integrator.rk4),
+                                     ("euler", integrator.euler)])
+def test_generic_integrator_over_gpu_derivatives(name, fn):
+    """The generic scheme (callables that are not one system's own bound
+    methods, here wrappers of them) with the GPU evaluation as calc_derivs,
+    followed by the box wrap, agrees with update(dt) of a twin system to the
+    FP64 step tolerance over three steps."""
+    g = load("lucy2d_400")
+    twins = []
+    for integ in ("ieuler", name):
+        box = PeriodicBox(xmax=float(g["box"][0]), ymax=float(g["box"][1]), zmax=1)
+        n = len(g["r0"])
+        p = SmoothParticleSystem(n, d=2, maxn=n, hshort=float(g["h_short"]),
+                                 hlong=float(g["h_long"]), simbox=box, integrator=integ,
+                                 precision="fp64")
+        p.r[:] = g["r0"]
+        p.v[:] = g["v0"]
+        p.m[:] = g["m"]
+        p.u[:] = g["u0"]
+        nl = VerletList(p, cutoff=float(g["cutoff"]), tolerance=0.0)
+        p.nlists.append(nl)
+        p.nl_default = nl
+        p.forces.append(SpamComplete(p, nl, eta=0.0, zeta=0.0, cgrad=0.0))
+        twins.append(p)
+    a, b = twins
+    dt = float(g["dt"])
+    fns = (lambda: a.gather_state(), lambda: a.derivatives(), lambda: a.gather_derivatives(),
+           lambda x: a.scatter_state(x))
+    assert integrator._system(*fns) is None
+    for _ in range(3):
+        fn(*fns, dt)
+        a.box.apply(a)
+        b.update(dt)
+    n = len(g["r0"])
+    for x, y in ((a.r[:n], b.r[:n]), (a.v[:n], b.v[:n]), (a.u[:n], b.u[:n])):
+        assert np.linalg.norm(x - y) / np.linalg.norm(y) < 1e-10
