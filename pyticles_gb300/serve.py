@@ -234,10 +234,19 @@ class Server:
                                 engine_factory, streams[d], schemes[d]) for d in (2, 3)}
         self.rejected = []
 
-    def run(self, jobs, realtime=True, time_limit=None):
+    def run(self, jobs, realtime=True, time_limit=None, concurrent=True):
         """Serves `jobs`.  With realtime, a job becomes visible at its arrival
         time on the server clock; otherwise all jobs are visible at once.
-        Latency and queueing delay are measured from when a job is visible."""
+        Latency and queueing delay are measured from when a job is visible.
+
+        concurrent: each dimension group runs its own loop on its own host
+        thread (admission, chunk, retirement), so a group starts its next
+        chunk as soon as its last one finished instead of waiting for the
+        other group's chunk; the engines' calls release the interpreter
+        lock while they wait on their streams.  Otherwise one loop launches
+        both groups' chunks and waits for both before the next."""
+        if concurrent:
+            return self._run_concurrent(jobs, realtime, time_limit)
         jobs = sorted(jobs, key=lambda j: j.arrival)
         pending = collections.deque(jobs)
         waiting = []
@@ -285,6 +294,84 @@ class Server:
             launched = {d: g.launch() for d, g in self.groups.items()}
             for d, g in self.groups.items():
                 completed.extend(g.finish(launched[d], now))
+        makespan = now()
+        return self.report(completed, makespan, jobs)
+
+    def _admit(self, g, waiting, t, completed):
+        """First-fit admission of the visible jobs into group g; returns the
+        jobs still waiting.  Malformed and oversized jobs are rejected."""
+        still = []
+        for job in waiting:
+            why = malformed(job)
+            if why is not None:
+                job.error = "rejected: " + why
+                job.finished = t
+                self.rejected.append(job)
+                continue
+            if job.n > g.capacity:
+                job.error = "rejected: larger than the group's HBM budget"
+                job.finished = t
+                self.rejected.append(job)
+            elif g.fits(job):
+                try:
+                    g.admit(job, t)
+                except _abi.SphError as exc:
+                    job.error = _abi.STATUS_NAMES.get(exc.status, str(exc.status))
+                    job.finished = t
+                    completed.append(job)
+            else:
+                still.append(job)
+        return still
+
+    def _run_concurrent(self, jobs, realtime, time_limit):
+        import threading
+        jobs = sorted(jobs, key=lambda j: j.arrival)
+        queues = {d: collections.deque() for d in self.groups}
+        for job in jobs:
+            # a job of no served dimension goes to the 2D loop, which rejects it
+            queues[job.dim if job.dim in self.groups else 2].append(job)
+        completed = []
+        lock = threading.Lock()
+        errors = []
+        t0 = self.clock()
+        now = lambda: self.clock() - t0
+
+        def serve_group(d):
+            g = self.groups[d]
+            pending, waiting = queues[d], []
+            try:
+                while pending or waiting or g.active:
+                    t = now()
+                    if time_limit is not None and t > time_limit:
+                        break
+                    while pending and (not realtime or pending[0].arrival <= t):
+                        job = pending.popleft()
+                        job.visible = t
+                        waiting.append(job)
+                    done = []
+                    with lock:
+                        waiting = self._admit(g, waiting, t, done)
+                        completed.extend(done)
+                    if not g.active:
+                        if pending and realtime:
+                            wait = pending[0].arrival - now()
+                            if wait > 0:
+                                time.sleep(min(wait, 0.05))
+                        continue
+                    steps = g.launch()
+                    retired = g.finish(steps, now)
+                    with lock:
+                        completed.extend(retired)
+            except Exception as exc:   # re-raised in the calling thread
+                errors.append(exc)
+
+        threads = [threading.Thread(target=serve_group, args=(d,)) for d in self.groups]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0]
         makespan = now()
         return self.report(completed, makespan, jobs)
 

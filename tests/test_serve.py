@@ -90,23 +90,27 @@ def fake_server(budget_particles, chunk=10, max_sims=4):
                   engine_factory=FakeEngine, clock=FakeClock(), group_params={2: None, 3: None})
 
 
-def test_jobs_run_exactly_their_steps_and_leave():
+@pytest.mark.parametrize("concurrent", [True, False])
+def test_jobs_run_exactly_their_steps_and_leave(concurrent):
+    """Both loops: one host thread per dimension group (the default) and the
+    single loop that waits for both groups' chunks."""
     srv = fake_server(1000)
     jobs = [fake_job(0, 0.0, 2, 100, 25), fake_job(1, 0.0, 2, 200, 40),
             fake_job(2, 0.0, 3, 50, 7)]
-    rep = srv.run(jobs, realtime=False)
+    rep = srv.run(jobs, realtime=False, concurrent=concurrent)
     assert rep["completed"] == 3 and rep["failed"] == 0
     assert [j.result[0] for j in jobs] == [25, 40, 7]
     assert not srv.groups[2].active and srv.groups[2].live == 0
 
 
-def test_each_job_is_credited_its_own_pairs():
+@pytest.mark.parametrize("concurrent", [True, False])
+def test_each_job_is_credited_its_own_pairs(concurrent):
     """A job's work is its own pair count x 2 evaluations x its steps, not a
     share of the chunk's total (the fake engine's pair set is 10 n)."""
     srv = fake_server(1000)
     jobs = [fake_job(0, 0.0, 2, 100, 25), fake_job(1, 0.0, 2, 200, 40),
             fake_job(2, 0.0, 3, 50, 7)]
-    srv.run(jobs, realtime=False)
+    srv.run(jobs, realtime=False, concurrent=concurrent)
     for j in jobs:
         assert j.work == 2.0 * j.steps * 10 * j.n
 
