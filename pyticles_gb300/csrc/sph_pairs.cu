@@ -14,8 +14,10 @@
 namespace sph {
 
 // At most 64 registers (4 blocks of 256 per SM): the two loop bodies of
-// for_pairs would otherwise take 80 and cost 5-20% in occupancy; 51 for a
-// single simulation (its constants are kernel parameters), 3% faster again.
+// for_pairs would otherwise take 80 and cost 5-20% in occupancy.  A single
+// simulation (its constants are kernel parameters): 2D mixed precision at
+// 32 registers (7 blocks, 60 B spilled), measured 6.3% faster than 48 and 2%
+// faster than 40; 3D and FP64 at 51.
 template <typename R, int D, int K, bool ONE>
 __device__ __forceinline__ void density_one(const View &v, int stage, int i) {
     const bool active = i < v.np;
@@ -93,7 +95,7 @@ __device__ __forceinline__ void density_one(const View &v, int stage, int i) {
 // One thread per particle; PERSIST: the resident blocks of pass_grid walk
 // the particles grid-stride (the same per-particle work, the same bits).
 template <typename R, int D, int K, bool ONE, bool PERSIST>
-__global__ void __launch_bounds__(256, ONE ? 5 : 4) k_density(const __grid_constant__ View v, int stage) {
+__global__ void __launch_bounds__(256, ONE ? ((D == 2 && sizeof(R) == 4) ? 7 : 5) : 4) k_density(const __grid_constant__ View v, int stage) {
     if constexpr (PERSIST) {
         for (int base = blockIdx.x * blockDim.x; base < v.np; base += gridDim.x * blockDim.x)
             density_one<R, D, K, ONE>(v, stage, base + threadIdx.x);
