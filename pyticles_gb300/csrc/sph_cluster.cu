@@ -641,9 +641,9 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_cl_force(const __grid_c
     const SimDev &S = cl_sim<ONE>(v, sim);
     const SimConst<float> &sc = S.cf;
     const PairCtx x = pair_ctx(S, cl_geom<ONE>(c, sim), sc.thr_hi);
-    const KConst<float> ks = make_kconst<float>(S, 0), kl = make_kconst<float>(S, 1);
+    // the long kernel with the cohesive factor -2a folded in (see k_force)
+    const KConst<float> ks = make_kconst<float>(S, 0), kl = make_kconst_cohesive<float>(S);
     const float hs = sc.hs, eps_h2 = sc.eps_h2, alpha_c = sc.alpha_c, beta = sc.beta;
-    const float pl2 = sc.pl2;
     const float4 fvi = c.cfv[si];
     const float rhoi = c.crho[si];
     const float4 qi = heat ? c.cq[si] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -661,7 +661,7 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_cl_force(const __grid_c
             const float gl = kernel_g<K, float, true>(kl, dd);
             const float4 fvj = c.cfv[sj];
             const float dvdx = (fvj.x - fvi.x) * d[0] + (fvj.y - fvi.y) * d[1] + (fvj.z - fvi.z) * d[2];
-            float gsum = pl2 * gl, gs = 0.0f;
+            float gsum = gl, gs = 0.0f;
             if constexpr (NEAR) {
                 gs = kernel_g<K, float, true>(ks, dd);
                 float ps = fvi.w + fvj.w;
@@ -670,16 +670,16 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_cl_force(const __grid_c
                     const float mu = fdiv<float>(hs * dvdx, rsq + eps_h2);
                     ps += fdiv<float>(2.0f * (-alpha_c * mu + beta * mu * mu), rhoi + rhoj);
                 }
-                gsum = ps * gs + pl2 * gl;
+                gsum = ps * gs + gl;
             }
             ax[0].add(gsum * d[0]);
             ax[1].add(gsum * d[1]);
             ax[2].add(gsum * d[2]);
-            float du = 0.5f * gsum * dvdx * pj.w;
+            float du = gsum * dvdx * pj.w;   // twice the term, halved at the end
             if (heat && NEAR) {
                 const float4 qj = c.cq[sj];
                 const float dq = (qi.x + qj.x) * d[0] + (qi.y + qj.y) * d[1] + (qi.z + qj.z) * d[2];
-                du -= dq * gs * pj.w;
+                du -= 2.0f * dq * gs * pj.w;
             }
             ud.add(du);
         },
@@ -691,7 +691,7 @@ __global__ void __launch_bounds__(kBlock, ONE ? 4 : 3) k_cl_force(const __grid_c
         });
     float vd[3];
     for (int a = 0; a < 3; ++a) vd[a] = (float)quad_sum(ax[a].get64());
-    const float u = (float)quad_sum(ud.get64());
+    const float u = (float)(0.5 * quad_sum(ud.get64()));
     if (jj != 0 || gi < 0) return;
     for (int a = 0; a < 3; ++a) ((float *)v.vdot[a])[gi] = vd[a];
     ((float *)v.udot)[gi] = u;

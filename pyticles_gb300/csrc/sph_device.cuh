@@ -157,6 +157,17 @@ __device__ __forceinline__ KConst<R> make_kconst(const SimDev &S, int which) {
     return k;
 }
 
+// The long kernel's constants with the cohesive factor -2a folded into its
+// gradient (the force passes need only -2a grad W_l).
+template <typename R>
+__device__ __forceinline__ KConst<R> make_kconst_cohesive(const SimDev &S) {
+    KConst<R> k = make_kconst<R>(S, 1);
+    const SimConst<R> &c = sconst<R>(S);
+    k.g0 = c.g0_pl;
+    k.g0_h2 = c.g0_h2_pl;
+    return k;
+}
+
 template <typename R> __device__ __forceinline__ R rexp(R x);
 template <> __device__ __forceinline__ float rexp<float>(float x) { return expf(x); }
 template <> __device__ __forceinline__ double rexp<double>(double x) { return exp(x); }

@@ -303,7 +303,11 @@ void fill_const(SimConst<R> &c, const sph_engine *e, const Sim &S, const SimDev 
     c.eps_h2 = (R)(p.visc_eps * p.h_short * p.h_short);
     c.alpha_c = (R)(p.visc_alpha * p.sound_speed);
     c.beta = (R)p.visc_beta;
-    c.pl2 = (R)(-2.0 * p.adash);
+    // the cohesive factor -2a folded into the long kernel's gradient
+    // constants: the force passes take -2a grad W_l as one kernel evaluation
+    const double g0l = kernel_g0(p.kernel, p.h_long, d.sig_l);
+    c.g0_pl = (R)(g0l * (-2.0 * p.adash));
+    c.g0_h2_pl = (R)(g0l / (p.h_long * p.h_long) * (-2.0 * p.adash));
     c.kappa = (R)p.thermalk;
 }
 

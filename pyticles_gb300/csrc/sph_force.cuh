@@ -200,11 +200,11 @@ __device__ __forceinline__ void force_one(const View &v, int stage, int mode, in
     const SimDev &S = ONE ? v.one : v.sims[s];
     if (S.cl_on) return;   // evaluated (and integrated) by the cluster passes
     KConst<R> ks = make_kconst<R>(S, 0);
-    KConst<R> kl = make_kconst<R>(S, 1);
+    // the long kernel with pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a folded in
+    KConst<R> kl = make_kconst_cohesive<R>(S);
     const SimConst<R> &sc = sconst<R>(S);
     const R hs = sc.hs, eps_h2 = sc.eps_h2;
     const R alpha_c = sc.alpha_c, beta = sc.beta;
-    const R pl2 = sc.pl2;  // pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
     // own velocity, p/rho^2 and rho
     const T4 fvi = FV[ii];
     const R vix = fvi.x, viy = fvi.y, viz = D == 3 ? fvi.z : (R)0;
@@ -219,13 +219,13 @@ __device__ __forceinline__ void force_one(const View &v, int stage, int mode, in
     auto body = [&](int j, const T4 &pj, const R *d, R rsq, auto near) {
         constexpr bool NEAR = decltype(near)::value;
         const Dist<R> dd = make_dist<R>(rsq);
-        R gl = kernel_g<K, R, true>(kl, dd);
+        const R gl = kernel_g<K, R, true>(kl, dd);   // -2a grad W_l / r
         const T4 fvj = FV[j];
         R dvdx = (fvj.x - vix) * d[0] + (fvj.y - viy) * d[1];
         if (D == 3) dvdx += (fvj.z - viz) * d[2];
         // beyond the short support gs = 0: the pressure and viscosity terms
-        // vanish and gsum = pl2 gl bit for bit
-        R gsum = pl2 * gl, gs = (R)0;
+        // vanish and gsum = gl bit for bit
+        R gsum = gl, gs = (R)0;
         if constexpr (NEAR) {
             gs = kernel_g<K, R, true>(ks, dd);
             R ps = fsi + (D == 2 ? fvj.z : fvj.w);
@@ -237,17 +237,19 @@ __device__ __forceinline__ void force_one(const View &v, int stage, int mode, in
                 R mu = fdiv<R>(hs * dvdx, rsq + eps_h2);
                 ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), rhoi + rhoj);
             }
-            gsum = ps * gs + pl2 * gl;
+            gsum = ps * gs + gl;
         }
         ax[0].add(gsum * d[0]);
         ax[1].add(gsum * d[1]);
         if (D == 3) ax[2].add(gsum * d[2]);
-        R du = (R)0.5 * gsum * dvdx * pj.w;
+        // twice the energy-rate term; the sum is halved once at the end
+        // (scaling by 2 is exact, so the bits are those of the halved terms)
+        R du = gsum * dvdx * pj.w;
         if (heat && NEAR) {
             T4 qj = Q[j];
             R dq = (qi.x + qj.x) * d[0] + (qi.y + qj.y) * d[1];
             if (D == 3) dq += (qi.z + qj.z) * d[2];
-            du -= dq * gs * pj.w;
+            du -= (R)2 * dq * gs * pj.w;
         }
         ud.add(du);
     };
@@ -264,7 +266,7 @@ __device__ __forceinline__ void force_one(const View &v, int stage, int mode, in
         for_pairs<R, D, D == 3, false>(v, S, fr, P, i, P[i], body, cell_done);
     }
     R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
-    R udr = ud.get();
+    R udr = (R)0.5 * ud.get();
     for (int a = 0; a < D; ++a) ((R *)v.vdot[a])[i] = vdr[a];
     ((R *)v.udot)[i] = udr;
     if (!isfinite(vdr[0]) || !isfinite(udr)) set_err(v.err, v.err_any, s, SPH_ENAN);

@@ -33,7 +33,9 @@ template <typename R> struct SimConst {
     R ext[3];                    // half cell extent + allowed drift (culling)
     R h[2], h_lo[2], inv_h[2], inv_h_lo[2], sig[2], g0[2], g0_h2[2];
     R inv_h2[2], inv_h2_lo[2];
-    R hs, eps_h2, alpha_c, beta, pl2, kappa;
+    R g0_pl, g0_h2_pl;           // the long kernel's g0 and g0/h^2 times the cohesive
+                                 // factor pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
+    R hs, eps_h2, alpha_c, beta, kappa;
 };
 
 // Normalisation sigma of a smoothing kernel (W = sigma w(q)) in dim 2 or 3:
@@ -45,6 +47,18 @@ double kernel_sigma(int kernel, int dim, double h);
 // and the gradient factor g0 (Lucy -12 sigma/h^2, Gaussian -2/h^2 with sigma
 // applied in the kernel, cubic sigma/h^2, Debrun -3 sigma).  The pair passes'
 // tables and sph_kernel_eval take them from here alike.
+// Gradient factor g0 of a kernel at smoothing length h (sigma applied where
+// the kernel's gradient carries it): Lucy -12 sigma/h^2, Gaussian -2/h^2
+// (sigma applied in the kernel), cubic sigma/h^2, Debrun -3 sigma.
+inline double kernel_g0(int kernel, double h, double sig) {
+    switch (kernel) {
+        case SPH_KERNEL_LUCY: return -12.0 * sig / (h * h);
+        case SPH_KERNEL_GAUSSIAN: return -2.0 / (h * h);
+        case SPH_KERNEL_CUBIC: return sig / (h * h);
+        default: return -3.0 * sig;
+    }
+}
+
 template <typename R>
 inline void kernel_consts(int kernel, double h, double sig, R &h_r, R &h_lo, R &inv_h,
                           R &inv_h_lo, R &sig_r, R &g0, R &g0_h2, R &inv_h2,
@@ -54,12 +68,7 @@ inline void kernel_consts(int kernel, double h, double sig, R &h_r, R &h_lo, R &
     inv_h = (R)(1.0 / h);
     inv_h_lo = (R)(1.0 / h - (double)inv_h);
     sig_r = (R)sig;
-    switch (kernel) {
-        case SPH_KERNEL_LUCY: g0 = (R)(-12.0 * sig / (h * h)); break;
-        case SPH_KERNEL_GAUSSIAN: g0 = (R)(-2.0 / (h * h)); break;
-        case SPH_KERNEL_CUBIC: g0 = (R)(sig / (h * h)); break;
-        default: g0 = (R)(-3.0 * sig); break;
-    }
+    g0 = (R)kernel_g0(kernel, h, sig);
     g0_h2 = (R)((double)g0 / (h * h));
     inv_h2 = (R)(1.0 / (h * h));
     inv_h2_lo = (R)(1.0 / (h * h) - (double)inv_h2);
