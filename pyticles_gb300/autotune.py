@@ -2,8 +2,10 @@
 
 Knobs (struct sph_tuning): threads per block of the pair passes, the
 cell-edge / cutoff ratio (1 -> cells of the cutoff and a 3^d window, 1/2 ->
-5^d, 1/3 -> 7^d, cells beyond the cutoff culled per particle) and, for 3D
-simulations in mixed precision, the pair scheme (cell windows or cluster
+5^d, 1/3 -> 7^d, cells beyond the cutoff culled per particle), for batches
+in mixed precision the launch form of the cell-window passes (one thread
+per particle, or persistent grids that walk the flattened table) and, for
+3D simulations in mixed precision, the pair scheme (cell windows or cluster
 pairs; the cluster scheme has its own fixed launch shape).  A candidate is
 timed with CUDA events over a few graph-captured steps on a clone of the
 simulations (same parameters, same current states), so tuning neither
@@ -35,7 +37,8 @@ def cluster_candidate(group, precision, sims):
     return group.dim == 3 and precision == "mixed" and group.collision == 0
 
 
-def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream, scheme=0):
+def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream, scheme=0,
+                   persistent=0):
     import torch
     total = sum(len(s[1]) for s in sims)
     with Engine(group, precision, max_particles=total, max_sims=len(sims),
@@ -43,7 +46,7 @@ def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream, 
         for prm, r, v, m, u in sims:
             e.add(prm, r, v, m, u)
         e.set_tuning(block_size=block, cell_ratio=ratio, steps_per_graph=steps, use_graph=1,
-                     pair_scheme=scheme)
+                     pair_scheme=scheme, persistent=persistent)
         e.advance(warmup)
         e.prepare()
         e.sync()
@@ -72,13 +75,20 @@ def tune(group, precision, sims, steps=4, warmup=2, blocks=BLOCKS, ratios=RATIOS
         for block in blocks:
             ms = time_candidate(group, precision, sims, block, ratio, steps, warmup, stream)
             table.append({"block_size": block, "cell_ratio": ratio, "pair_scheme": 0,
-                          "ms_per_step": ms})
+                          "persistent": 0, "ms_per_step": ms})
+    if precision == "mixed" and len(sims) > 1:
+        # the persistent launch form, at the best cell-window shape
+        cell = min(table, key=lambda row: row["ms_per_step"])
+        ms = time_candidate(group, precision, sims, cell["block_size"], cell["cell_ratio"], steps,
+                            warmup, stream, persistent=1)
+        table.append(dict(cell, persistent=1, ms_per_step=ms))
     if cluster_candidate(group, precision, sims):
         ms = time_candidate(group, precision, sims, 128, 0.5, steps, warmup, stream, scheme=1)
-        table.append({"block_size": 128, "cell_ratio": 0.5, "pair_scheme": 1, "ms_per_step": ms})
+        table.append({"block_size": 128, "cell_ratio": 0.5, "pair_scheme": 1, "persistent": 0,
+                      "ms_per_step": ms})
     best = min(table, key=lambda row: row["ms_per_step"])
     knobs = {"block_size": best["block_size"], "cell_ratio": best["cell_ratio"],
-             "pair_scheme": best["pair_scheme"]}
+             "pair_scheme": best["pair_scheme"], "persistent": best["persistent"]}
     _cache[key] = (knobs, table)
     return knobs, table
 
