@@ -244,7 +244,7 @@ def test_autotuner_times_the_persistent_launch_for_batches():
     persistent launch form at the best of them; a single simulation and an
     FP64 batch get no persistent candidate."""
     from pyticles_gb300 import autotune
-    sims = [(p, r, v, m, workloads.vdw_energy(np.full(len(r), 1.0), T))
+    sims = [(p, r, v, m, oracle.initial_energy(p, r, v, m, T))
             for p, r, v, m, T in workloads.batched_2d(3, seed_base=4600, n_lo=256, n_hi=1024,
                                                       ramp_steps=10)]
     knobs, table = autotune.tune(sims[0][0], "mixed", sims, steps=2, warmup=1,
