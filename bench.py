@@ -486,7 +486,7 @@ def main():
                     help="profiling driver: --steps eager steps of one workload "
                          "(--side, --precision, --pair-scheme), no timing")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--pair-scheme", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--pair-scheme", type=int, default=0, choices=[0, 1, 2])
     args = ap.parse_args()
     if args.profile_case:
         return profile_case(args)

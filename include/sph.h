@@ -48,9 +48,12 @@ enum sph_status {
     SPH_ENAN = 5,            /* a non-finite density, pressure or rate appeared  */
     SPH_ECUDA = 6,           /* a CUDA runtime call failed                       */
     SPH_ESKIN = 7,           /* a particle moved further within one step than the
-                                cell slack allows (cell list would miss pairs)   */
+                                cell slack allows (cell list would miss pairs),
+                                or with pair lists further from its position
+                                at the lists' build than half the skin       */
     SPH_ECAPACITY = 8,       /* engine particle / simulation capacity exceeded,
-                                or a cluster pair list outgrew its region       */
+                                or a cluster or particle pair list outgrew its
+                                region                                          */
     SPH_ENOTFOUND = 9,       /* unknown simulation id                           */
     SPH_EBOUNDS = 10         /* an index check failed and the access was
                                 skipped: the checking build's checks, and in
@@ -160,7 +163,8 @@ int sph_sim_set_steps(sph_engine *e, int32_t sim_id, int64_t steps);
 
 /* Advances every simulation by nsteps steps of its integrator, applying
  * the periodic box after each step and the thermostat when enabled.
- * Asynchronous except with cluster pairs on (sph_tuning.pair_scheme), where
+ * Asynchronous except with cluster pairs or pair lists on
+ * (sph_tuning.pair_scheme 1 or 2), where
  * steps run in graph chunks of steps_per_graph steps (at most 32; a longer
  * setting is split into even chunks of about 20) and the call returns once
  * all but its last chunk finished: each chunk's longest pair list is
@@ -232,6 +236,22 @@ typedef struct sph_tuning {
                                  (built every step) are per simulation, so a
                                  simulation gives the same bits alone or in a
                                  batch; same pair set, rounding differs from
+                                 scheme 0.
+                                 2: pair lists -- per particle the neighbours
+                                 within the cutoff plus list_skin, built when
+                                 the engine bins and kept while every particle
+                                 stays within a quarter of the skin of where
+                                 it was at the build (VerletList.build with
+                                 its skin and ponder_rebuild,
+                                 neighbour_list.py:160-234); the passes walk
+                                 the lists and still apply the exact pair test
+                                 at every evaluation.  2D mixed-precision
+                                 engines without collisions whose boxes span
+                                 at least 2W+1 cells per axis; otherwise cell
+                                 windows.  Bins on demand like rebin = 1 for
+                                 improved Euler and RK4, so the summation
+                                 order depends on when the engine last built;
+                                 same pair set, rounding differs from
                                  scheme 0                                     */
     int32_t persistent;       /* 0: the cell-window density, heat-flux and
                                  force passes launch one thread per particle.
@@ -241,6 +261,9 @@ typedef struct sph_tuning {
                                  stride: one persistent launch per pass over
                                  all simulations.  Each particle's sums are
                                  the same either way (same bits)           */
+    double list_skin;         /* pair_scheme 2: the lists' skin as a fraction of
+                                 the cutoff (0.01 .. 0.5; default 0.025); at
+                                 least 32 dt vmax is used                     */
 } sph_tuning;
 int sph_get_tuning(sph_engine *e, sph_tuning *t);
 int sph_set_tuning(sph_engine *e, const sph_tuning *t);

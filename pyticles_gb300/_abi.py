@@ -91,6 +91,7 @@ class SphTuning(ctypes.Structure):
         ("cell_ratio", ctypes.c_double),
         ("pair_scheme", ctypes.c_int32),
         ("persistent", ctypes.c_int32),
+        ("list_skin", ctypes.c_double),
     ]
 
 

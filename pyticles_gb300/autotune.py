@@ -4,9 +4,9 @@ Knobs (struct sph_tuning): threads per block of the pair passes, the
 cell-edge / cutoff ratio (1 -> cells of the cutoff and a 3^d window, 1/2 ->
 5^d, 1/3 -> 7^d, cells beyond the cutoff culled per particle), for batches
 in mixed precision the launch form of the cell-window passes (one thread
-per particle, or persistent grids that walk the flattened table) and, for
-3D simulations in mixed precision, the pair scheme (cell windows or cluster
-pairs; the cluster scheme has its own fixed launch shape).  A candidate is
+per particle, or persistent grids that walk the flattened table) and the
+pair scheme in mixed precision: cell windows, per-particle pair lists (2D)
+or cluster pairs (3D; the cluster scheme has its own fixed launch shape).  A candidate is
 timed with CUDA events over a few graph-captured steps on a clone of the
 simulations (same parameters, same current states), so tuning neither
 advances the live simulations nor shifts their thermostat schedules.  Results
@@ -35,6 +35,12 @@ def cluster_candidate(group, precision, sims):
     """Whether the cluster-pair scheme can apply: 3D simulations in mixed
     precision without collisions (the engine itself checks the boxes)."""
     return group.dim == 3 and precision == "mixed" and group.collision == 0
+
+
+def list_candidate(group, precision, sims):
+    """Whether per-particle pair lists can apply: 2D simulations in mixed
+    precision without collisions (the engine itself checks the grids)."""
+    return group.dim == 2 and precision == "mixed" and group.collision == 0
 
 
 def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream, scheme=0,
@@ -82,6 +88,12 @@ def tune(group, precision, sims, steps=4, warmup=2, blocks=BLOCKS, ratios=RATIOS
         ms = time_candidate(group, precision, sims, cell["block_size"], cell["cell_ratio"], steps,
                             warmup, stream, persistent=1)
         table.append(dict(cell, persistent=1, ms_per_step=ms))
+    if list_candidate(group, precision, sims):
+        for block in (128, 256):
+            ms = time_candidate(group, precision, sims, block, 0.5, steps, warmup, stream,
+                                scheme=2)
+            table.append({"block_size": block, "cell_ratio": 0.5, "pair_scheme": 2,
+                          "persistent": 0, "ms_per_step": ms})
     if cluster_candidate(group, precision, sims):
         ms = time_candidate(group, precision, sims, 128, 0.5, steps, warmup, stream, scheme=1)
         table.append({"block_size": 128, "cell_ratio": 0.5, "pair_scheme": 1, "persistent": 0,

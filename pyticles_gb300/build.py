@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libsph.so")
 SOURCES = ["sph_engine.cu", "sph_sort.cu", "sph_pairs.cu", "sph_force_f32.cu",
            "sph_force_f64.cu", "sph_noalloc.cu", "sph_splat.cu", "sph_collide.cu",
-           "sph_cluster.cu", "sph_kfunc.cu"]
+           "sph_cluster.cu", "sph_kfunc.cu", "sph_vlist.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]

@@ -53,6 +53,7 @@ struct Sim {
     int chunk_first = 0, nchunk = 0;
     int64_t steps = 0;
     double vmax = 0.0;
+    double vl_skin = 0.0;      // pair lists: skin (absolute) the grid leaves room for
 };
 
 template <typename T>
@@ -134,6 +135,9 @@ struct sph_engine {
     int *cl_fill_host = nullptr;   // pinned: longest list of the last advance
     cudaEvent_t cl_fill_ev = nullptr;
     bool cl_fill_pending = false;
+    VList vl = {};                 // tuning.pair_scheme = 2 (sph_vlist.cu)
+    bool vl_disabled = false;      // the pair lists did not fit: cell windows
+    long long vl_alloc = 0;        // entries allocated in vl.ent
 
     // profiling: event pairs recorded around each pass
     bool prof_on = false;
@@ -204,14 +208,17 @@ int validate_params(const sph_engine *e, const sph_params *p) {
 
 // Cell grid of one simulation.  reach = cutoff + 8 dt vmax: the cutoff plus
 // room for the largest displacement between binning and an evaluation of
-// the step (checked on the device, SPH_ESKIN).  Cells are r * reach wide
+// the step (checked on the device, SPH_ESKIN); with pair lists (list_skin =
+// the tuning's skin as a fraction of the cutoff, 0 otherwise) cutoff + skin,
+// the skin at least 32 dt vmax.  Cells are r * reach wide
 // (r = tuning.cell_ratio) and the pair passes scan +-W cells per axis with
 // W = ceil(1/r) for r < 1 (1 otherwise), culling cells beyond the cutoff.
 // An axis with fewer than 2W+1 cells becomes a single cell (the passes then
 // apply the minimum image on it).
-void make_grid(Sim &S, int dim, double ratio) {
+void make_grid(Sim &S, int dim, double ratio, double list_skin = 0.0) {
     double rc = std::sqrt(S.prm.cutoff * S.prm.cutoff + S.prm.tolerance * S.prm.tolerance);
-    double reach = rc + 8.0 * S.prm.dt * S.vmax;
+    S.vl_skin = list_skin > 0.0 ? std::max(list_skin * rc, 32.0 * S.prm.dt * S.vmax) : 0.0;
+    double reach = rc + std::max(8.0 * S.prm.dt * S.vmax, S.vl_skin);
     // cells of ratio x reach; the window spans the W = ceil(1/ratio) cells
     // per side that cover the reach (1/2 -> 2, 1/3 -> 3, 0.6 -> 2 with room
     // to spare)
@@ -295,6 +302,21 @@ void fill_const(SimConst<R> &c, const sph_engine *e, const Sim &S, const SimDev 
         c.ext[a] = (a < e->dim && S.win[a] > 0) ? (R)((0.5 * S.edge[a] + d.slack_half[a]) * 1.0001)
                                                : (R)1e30;
     }
+    if (S.vl_skin > 0.0) {
+        // pair lists: the build's FP32 squared distances carry ~1e-6; the
+        // 2^-10 margin files every pair that can enter the cutoff (or the
+        // short support) while the lists hold
+        const double rc = std::sqrt(d.thr), sk = S.vl_skin;
+        c.vl_thr = (R)((rc + sk) * (rc + sk) * (1.0 + 1.0 / 1024.0));
+        double near = (rc + sk) * (rc + sk);
+        if (p.kernel != SPH_KERNEL_GAUSSIAN && supp * supp * (1.0 + 1.0 / 1024.0) < d.thr) {
+            const double sq = supp * std::sqrt(1.0 + 1.0 / 1024.0);
+            near = std::min(near, (sq + sk) * (sq + sk));
+        }
+        c.vl_near = (R)(near * (1.0 + 1.0 / 1024.0));
+    } else {
+        c.vl_thr = c.vl_near = (R)0;
+    }
     const double hh[2] = {p.h_short, p.h_long}, sg[2] = {d.sig_s, d.sig_l};
     for (int k = 0; k < 2; ++k)
         kernel_consts<R>(p.kernel, hh[k], sg[k], c.h[k], c.h_lo[k], c.inv_h[k], c.inv_h_lo[k],
@@ -330,6 +352,8 @@ SimDev make_simdev(const sph_engine *e, const Sim &S) {
             (a < e->dim && S.win[a] > 0) ? 0.5 * S.edge[a] + 0.5 * d.slack_half[a] : 1e300;
         if (a < e->dim && S.nc[a] == 1) d.small_mask |= (1 << a);
     }
+    d.vl_gate2 = S.vl_skin > 0.0 ? 0.0625 * S.vl_skin * S.vl_skin : 1e300;
+    d.vl_eskin2 = S.vl_skin > 0.0 ? 0.25 * S.vl_skin * S.vl_skin : 1e300;
     d.active = S.active ? 1 : 0;
     d.cell_off = S.cell_off;
     d.ncells = S.ncells;
@@ -631,12 +655,72 @@ View make_view(const sph_engine *e) {
     v.bin_count = e->bin_count;
     v.one_sim = e->one_sim ? 1 : 0;
     if (e->one_sim) v.one = e->one_dev;
+    // pair lists once their rows exist (measured)
+    if (e->vl.on && e->vl.ent && e->vl.cap > 0) {
+        v.vl_on = 1;
+        v.vl_cap = e->vl.cap;
+        v.vl_stride = e->vl.stride;
+        v.vl_ent = e->vl.ent;
+        v.vl_cnt = e->vl.cnt;
+        v.vl_x0 = e->vl.x0;
+    }
     return v;
 }
 
 // Binning on demand applies to multi-stage integrators: their last stage
-// writes packed buffer 0, which no evaluation of that stage reads.
-bool rebin_on_demand(const sph_engine *e) { return e->tune.rebin != 0 && e->nstage > 1; }
+// writes packed buffer 0, which no evaluation of that stage reads.  Pair
+// lists always bin (and build) on demand.
+bool rebin_on_demand(const sph_engine *e) {
+    return (e->tune.rebin != 0 || e->vl.on) && e->nstage > 1;
+}
+
+// The pair lists' skin as a fraction of the cutoff, 0 without them.
+double list_skin_of(const sph_engine *e) {
+    return e->tune.pair_scheme == 2 ? e->tune.list_skin : 0.0;
+}
+
+// Pair lists (cluster or particle) whose fill the host tracks.
+bool lists_on(const sph_engine *e) { return e->cl.on || e->vl.on; }
+int *list_maxfill(const sph_engine *e) { return e->cl.on ? e->cl.maxfill : e->vl.maxfill; }
+int list_room(const sph_engine *e) { return e->cl.on ? e->cl.lstride : e->vl.cap; }
+
+// Pair lists of a 2D mixed-precision engine (tuning.pair_scheme = 2): on
+// when every live simulation's grid has a window of 1 to 3 cells per axis
+// and room for it, without collisions, and the slots fit the entries'
+// index field.  The rows are sized by vl_measure before the next use.
+int vl_setup(sph_engine *e) {
+    VList &l = e->vl;
+    l.on = 0;
+    if (e->tune.pair_scheme != 2 || e->vl_disabled || e->dim != 2 ||
+        e->precision != SPH_MIXED || e->group.collision != SPH_COLLIDE_OFF || e->np_b <= 0 ||
+        e->np_b > kVlIndexMask)
+        return SPH_OK;
+    for (const auto &S : e->sims) {
+        if (!S.active) continue;
+        if (!(S.vl_skin > 0.0)) return SPH_OK;
+        for (int a = 0; a < 2; ++a)
+            if (S.win[a] < 1 || S.win[a] > kVlMaxWindow || S.nc[a] < 2 * S.win[a] + 1)
+                return SPH_OK;
+    }
+    if (!l.cnt) {
+        TRY(dalloc(&l.cnt, e->cap_p));
+        TRY(dalloc(&l.x0, e->cap_p));
+        TRY(dalloc(&l.maxfill, 1));
+        CK(cudaMemset(l.maxfill, 0, sizeof(int)));
+    }
+    const long long stride = ((long long)e->np_b + 31) & ~31LL;
+    if (stride != l.stride) {
+        // rows of the old layout: measured again before the next use
+        cudaFree(l.ent);
+        l.ent = nullptr;
+        l.cap = 0;
+        e->vl_alloc = 0;
+        l.stride = stride;
+    }
+    l.on = 1;
+    e->cl_stale = true;
+    return SPH_OK;
+}
 
 // Evaluation buffers of stage s: stage 0 reads the permuted x0 (B) and
 // packed buffer 0; stage s >= 1 reads what stage s-1's force pass wrote.
@@ -728,6 +812,7 @@ int relayout(sph_engine *e) {
     e->one_sim = live == 1;
     // marks the simulations that run on cluster pairs (SimDev.cl_on)
     TRY(cluster_setup(e, sd));
+    TRY(vl_setup(e));
     e->n_cell_sims = 0;
     for (int s = 0; s < (int)e->sims.size(); ++s)
         if (e->sims[s].active && !sd[s].cl_on) ++e->n_cell_sims;
@@ -763,7 +848,7 @@ constexpr int kSortKernels = 7;  // bin, 3 scan, scatter, in-cell order, permute
 // Counting sort of A into B plus the packed first-evaluation copies.  Gated:
 // the kernels run only if the device gate is raised (binning on demand); the
 // close kernel then lowers it and counts the binning.
-void enqueue_prepare(sph_engine *e, cudaStream_t st, bool gated = false) {
+void enqueue_prepare(sph_engine *e, cudaStream_t st, bool gated = false, bool lists = true) {
     ProfScope ps(e, SPH_PASS_SORT, st);
     View v = make_view(e);
     stage_view(e, v, 0);
@@ -781,6 +866,8 @@ void enqueue_prepare(sph_engine *e, cudaStream_t st, bool gated = false) {
     launch_scatter(v, e->a_extent, st);
     launch_cellsort(v, e->ncells_total, st);
     launch_permute(v, e->precision, st);
+    // a binning renumbers the slots: the pair lists are built again
+    if (lists && e->vl.on && e->vl.ent && e->vl.cap > 0) launch_vlist_build(v, e->vl, gate, true, st);
     if (gated) launch_rebin_close(e->rebin_gate, e->bin_count, st);
 }
 
@@ -937,32 +1024,78 @@ int cluster_measure(sph_engine *e) {
     return SPH_OK;
 }
 
-// Before an advance or an evaluation with cluster pairs: re-measure if the
-// state changed or the last advance filled a list region past 80%.
+// Measures the longest pair list of the current state (a binning and a
+// build that only counts) and sizes the rows to 1.25 times it (+8, rounded
+// up to whole groups of four).  Lists
+// longer than the count field or rows that do not fit in device memory
+// leave the layout on cell windows.
+int vl_measure(sph_engine *e) {
+    VList &l = e->vl;
+    if (!l.on) return SPH_OK;
+    cudaStream_t st = e->stream;
+    const bool prof = e->prof_on;
+    e->prof_on = false;
+    CK(cudaMemsetAsync(l.maxfill, 0, sizeof(int), st));
+    enqueue_prepare(e, st, false, false);
+    View v = make_view(e);
+    stage_view(e, v, 0);
+    VList m = l;
+    m.cap = 0;   // counts only
+    launch_vlist_build(v, m, nullptr, false, st);
+    e->prof_on = prof;
+    int fill = 0;
+    CK(cudaMemcpyAsync(&fill, l.maxfill, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemsetAsync(l.maxfill, 0, sizeof(int), st));
+    CK(cudaStreamSynchronize(st));
+    e->cl_stale = false;
+    e->cl_fill_pending = false;
+    e->bins_valid = false;   // the next step bins and builds with the new rows
+    // rows of four-entry groups
+    const int need = (std::max(32, (int)std::ceil(1.25 * fill) + 8) + 3) & ~3;
+    if (need == l.cap && l.ent) return SPH_OK;
+    free_graph(e);
+    cudaFree(l.ent);
+    l.ent = nullptr;
+    l.cap = 0;
+    e->vl_alloc = 0;
+    if (need > 0xffff || dalloc(&l.ent, (size_t)need * (size_t)l.stride) != SPH_OK) {
+        l.on = 0;
+        e->vl_disabled = true;
+        e->layout_dirty = true;
+        return SPH_OK;
+    }
+    l.cap = need;
+    e->vl_alloc = (long long)need * l.stride;
+    return SPH_OK;
+}
+
+// Before an advance or an evaluation with cluster pairs or pair lists:
+// re-measure if the state changed or the last advance filled a list past
+// 80% of its room.
 int cluster_check(sph_engine *e) {
-    ClusterSet &c = e->cl;
-    if (!c.on) return SPH_OK;
+    if (!lists_on(e)) return SPH_OK;
     if (e->cl_fill_pending && cudaEventQuery(e->cl_fill_ev) == cudaSuccess) {
         e->cl_fill_pending = false;
-        if (*e->cl_fill_host > 0.8 * c.lstride) e->cl_stale = true;
+        if (*e->cl_fill_host > 0.8 * list_room(e)) e->cl_stale = true;
     }
-    if (e->cl_stale) TRY(cluster_measure(e));
+    if (e->cl_stale) TRY(e->cl.on ? cluster_measure(e) : vl_measure(e));
     if (e->layout_dirty) TRY(relayout(e));   // the lists did not fit
+    if (e->vl.on && e->cl_stale) TRY(vl_measure(e));   // set up again by the relayout
     return SPH_OK;
 }
 
 // After an advance: the longest list of its steps, read back without a
 // wait (checked by the next cluster_check).
 int cluster_note_fill(sph_engine *e) {
-    ClusterSet &c = e->cl;
-    if (!c.on) return SPH_OK;
+    if (!lists_on(e)) return SPH_OK;
     if (!e->cl_fill_host) {
         CK(cudaMallocHost((void **)&e->cl_fill_host, sizeof(int)));
         CK(cudaEventCreateWithFlags(&e->cl_fill_ev, cudaEventDisableTiming));
     }
     if (e->cl_fill_pending) return SPH_OK;   // the previous read is still in flight
-    CK(cudaMemcpyAsync(e->cl_fill_host, c.maxfill, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaMemsetAsync(c.maxfill, 0, sizeof(int), e->stream));
+    int *fill = list_maxfill(e);
+    CK(cudaMemcpyAsync(e->cl_fill_host, fill, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemsetAsync(fill, 0, sizeof(int), e->stream));
     CK(cudaEventRecord(e->cl_fill_ev, e->stream));
     e->cl_fill_pending = true;
     return SPH_OK;
@@ -980,7 +1113,7 @@ int64_t kernels_per_step(const sph_engine *e) {
         if (rebin_on_demand(e)) k += 2;
         return k;
     }
-    int64_t k = kSortKernels;
+    int64_t k = kSortKernels + (e->vl.on ? 1 : 0);   // + the pair lists' build
     k += (int64_t)e->nstage * (2 + (e->group.heat_flux ? 1 : 0));
     if (e->any_thermostat) k += 2;
     // collisions: per find 5 kernels + 7 for the levels, one apply per
@@ -1218,6 +1351,11 @@ void free_all(sph_engine *e) {
     for (void *p : cp)
         if (p) cudaFree(p);
     cluster_free(e);
+    void *vp[] = {e->vl.ent, e->vl.cnt, e->vl.x0, e->vl.maxfill};
+    for (void *p : vp)
+        if (p) cudaFree(p);
+    e->vl = VList{};
+    e->vl_alloc = 0;
     if (e->cl_geom_d) cudaFree(e->cl_geom_d);
     e->cl_geom_d = nullptr;
     if (e->cl_fill_host) cudaFreeHost(e->cl_fill_host);
@@ -1308,6 +1446,9 @@ int sph_engine_create(sph_engine **out, const sph_params *group, int32_t precisi
     e->tune.steps_per_graph = 1;
     e->tune.pair_scheme = 0;
     e->tune.persistent = 0;
+    // measured on GB300 (2D 1M fluid): 0.02-0.03 of the cutoff balance the
+    // lists' length against how often they are built
+    e->tune.list_skin = 0.025;
     if (stream) {
         e->stream = (cudaStream_t)stream;
     } else {
@@ -1380,7 +1521,7 @@ int sph_sim_add(sph_engine *e, const sph_params *p, int64_t n, const double *r, 
     S.prm = *p;
     S.n = n;
     S.vmax = vmax;
-    make_grid(S, e->dim, e->tune.cell_ratio);
+    make_grid(S, e->dim, e->tune.cell_ratio, list_skin_of(e));
     int off = e->a_extent;
     TRY(write_state_range(e, off, n, r, v, m, u, mem));
     launch_iota_sim(e->a_id + off, e->a_sim + off, id, (int)n, e->stream);
@@ -1494,7 +1635,7 @@ int cluster_between(sph_engine *e, bool *over) {
     if (e->cl_fill_pending) {
         CK(cudaEventSynchronize(e->cl_fill_ev));
         e->cl_fill_pending = false;
-        if (*e->cl_fill_host > 0.8 * e->cl.lstride) e->cl_stale = true;
+        if (*e->cl_fill_host > 0.8 * list_room(e)) e->cl_stale = true;
     }
     TRY(cluster_note_fill(e));
     *over = e->cl_stale;
@@ -1504,7 +1645,7 @@ int cluster_between(sph_engine *e, bool *over) {
 // Steps per graph launch of an advance.
 int graph_chunk(const sph_engine *e) {
     const int per = std::max(1, e->tune.steps_per_graph);
-    if (!e->cl.on || per <= kClMaxChunk) return per;
+    if (!lists_on(e) || per <= kClMaxChunk) return per;
     const int n = (per + kClChunk - 1) / kClChunk;
     return (per + n - 1) / n;
 }
@@ -1513,7 +1654,7 @@ int graph_chunk(const sph_engine *e) {
 // cluster list region needs re-measuring before further steps.
 int advance_span(sph_engine *e, int n, int *ran) {
     cudaStream_t st = e->stream;
-    const bool cl = e->cl.on;
+    const bool cl = lists_on(e);
     const int per = graph_chunk(e);
     int done = 0;
     *ran = 0;
@@ -1623,10 +1764,10 @@ int sph_sim_pair_count(sph_engine *e, int32_t id, int64_t *nip) {
     TRY(check_sim(e, id));
     if (!nip) return SPH_EINVAL;
     TRY(ensure_layout(e));
+    TRY(cluster_check(e));
     cudaStream_t st = e->stream;
     if (e->cl.on) {
         // simulations on cluster pairs count in the cluster density pass
-        TRY(cluster_check(e));
         enqueue_prepare(e, st);
         enqueue_stage(e, 0, 0, st);
     } else {
@@ -1779,19 +1920,24 @@ int sph_set_tuning(sph_engine *e, const sph_tuning *t) {
     if (!e || !t) return SPH_EINVAL;
     if (t->block_size < 32 || t->block_size > 256 || (t->block_size & 31) ||
         !(t->cell_ratio >= 0.2 && t->cell_ratio <= 4.0) || (t->rebin != 0 && t->rebin != 1) ||
-        t->steps_per_graph < 1 || (t->pair_scheme != 0 && t->pair_scheme != 1) ||
-        (t->persistent != 0 && t->persistent != 1))
+        t->steps_per_graph < 1 || t->pair_scheme < 0 || t->pair_scheme > 2 ||
+        (t->persistent != 0 && t->persistent != 1) ||
+        !(t->list_skin >= 0.01 && t->list_skin <= 0.5))
         return SPH_EINVAL;
+    // the grid's reach holds the pair lists' skin
+    const double skin_old = list_skin_of(e);
     bool regrid = t->cell_ratio != e->tune.cell_ratio;
     if (t->pair_scheme != e->tune.pair_scheme) {
         e->layout_dirty = true;
         e->cl_disabled = false;
+        e->vl_disabled = false;
     }
     e->tune = *t;
+    regrid |= list_skin_of(e) != skin_old;
     free_graph(e);
     if (regrid) {
         for (auto &S : e->sims)
-            if (S.active) make_grid(S, e->dim, e->tune.cell_ratio);
+            if (S.active) make_grid(S, e->dim, e->tune.cell_ratio, list_skin_of(e));
         e->layout_dirty = true;
         e->props_valid = false;
     }

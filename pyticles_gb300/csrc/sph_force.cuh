@@ -22,6 +22,7 @@ __device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S,
     using T4 = typename V4<R>::T;
     R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
     bool skin = false;
+    double moved = 0.0;   // squared displacement from the pair lists' build
 #pragma unroll
     for (int a = 0; a < D; ++a) {
         // relative to the cell the particle was binned in; with binning on
@@ -29,6 +30,10 @@ __device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S,
         double d = x[a] - v.org[a][i];
         if (d > S.half_L[a]) d -= S.L[a];
         if (d < -S.half_L[a]) d += S.L[a];
+        if (D == 2 && v.vl_on) {
+            const double m = d - (double)(a == 0 ? v.vl_x0[i].x : v.vl_x0[i].y);
+            moved += m * m;
+        }
         xl[a] = (R)d;
         vv[a] = (R)vel[a];
         v.xe_out[a][i] = x[a];
@@ -37,6 +42,9 @@ __device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S,
         // cell grown by the slack
         skin |= fabs(d) > S.box_half[a];
     }
+    // with pair lists: a pair can be missing from them once a particle has
+    // moved half the skin
+    skin |= moved > S.vl_eskin2;
     if (skin) set_err(v.err, v.err_any, v.b_sim[i], SPH_ESKIN);
     v.ue_out[i] = u;
     ((T4 *)v.pk_pos_out)[i] = make_v4<R>(xl[0], xl[1], xl[2], (R)m);
@@ -47,13 +55,15 @@ __device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S,
 // In rebin mode it is also the next step's start state in B and its packed
 // stage-0 copies, relative to the unchanged cells (the final stage writes
 // pk_*_out == buffer 0 for improved Euler and RK4); a particle past half of
-// its cell slack asks for a binning before the next step.
+// its cell slack -- with pair lists, one that has moved a quarter of the
+// skin since their build -- asks for a binning before the next step.
 template <typename R, int D>
 __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S, int i,
                                                   double *x, const double *vel, double u) {
     using T4 = typename V4<R>::T;
     R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
     bool far = false;
+    double moved = 0.0;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
         double L = S.L[a];
@@ -65,7 +75,12 @@ __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S
             double d = x[a] - v.org[a][i];
             if (d > S.half_L[a]) d -= L;   // the wrap moved it across the box
             if (d < -S.half_L[a]) d += L;
-            far |= fabs(d) > S.rebin_half[a];
+            if (D == 2 && v.vl_on) {
+                const double m = d - (double)(a == 0 ? v.vl_x0[i].x : v.vl_x0[i].y);
+                moved += m * m;
+            } else {
+                far |= fabs(d) > S.rebin_half[a];
+            }
             xl[a] = (R)d;
             vv[a] = (R)vel[a];
             v.b_pos[a][i] = x[a];
@@ -77,6 +92,7 @@ __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S
     v.a_id[i] = v.b_id[i];
     v.a_sim[i] = v.b_sim[i];
     if (v.reuse) {
+        far |= moved > S.vl_gate2;
         v.b_u[i] = u;
         ((T4 *)v.pk_pos_out)[i] = make_v4<R>(xl[0], xl[1], xl[2], (R)v.b_m[i]);
         ((T4 *)v.pk_vel_out)[i] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
@@ -185,7 +201,8 @@ __device__ __forceinline__ void integrate_stage(const View &v, const SimDev &S, 
 // unconstrained 80-104 despite a few spilled words outside the pair loop; a
 // single 2D simulation, with its constants out of registers, runs best at 51
 // (5 blocks), 3D at 64.
-template <typename R, int D, int K, int VH, bool ONE>
+// LIST: the pair lists (tuning.pair_scheme 2) instead of the cell windows.
+template <typename R, int D, int K, int VH, bool ONE, bool LIST = false>
 __device__ __forceinline__ void force_one(const View &v, int stage, int mode, int integ, int i) {
     constexpr bool visc = (VH & 1) != 0;
     constexpr bool heat = (VH & 2) != 0;
@@ -263,7 +280,8 @@ __device__ __forceinline__ void force_one(const View &v, int stage, int mode, in
     {
         PairFrame<R, D> fr;
         fr.init(S);
-        for_pairs<R, D, D == 3, false>(v, S, fr, P, i, P[i], body, cell_done);
+        if constexpr (LIST) for_list<R, D, true>(v, S, fr, P, i, P[i], body, cell_done);
+        else for_pairs<R, D, D == 3, false>(v, S, fr, P, i, P[i], body, cell_done);
     }
     R vdr[3] = {ax[0].get(), ax[1].get(), ax[2].get()};
     R udr = (R)0.5 * ud.get();
@@ -288,6 +306,18 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
     }
 }
 
+// The force pass over the pair lists (2D, mixed precision); a single
+// simulation at SPH_VL_FORCE_BLOCKS resident blocks of 256 per SM.
+#ifndef SPH_VL_FORCE_BLOCKS
+#define SPH_VL_FORCE_BLOCKS 5
+#endif
+template <int K, int VH, bool ONE>
+__global__ void __launch_bounds__(256, ONE ? SPH_VL_FORCE_BLOCKS : 4) k_force_vl(const __grid_constant__ View v, int stage,
+                                                              int mode, int integ) {
+    force_one<float, 2, K, VH, ONE, true>(v, stage, mode, integ,
+                                          blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // Integrator stage from the stored rates: the epilogue of k_force as a pass
 // of its own, for steps whose velocities change between the force pass and
 // the update (hard collisions).
@@ -306,6 +336,13 @@ __global__ void __launch_bounds__(256) k_integrate(View v, int stage, int integ,
 // the persistent form for the mixed-precision pass only (see density_launch)
 template <typename R, int D, int K, int VH, bool ONE>
 void force_launch(const View &v, int stage, int mode, int integ, int block, cudaStream_t s) {
+    if constexpr (std::is_same<R, float>::value && D == 2) {
+        if (v.vl_on) {
+            k_force_vl<K, VH, ONE>
+                <<<(v.np + block - 1) / block, block, 0, s>>>(v, stage, mode, integ);
+            return;
+        }
+    }
     if (std::is_same<R, float>::value && v.persist) {
         auto *fn = k_force<R, D, K, VH, ONE, std::is_same<R, float>::value>;
         fn<<<pass_grid(v, fn, block), block, 0, s>>>(v, stage, mode, integ);

@@ -36,6 +36,10 @@ template <typename R> struct SimConst {
     R g0_pl, g0_h2_pl;           // the long kernel's g0 and g0/h^2 times the cohesive
                                  // factor pco_i/rho_l,i^2 + pco_j/rho_l,j^2 = -2a
     R hs, eps_h2, alpha_c, beta, kappa;
+    // pair lists (tuning.pair_scheme 2): the build takes pairs with FP32
+    // rsq <= vl_thr ((cutoff + skin)^2 grown by a margin) and files those
+    // with rsq < vl_near ((short support + skin)^2, grown) as near
+    R vl_thr, vl_near;
 };
 
 // Normalisation sigma of a smoothing kernel (W = sigma w(q)) in dim 2 or 3:
@@ -82,6 +86,9 @@ struct SimDev {
     double box_half[3];     // 0.5 edge + slack_half: a particle must stay this close
                             // to its cell centre (SPH_ESKIN beyond)
     double rebin_half[3];   // 0.5 edge + slack_half / 2: past it, bin again (rebin mode)
+    double vl_gate2;        // pair lists: squared displacement from the build position
+                            // past which the engine builds again (skin/4)^2
+    double vl_eskin2;       // ... and past which the lists may miss pairs (skin/2)^2
     int nc[3];
     int win[3];             // neighbour window: +-win cells per axis (0 on single-cell axes)
     int small_mask;         // bit a set: axis a has one cell (minimum image in the pair pass)
@@ -167,6 +174,17 @@ struct View {
     // persist: the pair passes launch pass_grid()'s resident blocks, which
     // walk the particles grid-stride (tuning.persistent)
     int persist;
+    // pair lists (tuning.pair_scheme 2, VList): entries four to a group,
+    // group row g of particle i at int4 slot g * vl_stride + i; near
+    // entries from row 0 up, far ones from row vl_cap/4 - 1 down (see
+    // VList); vl_cnt[i] = near | far << 16; vl_x0[i] the particle's
+    // cell-local position at the build
+    int vl_on;
+    int vl_cap;
+    long long vl_stride;
+    const int *vl_ent;
+    const unsigned *vl_cnt;
+    float2 *vl_x0;
     SimDev one;
 };
 
@@ -257,6 +275,31 @@ void launch_cluster_heat(const View &v, const ClusterSet &c, int kernel, cudaStr
 void launch_cluster_force(const View &v, const ClusterSet &c, int kernel, int viscosity, int heat,
                           cudaStream_t s);
 int cluster_build_kernels();
+
+// Pair lists of the 2D mixed-precision cell-window engine (tuning.pair_scheme
+// 2, sph_vlist.cu).  An entry packs the neighbour's B-order index (bits
+// 0-25) and its cell's window offset from the particle's cell, ox + 3 and
+// oy + 3 in three bits each (bits 26-28, 29-31).
+struct VList {
+    int on;
+    int cap;                      // entries reserved per particle (a multiple of 4)
+    long long stride;             // particle slots per group row
+    int *ent;                     // [cap/4][stride][4]: four entries of one particle
+                                  // per 16-byte group; near entry k at group row k/4,
+                                  // slot k%4; far entry k at group row cap/4 - 1 - k/4,
+                                  // slot 3 - k%4
+    unsigned *cnt;                // [stride] near | far << 16
+    float2 *x0;                   // [stride] cell-local position at the build
+    int *maxfill;                 // longest list since the host last read it
+};
+constexpr int kVlIndexBits = 26;
+constexpr int kVlIndexMask = (1 << kVlIndexBits) - 1;
+constexpr int kVlMaxWindow = 3;   // window offsets -3 .. 3
+
+// Builds every particle's list from the binned stage-0 state (gated like
+// the binning); with store false only measures (maxfill).
+void launch_vlist_build(const View &v, const VList &l, const int *gate, bool store,
+                        cudaStream_t s);
 
 // ---- launch wrappers (sph_collide.cu) ----
 // Engine path: candidates of every simulation with collisions on, found

@@ -18,7 +18,8 @@ namespace sph {
 // simulation (its constants are kernel parameters): 2D mixed precision at
 // 32 registers (7 blocks, 60 B spilled), measured 6.3% faster than 48 and 2%
 // faster than 40; 3D and FP64 at 51.
-template <typename R, int D, int K, bool ONE>
+// LIST: the pair lists (tuning.pair_scheme 2) instead of the cell windows.
+template <typename R, int D, int K, bool ONE, bool LIST = false>
 __device__ __forceinline__ void density_one(const View &v, int stage, int i) {
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
@@ -52,7 +53,8 @@ __device__ __forceinline__ void density_one(const View &v, int stage, int i) {
     {
         PairFrame<R, D> fr;
         fr.init(S);
-        for_pairs<R, D>(v, S, fr, P, i, P[i], body, cell_done);
+        if constexpr (LIST) for_list<R, D, true>(v, S, fr, P, i, P[i], body, cell_done);
+        else for_pairs<R, D>(v, S, fr, P, i, P[i], body, cell_done);
     }
     // EOS in FP64 from the compensated sums plus the FP64 self term
     // (properties.py:77-78): the temperature T = (u + a rho)/k_B cancels
@@ -104,8 +106,18 @@ __global__ void __launch_bounds__(256, ONE ? ((D == 2 && sizeof(R) == 4) ? 7 : 5
     }
 }
 
+// The density pass over the pair lists (2D, mixed precision); a single
+// simulation at SPH_VL_DENSITY_BLOCKS resident blocks of 256 per SM.
+#ifndef SPH_VL_DENSITY_BLOCKS
+#define SPH_VL_DENSITY_BLOCKS 7
+#endif
+template <int K, bool ONE>
+__global__ void __launch_bounds__(256, ONE ? SPH_VL_DENSITY_BLOCKS : 4) k_density_vl(const __grid_constant__ View v, int stage) {
+    density_one<float, 2, K, ONE, true>(v, stage, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // At most 64 registers (4 blocks of 256 per SM): 8% faster in 3D than 80.
-template <typename R, int D, int K, bool ONE>
+template <typename R, int D, int K, bool ONE, bool LIST = false>
 __device__ __forceinline__ void heat_one(const View &v, int i) {
     const bool active = i < v.np;
     const int ii = active ? i : v.np - 1;
@@ -142,7 +154,8 @@ __device__ __forceinline__ void heat_one(const View &v, int i) {
         // only the short kernel enters q: cells and pairs beyond its support
         // contribute exactly zero and are not visited
         fr.thr_hi = fr.thr_s;
-        for_pairs<R, D, D == 3, false>(v, S, fr, P, i, P[i], body, cell_done);
+        if constexpr (LIST) for_list<R, D, false>(v, S, fr, P, i, P[i], body, cell_done);
+        else for_pairs<R, D, D == 3, false>(v, S, fr, P, i, P[i], body, cell_done);
     }
     R kap = sconst<R>(S).kappa;
     R qq[3] = {kap * q[0].get(), kap * q[1].get(), kap * q[2].get()};
@@ -161,10 +174,22 @@ __global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v)
     }
 }
 
+template <int K, bool ONE>
+__global__ void __launch_bounds__(256, 4) k_heat_vl(const __grid_constant__ View v) {
+    heat_one<float, 2, K, ONE, true>(v, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // The persistent form is instantiated for the mixed-precision passes only;
 // FP64 engines launch one thread per particle whatever tuning.persistent says.
+// Pair lists (v.vl_on) exist for 2D mixed-precision engines only.
 template <typename R, int D, int K, bool ONE>
 void density_launch(const View &v, int stage, int block, cudaStream_t s) {
+    if constexpr (std::is_same<R, float>::value && D == 2) {
+        if (v.vl_on) {
+            k_density_vl<K, ONE><<<(v.np + block - 1) / block, block, 0, s>>>(v, stage);
+            return;
+        }
+    }
     if (std::is_same<R, float>::value && v.persist) {
         auto *fn = k_density<R, D, K, ONE, std::is_same<R, float>::value>;
         fn<<<pass_grid(v, fn, block), block, 0, s>>>(v, stage);
@@ -175,6 +200,12 @@ void density_launch(const View &v, int stage, int block, cudaStream_t s) {
 
 template <typename R, int D, int K, bool ONE>
 void heat_launch(const View &v, int block, cudaStream_t s) {
+    if constexpr (std::is_same<R, float>::value && D == 2) {
+        if (v.vl_on) {
+            k_heat_vl<K, ONE><<<(v.np + block - 1) / block, block, 0, s>>>(v);
+            return;
+        }
+    }
     if (std::is_same<R, float>::value && v.persist) {
         auto *fn = k_heat<R, D, K, ONE, std::is_same<R, float>::value>;
         fn<<<pass_grid(v, fn, block), block, 0, s>>>(v);

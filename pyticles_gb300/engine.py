@@ -209,22 +209,26 @@ class Engine:
         return {"block_size": t.block_size, "use_graph": t.use_graph,
                 "steps_per_graph": t.steps_per_graph, "rebin": t.rebin,
                 "cell_ratio": t.cell_ratio, "pair_scheme": t.pair_scheme,
-                "persistent": t.persistent}
+                "persistent": t.persistent, "list_skin": t.list_skin}
 
     def set_tuning(self, **kw):
         """block_size, use_graph, steps_per_graph, cell_ratio, rebin (1: bin
         into cells only when a particle has used half of the cell slack,
-        VerletList.ponder_rebuild's skin reuse; 0: every step) and
+        VerletList.ponder_rebuild's skin reuse; 0: every step),
         pair_scheme (0: cell windows; 1: cluster pairs, for 3D simulations
-        in mixed precision without collisions) and persistent (1: the
-        cell-window passes as persistent grid-stride launches)."""
+        in mixed precision without collisions; 2: per-particle pair lists
+        with a skin, for 2D simulations in mixed precision without
+        collisions), list_skin (the lists' skin as a fraction of the
+        cutoff) and persistent (1: the cell-window passes as persistent
+        grid-stride launches)."""
         cur = self.tuning
         cur.update(kw)
         t = SphTuning(block_size=int(cur["block_size"]), use_graph=int(cur["use_graph"]),
                       steps_per_graph=int(cur["steps_per_graph"]), rebin=int(cur["rebin"]),
                       cell_ratio=float(cur["cell_ratio"]),
                       pair_scheme=int(cur["pair_scheme"]),
-                      persistent=int(cur["persistent"]))
+                      persistent=int(cur["persistent"]),
+                      list_skin=float(cur["list_skin"]))
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), "sph_set_tuning")
 
     def rebin_count(self):

@@ -52,10 +52,11 @@ def test_struct_layout_matches_header(tmp_path):
     src = tmp_path / "layout.c"
     src.write_text(
         '#include <stddef.h>\n#include <stdio.h>\n#include "sph.h"\n'
-        'int main(void) { printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(sph_params),'
+        'int main(void) { printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(sph_params),'
         ' offsetof(sph_params, box), offsetof(sph_params, thermostat_ramp_steps),'
         ' offsetof(sph_params, collision_cutoff), sizeof(sph_tuning),'
-        ' offsetof(sph_tuning, cell_ratio), offsetof(sph_tuning, pair_scheme)); return 0; }\n')
+        ' offsetof(sph_tuning, cell_ratio), offsetof(sph_tuning, pair_scheme),'
+        ' offsetof(sph_tuning, list_skin)); return 0; }\n')
     exe = tmp_path / "layout"
     subprocess.run([gcc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
                    check=True)
@@ -64,7 +65,7 @@ def test_struct_layout_matches_header(tmp_path):
     P, T = _abi.SphParams, _abi.SphTuning
     assert got == [ctypes.sizeof(P), P.box.offset, P.thermostat_ramp_steps.offset,
                    P.collision_cutoff.offset, ctypes.sizeof(T), T.cell_ratio.offset,
-                   T.pair_scheme.offset]
+                   T.pair_scheme.offset, T.list_skin.offset]
 
 
 def test_make_params_defaults_follow_reference():

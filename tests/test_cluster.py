@@ -241,24 +241,27 @@ def test_autotuner_times_the_cluster_scheme_for_one_3d_simulation():
 
 def test_autotuner_times_the_persistent_launch_for_batches():
     """A mixed-precision batch: the cell-window candidates, then the
-    persistent launch form at the best of them; a single simulation and an
-    FP64 batch get no persistent candidate."""
+    persistent launch form at the best of them, then the 2D pair lists; a
+    single simulation and an FP64 batch get no persistent candidate, and
+    FP64 no lists."""
     from pyticles_gb300 import autotune
     sims = [(p, r, v, m, oracle.initial_energy(p, r, v, m, T))
             for p, r, v, m, T in workloads.batched_2d(3, seed_base=4600, n_lo=256, n_hi=1024,
                                                       ramp_steps=10)]
     knobs, table = autotune.tune(sims[0][0], "mixed", sims, steps=2, warmup=1,
                                  blocks=(64, 128), ratios=(0.5,), use_cache=False)
-    assert [row["persistent"] for row in table] == [0, 0, 1]
-    best_cell = min(table[:2], key=lambda row: row["ms_per_step"])
-    assert table[2]["block_size"] == best_cell["block_size"]
+    cells = [row for row in table if row["pair_scheme"] == 0]
+    assert [row["persistent"] for row in cells] == [0, 0, 1]
+    best_cell = min(cells[:2], key=lambda row: row["ms_per_step"])
+    assert cells[2]["block_size"] == best_cell["block_size"]
+    assert [row["pair_scheme"] for row in table] == [0, 0, 0, 2, 2]
     assert knobs["persistent"] in (0, 1)
     _, one = autotune.tune(sims[0][0], "mixed", sims[:1], steps=2, warmup=1, blocks=(128,),
                            ratios=(0.5,), use_cache=False)
     _, fp64 = autotune.tune(sims[0][0], "fp64", sims, steps=2, warmup=1, blocks=(128,),
                             ratios=(0.5,), use_cache=False)
-    assert [row["persistent"] for row in one] == [0]
-    assert [row["persistent"] for row in fp64] == [0]
+    assert [(row["pair_scheme"], row["persistent"]) for row in one] == [(0, 0), (2, 0), (2, 0)]
+    assert [(row["pair_scheme"], row["persistent"]) for row in fp64] == [(0, 0)]
 
 
 def droplet(seed=3160, gas=False):
