@@ -315,9 +315,11 @@ def serve_window(njobs, time_limit, budget_gb, seed=5000, dist=None):
     return replicas.merge_served(replicas.gather(rep, dist))
 
 
-def run_e2e(prm, r, v, m, u, steps, torch, stream):
+def run_e2e(prm, r, v, m, u, steps, torch, stream, knobs=None):
     """Through the C ABI with host (pinned) buffers: every step copies the
-    state in, advances one step and reads the state back."""
+    state in, advances one step and reads the state back (the timed arm's
+    knobs; a state set from the host is binned, and with pair lists listed,
+    before its step)."""
     from pyticles_gb300 import Engine
     n, d = r.shape
     pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
@@ -325,6 +327,8 @@ def run_e2e(prm, r, v, m, u, steps, torch, stream):
     hr[:], hv[:], hm[:], hu[:] = r, v, m, u
     e = Engine(prm, "mixed", max_particles=n, stream=stream.cuda_stream)
     s = e.add(prm, hr, hv, hm, hu)
+    if knobs:
+        e.set_tuning(**knobs)
     e.set_tuning(steps_per_graph=1, use_graph=1)
     for _ in range(3):
         e.set_state(s, hr, hv, hm, hu)
@@ -445,7 +449,7 @@ def profile_case(args):
         u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
     with Engine(prm, args.precision, max_particles=len(r)) as e:
         e.add(prm, r, v, m, u)
-        e.set_tuning(use_graph=0, pair_scheme=args.pair_scheme)
+        e.set_tuning(use_graph=0, pair_scheme=args.pair_scheme or 0)
         e.advance(args.steps)
         e.sync()
         print(f"{args.profile_case} n={len(r)} steps={args.steps} "
@@ -486,7 +490,9 @@ def main():
                     help="profiling driver: --steps eager steps of one workload "
                          "(--side, --precision, --pair-scheme), no timing")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--pair-scheme", type=int, default=0, choices=[0, 1, 2])
+    ap.add_argument("--pair-scheme", type=int, default=None, choices=[0, 1, 2],
+                    help="force the pair scheme (profiling case: default 0; the timed "
+                         "2D workload: the tuner's choice)")
     args = ap.parse_args()
     if args.profile_case:
         return profile_case(args)
@@ -515,6 +521,8 @@ def main():
     if not args.no_tune:
         knobs, _ = autotune.tune(prm, "mixed", [(prm, r, v, m, u)], steps=3, warmup=2)
     knobs = dict(knobs or {}, rebin=args.rebin)
+    if args.pair_scheme is not None:
+        knobs["pair_scheme"] = args.pair_scheme
     if dist:
         dist.barrier()
     with ClockSampler(local) as clocks:
@@ -530,25 +538,30 @@ def main():
     fp64_value = pairs64 * 2 * args.fp64_steps / (ms64 * 1e-3)
 
     # end to end through the C ABI with pinned host buffers
-    wall, pairs_e, h2d, d2h = run_e2e(prm, r, v, m, u, args.e2e_steps, torch, stream)
+    wall, pairs_e, h2d, d2h = run_e2e(prm, r, v, m, u, args.e2e_steps, torch, stream,
+                                      knobs=knobs)
     e2e_value = pairs_e * 2 * args.e2e_steps / wall
 
-    # roofline of the dominant pass (force + integrator epilogue)
+    # roofline of the dominant pass (force + integrator epilogue): the pair
+    # lists' k_force_vl when the tuner chose them, else the cell windows'
+    # k_force; pair lists bin on demand whatever `rebin` says
+    lists = knobs.get("pair_scheme") == 2
+    fprof = "k_force_vl_2d_mixed.md" if lists else "k_force_2d_mixed.md"
     f = passes["force"]
     nlaunch = max(1, f["launches"])
     avg_ms = f["ms"] / nlaunch
     from pyticles_gb300 import opcount
-    bpp = opcount.force_bytes_per_step_average(2, 4, reuse=bool(args.rebin))
+    bpp = opcount.force_bytes_per_step_average(2, 4, reuse=bool(args.rebin) or lists)
     achieved = bpp * n / (avg_ms * 1e-3) / 1e9
-    trafpp = committed_traffic("k_force_2d_mixed.md")
+    trafpp = committed_traffic(fprof)
     # the binding limit, instruction issue: from one ncu launch, its warp
     # instructions over its own duration and clock against SMs x 4 issue
     # slots per cycle (both from the same launch); the live figure scales
     # that launch's instruction count to the bench's in-graph launch time
     sms = torch.cuda.get_device_properties(local).multi_processor_count
-    winst_pp = committed_figure("k_force_2d_mixed.md", "warp_instructions_per_particle")
-    ncu_ms = committed_figure("k_force_2d_mixed.md", "launch_ms")
-    ncu_mhz = committed_figure("k_force_2d_mixed.md", "sm_mhz")
+    winst_pp = committed_figure(fprof, "warp_instructions_per_particle")
+    ncu_ms = committed_figure(fprof, "launch_ms")
+    ncu_mhz = committed_figure(fprof, "sm_mhz")
     ncu_issue = None
     if winst_pp is not None and ncu_ms and ncu_mhz:
         ncu_issue = winst_pp * n / (sms * 4 * ncu_mhz * 1e6 * ncu_ms * 1e-3)
@@ -629,11 +642,16 @@ def main():
             # pass is bound by instruction issue (FP32 pair arithmetic), whose
             # fraction is `binding`
             "bound": "issue",
-            "kernel": "k_force<float,2,lucy> (force + energy rate + integrator)",
+            "kernel": ("k_force_vl<lucy> (pair lists; force + energy rate + integrator)"
+                       if lists else
+                       "k_force<float,2,lucy> (force + energy rate + integrator)"),
             "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "peak_kind": peak_kind,
             "bytes_per_particle": bpp,
             "traffic": None if trafpp is None else trafpp * n,
+            "traffic_note": ("DRAM bytes of one ncu launch (" + fprof + "); with pair lists "
+                             "they include the list entries streamed per pass (4 B each), "
+                             "which the algorithmic bytes do not count"),
             "binding": None if winst_pp is None else {
                 "limit": "instruction issue (FP32 pair arithmetic)",
                 "frac": ncu_issue,

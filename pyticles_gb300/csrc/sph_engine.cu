@@ -867,7 +867,8 @@ void enqueue_prepare(sph_engine *e, cudaStream_t st, bool gated = false, bool li
     launch_cellsort(v, e->ncells_total, st);
     launch_permute(v, e->precision, st);
     // a binning renumbers the slots: the pair lists are built again
-    if (lists && e->vl.on && e->vl.ent && e->vl.cap > 0) launch_vlist_build(v, e->vl, gate, true, st);
+    if (lists && e->vl.on && e->vl.ent && e->vl.cap > 0)
+        launch_vlist_build(v, e->vl, gate, kVlStore, st);
     if (gated) launch_rebin_close(e->rebin_gate, e->bin_count, st);
 }
 
@@ -1024,11 +1025,13 @@ int cluster_measure(sph_engine *e) {
     return SPH_OK;
 }
 
-// Measures the longest pair list of the current state (a binning and a
-// build that only counts) and sizes the rows to 1.25 times it (+8, rounded
-// up to whole groups of four).  Lists
-// longer than the count field or rows that do not fit in device memory
-// leave the layout on cell windows.
+// Bins the current state and builds the pair lists into the existing rows
+// (only counts without rows), reading back the longest list: the lists are
+// kept if it left a fifth of the rows free, otherwise the rows are resized
+// to 1.25 times it (+8, whole groups of four) and the lists built again.
+// Either way the cells and lists then match the state, so the next step
+// need not bin.  Lists longer than the count field or rows that do not fit
+// in device memory leave the layout on cell windows.
 int vl_measure(sph_engine *e) {
     VList &l = e->vl;
     if (!l.on) return SPH_OK;
@@ -1037,35 +1040,46 @@ int vl_measure(sph_engine *e) {
     e->prof_on = false;
     CK(cudaMemsetAsync(l.maxfill, 0, sizeof(int), st));
     enqueue_prepare(e, st, false, false);
-    View v = make_view(e);
-    stage_view(e, v, 0);
-    VList m = l;
-    m.cap = 0;   // counts only
-    launch_vlist_build(v, m, nullptr, false, st);
-    e->prof_on = prof;
+    const bool have = l.ent && l.cap > 0;
+    {
+        View v = make_view(e);
+        stage_view(e, v, 0);
+        VList m = l;
+        if (!have) m.cap = 0;
+        launch_vlist_build(v, m, nullptr, have ? kVlStoreQuiet : kVlCount, st);
+    }
     int fill = 0;
     CK(cudaMemcpyAsync(&fill, l.maxfill, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaMemsetAsync(l.maxfill, 0, sizeof(int), st));
     CK(cudaStreamSynchronize(st));
+    e->prof_on = prof;
     e->cl_stale = false;
     e->cl_fill_pending = false;
-    e->bins_valid = false;   // the next step bins and builds with the new rows
-    // rows of four-entry groups
-    const int need = (std::max(32, (int)std::ceil(1.25 * fill) + 8) + 3) & ~3;
-    if (need == l.cap && l.ent) return SPH_OK;
-    free_graph(e);
-    cudaFree(l.ent);
-    l.ent = nullptr;
-    l.cap = 0;
-    e->vl_alloc = 0;
-    if (need > 0xffff || dalloc(&l.ent, (size_t)need * (size_t)l.stride) != SPH_OK) {
-        l.on = 0;
-        e->vl_disabled = true;
-        e->layout_dirty = true;
+    if (have && fill <= 0.8 * l.cap) {
+        e->bins_valid = true;
         return SPH_OK;
     }
-    l.cap = need;
-    e->vl_alloc = (long long)need * l.stride;
+    const int need = (std::max(32, (int)std::ceil(1.25 * fill) + 8) + 3) & ~3;
+    if (need != l.cap || !l.ent) {
+        free_graph(e);
+        cudaFree(l.ent);
+        l.ent = nullptr;
+        l.cap = 0;
+        e->vl_alloc = 0;
+        if (need > 0xffff || dalloc(&l.ent, (size_t)need * (size_t)l.stride) != SPH_OK) {
+            l.on = 0;
+            e->vl_disabled = true;
+            e->layout_dirty = true;
+            e->bins_valid = false;
+            return SPH_OK;
+        }
+        l.cap = need;
+        e->vl_alloc = (long long)need * l.stride;
+    }
+    View v = make_view(e);
+    stage_view(e, v, 0);
+    launch_vlist_build(v, l, nullptr, kVlStoreQuiet, st);
+    e->bins_valid = true;
     return SPH_OK;
 }
 

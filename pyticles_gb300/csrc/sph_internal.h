@@ -297,8 +297,12 @@ constexpr int kVlIndexMask = (1 << kVlIndexBits) - 1;
 constexpr int kVlMaxWindow = 3;   // window offsets -3 .. 3
 
 // Builds every particle's list from the binned stage-0 state (gated like
-// the binning); with store false only measures (maxfill).
-void launch_vlist_build(const View &v, const VList &l, const int *gate, bool store,
+// the binning) and records the longest (maxfill).  kVlCount only counts;
+// kVlStore stores and reports a list that outgrew its rows (SPH_ECAPACITY,
+// its first entries kept); kVlStoreQuiet stores without reporting (the
+// engine's measuring build, which resizes the rows instead).
+enum { kVlCount = 0, kVlStore = 1, kVlStoreQuiet = 2 };
+void launch_vlist_build(const View &v, const VList &l, const int *gate, int mode,
                         cudaStream_t s);
 
 // ---- launch wrappers (sph_collide.cu) ----

@@ -18,10 +18,10 @@
 namespace sph {
 
 // One thread per particle, 2D, FP32 cell-local positions (pk_pos_in holds the
-// stage-0 packed state).  With store false only the longest list is
-// measured.
+// stage-0 packed state); mode as launch_vlist_build.
 __global__ void __launch_bounds__(256) k_vlist_build(const __grid_constant__ View v, VList l,
-                                                     const int *gate, int store) {
+                                                     const int *gate, int mode) {
+    const bool store = mode != kVlCount;
     if (gate && *gate == 0) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < v.np;
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) k_vlist_build(const __grid_constant__ Vie
         if (store) {
             // an overflowing list keeps the entries that fit (the first cap
             // of the scan) and its simulation reports the overflow
-            if (nn + nf > l.cap) set_err(v.err, v.err_any, s, SPH_ECAPACITY);
+            if (mode == kVlStore && nn + nf > l.cap) set_err(v.err, v.err_any, s, SPH_ECAPACITY);
             l.cnt[i] = (unsigned)wn | ((unsigned)wf << 16);
         }
     }
@@ -101,10 +101,10 @@ __global__ void __launch_bounds__(256) k_vlist_build(const __grid_constant__ Vie
     if ((threadIdx.x & 31) == 0 && tot > 0) atomicMax(l.maxfill, tot);
 }
 
-void launch_vlist_build(const View &v, const VList &l, const int *gate, bool store,
+void launch_vlist_build(const View &v, const VList &l, const int *gate, int mode,
                         cudaStream_t s) {
     if (v.np <= 0 || !l.on) return;
-    k_vlist_build<<<(v.np + 255) / 256, 256, 0, s>>>(v, l, gate, store ? 1 : 0);
+    k_vlist_build<<<(v.np + 255) / 256, 256, 0, s>>>(v, l, gate, mode);
 }
 
 }  // namespace sph
