@@ -5,8 +5,8 @@ cell-edge / cutoff ratio (1 -> cells of the cutoff and a 3^d window, 1/2 ->
 5^d, 1/3 -> 7^d, cells beyond the cutoff culled per particle), for batches
 in mixed precision the launch form of the cell-window passes (one thread
 per particle, or persistent grids that walk the flattened table) and the
-pair scheme in mixed precision: cell windows, per-particle pair lists (2D)
-or cluster pairs (3D; the cluster scheme has its own fixed launch shape).  A candidate is
+pair scheme in mixed precision: cell windows, per-particle pair lists or
+cluster pairs (3D; the cluster scheme has its own fixed launch shape).  A candidate is
 timed with CUDA events over a few graph-captured steps on a clone of the
 simulations (same parameters, same current states), so tuning neither
 advances the live simulations nor shifts their thermostat schedules.  Results
@@ -38,9 +38,9 @@ def cluster_candidate(group, precision, sims):
 
 
 def list_candidate(group, precision, sims):
-    """Whether per-particle pair lists can apply: 2D simulations in mixed
-    precision without collisions (the engine itself checks the grids)."""
-    return group.dim == 2 and precision == "mixed" and group.collision == 0
+    """Whether per-particle pair lists can apply: mixed precision without
+    collisions (the engine itself checks the grids and the slot count)."""
+    return precision == "mixed" and group.collision == 0
 
 
 def time_candidate(group, precision, sims, block, ratio, steps, warmup, stream, scheme=0,

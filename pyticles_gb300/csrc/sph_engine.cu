@@ -684,21 +684,21 @@ bool lists_on(const sph_engine *e) { return e->cl.on || e->vl.on; }
 int *list_maxfill(const sph_engine *e) { return e->cl.on ? e->cl.maxfill : e->vl.maxfill; }
 int list_room(const sph_engine *e) { return e->cl.on ? e->cl.lstride : e->vl.cap; }
 
-// Pair lists of a 2D mixed-precision engine (tuning.pair_scheme = 2): on
-// when every live simulation's grid has a window of 1 to 3 cells per axis
-// and room for it, without collisions, and the slots fit the entries'
-// index field.  The rows are sized by vl_measure before the next use.
+// Pair lists of a mixed-precision engine (tuning.pair_scheme = 2): on when
+// every live simulation's grid has a window of 1 to 3 cells per axis and
+// room for it, without collisions, and the slots fit the entries' index
+// field.  The rows are sized by vl_measure before the next use.
 int vl_setup(sph_engine *e) {
     VList &l = e->vl;
     l.on = 0;
-    if (e->tune.pair_scheme != 2 || e->vl_disabled || e->dim != 2 ||
-        e->precision != SPH_MIXED || e->group.collision != SPH_COLLIDE_OFF || e->np_b <= 0 ||
-        e->np_b > kVlIndexMask)
+    if (e->tune.pair_scheme != 2 || e->vl_disabled || e->precision != SPH_MIXED ||
+        e->group.collision != SPH_COLLIDE_OFF || e->np_b <= 0 ||
+        e->np_b > vl_index_mask(e->dim))
         return SPH_OK;
     for (const auto &S : e->sims) {
         if (!S.active) continue;
         if (!(S.vl_skin > 0.0)) return SPH_OK;
-        for (int a = 0; a < 2; ++a)
+        for (int a = 0; a < e->dim; ++a)
             if (S.win[a] < 1 || S.win[a] > kVlMaxWindow || S.nc[a] < 2 * S.win[a] + 1)
                 return SPH_OK;
     }
@@ -1028,7 +1028,8 @@ int cluster_measure(sph_engine *e) {
 // Bins the current state and builds the pair lists into the existing rows
 // (only counts without rows), reading back the longest list: the lists are
 // kept if it left a fifth of the rows free, otherwise the rows are resized
-// to 1.25 times it (+8, whole groups of four) and the lists built again.
+// to 1.25 times it (+8, at least 40, whole groups of four; the near and far
+// runs each fill whole groups) and the lists built again.
 // Either way the cells and lists then match the state, so the next step
 // need not bin.  Lists longer than the count field or rows that do not fit
 // in device memory leave the layout on cell windows.
@@ -1059,7 +1060,7 @@ int vl_measure(sph_engine *e) {
         e->bins_valid = true;
         return SPH_OK;
     }
-    const int need = (std::max(32, (int)std::ceil(1.25 * fill) + 8) + 3) & ~3;
+    const int need = (std::max(40, (int)std::ceil(1.25 * fill) + 8) + 3) & ~3;
     if (need != l.cap || !l.ent) {
         free_graph(e);
         cudaFree(l.ent);

@@ -30,8 +30,9 @@ __device__ __forceinline__ void write_eval_state(const View &v, const SimDev &S,
         double d = x[a] - v.org[a][i];
         if (d > S.half_L[a]) d -= S.L[a];
         if (d < -S.half_L[a]) d += S.L[a];
-        if (D == 2 && v.vl_on) {
-            const double m = d - (double)(a == 0 ? v.vl_x0[i].x : v.vl_x0[i].y);
+        if (v.vl_on) {
+            const float4 x0 = v.vl_x0[i];
+            const double m = d - (double)(a == 0 ? x0.x : (a == 1 ? x0.y : x0.z));
             moved += m * m;
         }
         xl[a] = (R)d;
@@ -75,8 +76,9 @@ __device__ __forceinline__ void write_final_state(const View &v, const SimDev &S
             double d = x[a] - v.org[a][i];
             if (d > S.half_L[a]) d -= L;   // the wrap moved it across the box
             if (d < -S.half_L[a]) d += L;
-            if (D == 2 && v.vl_on) {
-                const double m = d - (double)(a == 0 ? v.vl_x0[i].x : v.vl_x0[i].y);
+            if (v.vl_on) {
+                const float4 x0 = v.vl_x0[i];
+                const double m = d - (double)(a == 0 ? x0.x : (a == 1 ? x0.y : x0.z));
                 moved += m * m;
             } else {
                 far |= fabs(d) > S.rebin_half[a];
@@ -306,15 +308,15 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
     }
 }
 
-// The force pass over the pair lists (2D, mixed precision); a single
+// The force pass over the pair lists (mixed precision); a single 2D
 // simulation at SPH_VL_FORCE_BLOCKS resident blocks of 256 per SM.
 #ifndef SPH_VL_FORCE_BLOCKS
 #define SPH_VL_FORCE_BLOCKS 5
 #endif
-template <int K, int VH, bool ONE>
-__global__ void __launch_bounds__(256, ONE ? SPH_VL_FORCE_BLOCKS : 4) k_force_vl(const __grid_constant__ View v, int stage,
-                                                              int mode, int integ) {
-    force_one<float, 2, K, VH, ONE, true>(v, stage, mode, integ,
+template <int D, int K, int VH, bool ONE>
+__global__ void __launch_bounds__(256, ONE && D == 2 ? SPH_VL_FORCE_BLOCKS : 4)
+    k_force_vl(const __grid_constant__ View v, int stage, int mode, int integ) {
+    force_one<float, D, K, VH, ONE, true>(v, stage, mode, integ,
                                           blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -336,9 +338,9 @@ __global__ void __launch_bounds__(256) k_integrate(View v, int stage, int integ,
 // the persistent form for the mixed-precision pass only (see density_launch)
 template <typename R, int D, int K, int VH, bool ONE>
 void force_launch(const View &v, int stage, int mode, int integ, int block, cudaStream_t s) {
-    if constexpr (std::is_same<R, float>::value && D == 2) {
+    if constexpr (std::is_same<R, float>::value) {
         if (v.vl_on) {
-            k_force_vl<K, VH, ONE>
+            k_force_vl<D, K, VH, ONE>
                 <<<(v.np + block - 1) / block, block, 0, s>>>(v, stage, mode, integ);
             return;
         }

@@ -184,7 +184,7 @@ struct View {
     long long vl_stride;
     const int *vl_ent;
     const unsigned *vl_cnt;
-    float2 *vl_x0;
+    float4 *vl_x0;
     SimDev one;
 };
 
@@ -276,10 +276,11 @@ void launch_cluster_force(const View &v, const ClusterSet &c, int kernel, int vi
                           cudaStream_t s);
 int cluster_build_kernels();
 
-// Pair lists of the 2D mixed-precision cell-window engine (tuning.pair_scheme
-// 2, sph_vlist.cu).  An entry packs the neighbour's B-order index (bits
-// 0-25) and its cell's window offset from the particle's cell, ox + 3 and
-// oy + 3 in three bits each (bits 26-28, 29-31).
+// Pair lists of the mixed-precision cell-window engine (tuning.pair_scheme
+// 2, sph_vlist.cu).  An entry packs the neighbour's B-order index (the low
+// vl_index_bits(D) bits: 26 in 2D, 23 in 3D) and its cell's window offset
+// from the particle's cell, o + 3 in three bits per axis above it (x, y[, z]
+// upward, z in the top bits).
 struct VList {
     int on;
     int cap;                      // entries reserved per particle (a multiple of 4)
@@ -289,15 +290,16 @@ struct VList {
                                   // slot k%4; far entry k at group row cap/4 - 1 - k/4,
                                   // slot 3 - k%4
     unsigned *cnt;                // [stride] near | far << 16
-    float2 *x0;                   // [stride] cell-local position at the build
+    float4 *x0;                   // [stride] cell-local position at the build
     int *maxfill;                 // longest list since the host last read it
 };
-constexpr int kVlIndexBits = 26;
-constexpr int kVlIndexMask = (1 << kVlIndexBits) - 1;
+__host__ __device__ constexpr int vl_index_bits(int dim) { return 32 - 3 * dim; }
+__host__ __device__ constexpr int vl_index_mask(int dim) { return (1 << vl_index_bits(dim)) - 1; }
 constexpr int kVlMaxWindow = 3;   // window offsets -3 .. 3
 
 // Builds every particle's list from the binned stage-0 state (gated like
-// the binning) and records the longest (maxfill).  kVlCount only counts;
+// the binning) and records the longest (maxfill, in entries of whole groups:
+// the near and the far run each fill whole groups).  kVlCount only counts;
 // kVlStore stores and reports a list that outgrew its rows (SPH_ECAPACITY,
 // its first entries kept); kVlStoreQuiet stores without reporting (the
 // engine's measuring build, which resizes the rows instead).

@@ -106,14 +106,15 @@ __global__ void __launch_bounds__(256, ONE ? ((D == 2 && sizeof(R) == 4) ? 7 : 5
     }
 }
 
-// The density pass over the pair lists (2D, mixed precision); a single
+// The density pass over the pair lists (mixed precision); a single 2D
 // simulation at SPH_VL_DENSITY_BLOCKS resident blocks of 256 per SM.
 #ifndef SPH_VL_DENSITY_BLOCKS
 #define SPH_VL_DENSITY_BLOCKS 7
 #endif
-template <int K, bool ONE>
-__global__ void __launch_bounds__(256, ONE ? SPH_VL_DENSITY_BLOCKS : 4) k_density_vl(const __grid_constant__ View v, int stage) {
-    density_one<float, 2, K, ONE, true>(v, stage, blockIdx.x * blockDim.x + threadIdx.x);
+template <int D, int K, bool ONE>
+__global__ void __launch_bounds__(256, ONE ? (D == 2 ? SPH_VL_DENSITY_BLOCKS : 5) : 4)
+    k_density_vl(const __grid_constant__ View v, int stage) {
+    density_one<float, D, K, ONE, true>(v, stage, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // At most 64 registers (4 blocks of 256 per SM): 8% faster in 3D than 80.
@@ -174,19 +175,19 @@ __global__ void __launch_bounds__(256, 4) k_heat(const __grid_constant__ View v)
     }
 }
 
-template <int K, bool ONE>
+template <int D, int K, bool ONE>
 __global__ void __launch_bounds__(256, 4) k_heat_vl(const __grid_constant__ View v) {
-    heat_one<float, 2, K, ONE, true>(v, blockIdx.x * blockDim.x + threadIdx.x);
+    heat_one<float, D, K, ONE, true>(v, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // The persistent form is instantiated for the mixed-precision passes only;
 // FP64 engines launch one thread per particle whatever tuning.persistent says.
-// Pair lists (v.vl_on) exist for 2D mixed-precision engines only.
+// Pair lists (v.vl_on) exist for mixed-precision engines only.
 template <typename R, int D, int K, bool ONE>
 void density_launch(const View &v, int stage, int block, cudaStream_t s) {
-    if constexpr (std::is_same<R, float>::value && D == 2) {
+    if constexpr (std::is_same<R, float>::value) {
         if (v.vl_on) {
-            k_density_vl<K, ONE><<<(v.np + block - 1) / block, block, 0, s>>>(v, stage);
+            k_density_vl<D, K, ONE><<<(v.np + block - 1) / block, block, 0, s>>>(v, stage);
             return;
         }
     }
@@ -200,9 +201,9 @@ void density_launch(const View &v, int stage, int block, cudaStream_t s) {
 
 template <typename R, int D, int K, bool ONE>
 void heat_launch(const View &v, int block, cudaStream_t s) {
-    if constexpr (std::is_same<R, float>::value && D == 2) {
+    if constexpr (std::is_same<R, float>::value) {
         if (v.vl_on) {
-            k_heat_vl<K, ONE><<<(v.np + block - 1) / block, block, 0, s>>>(v);
+            k_heat_vl<D, K, ONE><<<(v.np + block - 1) / block, block, 0, s>>>(v);
             return;
         }
     }

@@ -200,7 +200,7 @@ __device__ __forceinline__ float vl_offset(unsigned k) {
 }
 
 // Iterates the pair set of particle i from its pair list (tuning.pair_scheme
-// 2; 2D, FP32): the near entries, then with FAR the far ones, each in the
+// 2; FP32): the near entries, then with FAR the far ones, each in the
 // order of the build (window cells in raster order, particles in cell
 // order), with the same fast test and exact FP64 fallback as for_pairs.
 // body(j, pj, d, rsq, near) as in for_pairs; cell_done() folds the blocked
@@ -220,21 +220,28 @@ template <typename R, int D, bool FAR, typename T4, typename F, typename G>
 __device__ __forceinline__ void for_list(const View &v, const SimDev &S,
                                          const PairFrame<R, D> &fr, const T4 *__restrict__ P,
                                          int i, const T4 &pi, F body, G cell_done) {
-    static_assert(std::is_same<R, float>::value && D == 2, "pair lists: 2D mixed precision");
+    static_assert(std::is_same<R, float>::value, "pair lists: mixed precision");
+    constexpr int kBits = vl_index_bits(D);
     const unsigned cnt = v.vl_cnt[i];
     const int nn = (int)(cnt & 0xffffu), nf = (int)(cnt >> 16);
     const long long st = v.vl_stride;
     auto one = [&](int code, auto near) {
-        const int j = code & kVlIndexMask;
+        const int j = code & vl_index_mask(D);
         if (!SPH_IN_BOUNDS(j >= 0 && j < v.np, v.err_any)) return;
-        const float fx = vl_offset(((unsigned)code >> 26) & 7u);
-        const float fy = vl_offset((unsigned)code >> 29);
+        const unsigned t = (unsigned)code >> kBits;
+        const float fx = vl_offset(t & 7u);
+        const float fy = vl_offset(D == 3 ? (t >> 3) & 7u : t >> 3);
         const T4 pj = P[j];
         R d[3];
         d[0] = __fmaf_rn(fx, fr.edge_lo[0], __fmaf_rn(fx, fr.edge[0], __fsub_rn(pj.x, pi.x)));
         d[1] = __fmaf_rn(fy, fr.edge_lo[1], __fmaf_rn(fy, fr.edge[1], __fsub_rn(pj.y, pi.y)));
         d[2] = (R)0;
-        const R rsq = d[0] * d[0] + d[1] * d[1];
+        R rsq = d[0] * d[0] + d[1] * d[1];
+        if (D == 3) {
+            const float fz = vl_offset(t >> 6);
+            d[2] = __fmaf_rn(fz, fr.edge_lo[2], __fmaf_rn(fz, fr.edge[2], __fsub_rn(pj.z, pi.z)));
+            rsq += d[2] * d[2];
+        }
         if (rsq > fr.thr_hi) return;
         if (rsq >= fr.thr_lo && !exact_in_set<D>(v.xe_in, &S, i, j)) return;
         body(j, pj, d, rsq, near);

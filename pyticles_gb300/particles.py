@@ -136,7 +136,10 @@ class SmoothParticleSystem(ParticleSystem):
                  stays exact, the summation order follows the binning times
     pair_scheme -- 0: cell-window pair passes; 1: cluster pairs (a 3D system
                  in mixed precision, 1.5x faster; elsewhere the cell scheme
-                 runs); same pair set, rounding differs
+                 runs); 2: per-particle pair lists with a skin, rebuilt when
+                 a particle has moved a quarter of it (mixed precision, 2D
+                 or 3D; 1.5x the cell scheme in 2D, 1.7x the cluster pairs
+                 in 3D); same pair set, rounding differs
     """
 
     N_VARIABLES = 11   # + rho, p, pco, u (particles.py:355-358)

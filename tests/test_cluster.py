@@ -227,13 +227,14 @@ def test_cluster_scheme_full_size_invariants():
 
 
 def test_autotuner_times_the_cluster_scheme_for_one_3d_simulation():
+    """Cell windows, the pair lists (two block sizes) and the cluster pairs."""
     from pyticles_gb300 import autotune
     prm, r, v, m, T0 = workloads.config_3d(20, 3150)
     u = workloads.vdw_energy(np.full(len(r), 0.7), T0)
     knobs, table = autotune.tune(prm, "mixed", [(prm, r, v, m, u)], steps=2, warmup=1,
                                  blocks=(128,), ratios=(0.5,), use_cache=False)
-    assert [row["pair_scheme"] for row in table] == [0, 1]
-    assert knobs["pair_scheme"] in (0, 1)
+    assert [row["pair_scheme"] for row in table] == [0, 2, 2, 1]
+    assert knobs["pair_scheme"] in (0, 1, 2)
     _, table2 = autotune.tune(prm, "fp64", [(prm, r, v, m, u)], steps=2, warmup=1,
                               blocks=(128,), ratios=(0.5,), use_cache=False)
     assert [row["pair_scheme"] for row in table2] == [0]
