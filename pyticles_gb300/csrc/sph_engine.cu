@@ -119,6 +119,7 @@ struct sph_engine {
     int *chunk_sim = nullptr, *chunk_start = nullptr, *chunk_len = nullptr;
     CollideSet coll = {};          // hard-collision candidates (group.collision)
     int *rebin_gate = nullptr;     // tuning.rebin: bin before the next step
+    int *restage_far = nullptr;    // set_state kept the binning unless raised
     unsigned long long *bin_count = nullptr;
     bool bins_valid = false;       // B, its packed copies and the cells match A
     bool one_sim = false;          // exactly one live simulation (one_dev)
@@ -1334,6 +1335,7 @@ int alloc_sims(sph_engine *e) {
     TRY(dalloc(&e->err, S));
     TRY(dalloc(&e->err_any, 1));
     TRY(dalloc(&e->rebin_gate, 1));
+    TRY(dalloc(&e->restage_far, 1));
     TRY(dalloc(&e->bin_count, 1));
     CK(cudaMemset(e->rebin_gate, 0, sizeof(int)));
     CK(cudaMemset(e->bin_count, 0, sizeof(unsigned long long)));
@@ -1354,7 +1356,8 @@ void free_all(sph_engine *e) {
                     e->pk_vel[0], e->pk_vel[1], e->pk_f, e->pk_q, e->pk_fv, e->ue, e->rho, e->rho_l,
                     e->temp, e->pres, e->pco, e->rho0, e->pres0, e->pco0, e->udot, e->f0u,
                     e->acc_u, e->stage_buf, e->sims_d, e->t_scale, e->tsum_part, e->steps_d,
-                    e->pair_count, e->err, e->err_any, e->rebin_gate, e->bin_count,
+                    e->pair_count, e->err, e->err_any, e->rebin_gate, e->restage_far,
+                    e->bin_count,
                     e->chunk_sim, e->chunk_start,
                     e->chunk_len, e->cell_xyz};
     for (void *p : ptrs)
@@ -1577,10 +1580,30 @@ int sph_sim_set_state(sph_engine *e, int32_t id, const double *r, const double *
     // gives original order, so reset ids to identity for the range.
     TRY(write_state_range(e, S.a_off, S.n, r, v, m, u, mem));
     if (all) launch_iota_sim(e->a_id + S.a_off, e->a_sim + S.a_off, id, (int)S.n, e->stream);
-    CK(cudaStreamSynchronize(e->stream));
+    // With binning on demand the current cells (and pair lists) are kept
+    // when the new state lies within their slack: it goes straight into the
+    // simulation's B slots in the current order.  Otherwise the next step
+    // bins (and measures the lists) again.
+    bool kept = false;
+    if (all && rebin_on_demand(e) && e->bins_valid && !e->layout_dirty && !e->cl.on &&
+        (!e->vl.on || (e->vl.ent && !e->cl_stale))) {
+        cudaStream_t st = e->stream;
+        int far = 1;
+        CK(cudaMemsetAsync(e->restage_far, 0, sizeof(int), st));
+        View vw = make_view(e);
+        stage_view(e, vw, 0);
+        launch_restage(vw, e->precision, S.a_off, S.part_off, (int)S.n, e->restage_far, st);
+        CK(cudaMemcpyAsync(&far, e->restage_far, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        kept = far == 0;
+    } else {
+        CK(cudaStreamSynchronize(e->stream));
+    }
     e->props_valid = false;
-    e->bins_valid = false;
-    e->cl_stale = true;
+    if (!kept) {
+        e->bins_valid = false;
+        e->cl_stale = true;
+    }
     return SPH_OK;
 }
 

@@ -333,6 +333,11 @@ void launch_scan(int *count, int *start, int n, int *block_tmp, cudaStream_t s,
 void launch_scatter(const View &v, int np_a, cudaStream_t s);
 void launch_cellsort(const View &v, int ncells, cudaStream_t s);
 void launch_permute(const View &v, int precision, cudaStream_t s);
+// A simulation's state just set in A (identity order from a_off) into its B
+// slots [b0, b0 + n) of the current binning; raises *far if it needs a new
+// binning (sph_sort.cu).
+void launch_restage(const View &v, int precision, int a_off, int b0, int n, int *far,
+                    cudaStream_t s);
 void launch_load_aos(double *dst[3], const double *src, int n, int dim, cudaStream_t s);
 void launch_store_aos(double *dst, double *const src[3], const int *id, int off, int n, int dim,
                       cudaStream_t s);

@@ -236,6 +236,58 @@ __global__ void k_permute(View v) {
     for (int j = first; j < v.np; j += gridDim.x * blockDim.x) permute_one<R>(v, j);
 }
 
+// A state set from the host (A in identity order from a_off) into the B
+// slots [b0, b0 + n) of the current binning, keeping the cells, the order
+// and the pair lists: B and the stage-0 packed copies relative to the cells'
+// frames.  *far is raised if some particle lies past half of its cell slack
+// or, with pair lists, a quarter of the skin from its position at their
+// build -- the caller then bins again.  The check is write_final_state's.
+template <typename R>
+__global__ void k_restage(View v, int a_off, int b0, int n, int *far) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int j = b0 + k;
+    const int a = a_off + v.b_id[j];
+    const SimDev &S = v.one_sim ? v.one : v.sims[v.b_sim[j]];
+    R xl[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
+    bool out = false;
+    double moved = 0.0;
+    for (int d = 0; d < v.dim; ++d) {
+        const double x = v.a_pos[d][a], vel = v.a_vel[d][a];
+        v.b_pos[d][j] = x;
+        v.b_vel[d][j] = vel;
+        double r = x - v.org[d][j];
+        if (r > S.half_L[d]) r -= S.L[d];
+        if (r < -S.half_L[d]) r += S.L[d];
+        if (v.vl_on) {
+            const float4 x0 = v.vl_x0[j];
+            const double m = r - (double)(d == 0 ? x0.x : (d == 1 ? x0.y : x0.z));
+            moved += m * m;
+        } else {
+            out |= fabs(r) > S.rebin_half[d];
+        }
+        xl[d] = (R)r;
+        vv[d] = (R)vel;
+    }
+    out |= moved > S.vl_gate2;
+    const double m = v.a_m[a];
+    v.b_u[j] = v.a_u[a];
+    v.b_m[j] = m;
+    using T4 = typename V4<R>::T;
+    ((T4 *)v.pk_pos_out)[j] = make_v4<R>(xl[0], xl[1], xl[2], (R)m);
+    ((T4 *)v.pk_vel_out)[j] = make_v4<R>(vv[0], vv[1], vv[2], (R)0);
+    if (out) *far = 1;
+}
+
+void launch_restage(const View &v, int precision, int a_off, int b0, int n, int *far,
+                    cudaStream_t s) {
+    if (n <= 0) return;
+    if (precision == SPH_MIXED)
+        k_restage<float><<<(n + 255) / 256, 256, 0, s>>>(v, a_off, b0, n, far);
+    else
+        k_restage<double><<<(n + 255) / 256, 256, 0, s>>>(v, a_off, b0, n, far);
+}
+
 void launch_permute(const View &v, int precision, cudaStream_t s) {
     if (v.np <= 0) return;
     int nb = sort_blocks(v.np, 256);

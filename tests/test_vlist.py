@@ -286,3 +286,35 @@ def test_lists_agree_with_clusters_in_3d():
     # JQ_TOL against the oracle)
     for k in ("rho", "vdot", "udot", "jq"):
         assert rel_l2(out[2][0][k], out[0][0][k]) < (JQ_TOL if k == "jq" else 5e-7), k
+
+
+@pytest.mark.parametrize("scheme", [0, 2])
+def test_state_round_trips_keep_the_trajectory(scheme):
+    """The end-to-end pattern -- the state out to the host and back in every
+    step -- gives the bits of the plain advance: a state set within the
+    cells' slack (and the lists' skin) goes into the current binning, and
+    one beyond it is binned exactly as the step would have."""
+    prm, r, v, m, T0 = workloads.config_2d(32, 1004, viscosity=True)
+    v = v * 5.0
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    knobs = dict(pair_scheme=scheme, rebin=1, steps_per_graph=1)
+    with Engine(prm, "mixed", max_particles=len(r)) as e:
+        s = e.add(prm, r, v, m, u)
+        e.set_tuning(**knobs)
+        e.advance(30)
+        e.sync()
+        ref = e.get_state(s)
+        bins_ref = e.rebin_count()
+    with Engine(prm, "mixed", max_particles=len(r)) as e:
+        s = e.add(prm, r, v, m, u)
+        e.set_tuning(**knobs)
+        e.advance(1)
+        for _ in range(29):
+            rr, vv, uu = e.get_state(s)
+            e.set_state(s, rr, vv, m, uu)
+            e.advance(1)
+        e.sync()
+        got = e.get_state(s)
+        assert bins_ref >= 2
+    for a, b in zip(ref, got):
+        assert np.array_equal(a, b)
