@@ -604,7 +604,7 @@ def main():
     accuracy = None
     if rank == 0 and not args.no_cpu and args.accuracy_steps > 0:
         accuracy = accuracy_track(prm, r, v, m, u, args.accuracy_steps,
-                                  max(1, min(100, args.accuracy_steps)), stream)
+                                  max(1, min(100, args.accuracy_steps)), stream, knobs=knobs)
         for row in accuracy:
             row.pop("oracle_eval")
 
