@@ -308,13 +308,17 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
     }
 }
 
-// The force pass over the pair lists (mixed precision); a single 2D
-// simulation at SPH_VL_FORCE_BLOCKS resident blocks of 256 per SM.
+// The force pass over the pair lists (mixed precision); a single
+// simulation at SPH_VL_FORCE_BLOCKS (2D) / SPH_VL_FORCE3_BLOCKS (3D)
+// resident blocks of 256 per SM.
 #ifndef SPH_VL_FORCE_BLOCKS
 #define SPH_VL_FORCE_BLOCKS 5
 #endif
+#ifndef SPH_VL_FORCE3_BLOCKS
+#define SPH_VL_FORCE3_BLOCKS 4
+#endif
 template <int D, int K, int VH, bool ONE>
-__global__ void __launch_bounds__(256, ONE && D == 2 ? SPH_VL_FORCE_BLOCKS : 4)
+__global__ void __launch_bounds__(256, ONE ? (D == 2 ? SPH_VL_FORCE_BLOCKS : SPH_VL_FORCE3_BLOCKS) : 4)
     k_force_vl(const __grid_constant__ View v, int stage, int mode, int integ) {
     force_one<float, D, K, VH, ONE, true>(v, stage, mode, integ,
                                           blockIdx.x * blockDim.x + threadIdx.x);

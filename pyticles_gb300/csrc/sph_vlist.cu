@@ -95,41 +95,44 @@ __global__ void __launch_bounds__(256) k_vlist_build(const __grid_constant__ Vie
                             rsq += ddz * ddz;
                         }
                         if (rsq > thr) continue;
+                        const bool near = rsq < thr_n;
+                        nn += near ? 1 : 0;
+                        nf += near ? 0 : 1;
+                        if (!store) continue;
+                        // groups fill as shift registers: near entries enter
+                        // at w (the oldest ends in x), far ones at x (the
+                        // oldest ends in w); whole groups only, so the near
+                        // and far runs never share one
                         const int code = j | tag;
-                        // whole groups: the near and far runs never share one
                         const int rows_cap = l.cap >> 2;
-                        if (rsq < thr_n) {
+                        if (near) {
                             if (((wn + 4) >> 2) + ((wf + 3) >> 2) <= rows_cap) {
-                                const int k = wn & 3;
-                                if (k == 0) gn.x = code;
-                                else if (k == 1) gn.y = code;
-                                else if (k == 2) gn.z = code;
-                                else gn.w = code;
-                                if (store && k == 3) rows[(long long)(wn >> 2) * l.stride] = gn;
-                                ++wn;
+                                gn = make_int4(gn.y, gn.z, gn.w, code);
+                                if ((++wn & 3) == 0)
+                                    rows[(long long)((wn >> 2) - 1) * l.stride] = gn;
                             }
-                            ++nn;
                         } else {
                             if (((wn + 3) >> 2) + ((wf + 4) >> 2) <= rows_cap) {
-                                const int k = wf & 3;
-                                if (k == 0) gf.w = code;
-                                else if (k == 1) gf.z = code;
-                                else if (k == 2) gf.y = code;
-                                else gf.x = code;
-                                if (store && k == 3)
-                                    rows[far0 - (long long)(wf >> 2) * l.stride] = gf;
-                                ++wf;
+                                gf = make_int4(code, gf.x, gf.y, gf.z);
+                                if ((++wf & 3) == 0)
+                                    rows[far0 - (long long)((wf >> 2) - 1) * l.stride] = gf;
                             }
-                            ++nf;
                         }
                     }
                 }
             }
         }
         if (store) {
-            // the partial last groups (their unused slots are never read)
-            if (wn & 3) rows[(long long)(wn >> 2) * l.stride] = gn;
-            if (wf & 3) rows[far0 - (long long)(wf >> 2) * l.stride] = gf;
+            // the partial last groups, shifted into place (their unused
+            // slots are never read)
+            if (wn & 3) {
+                for (int t = wn & 3; t < 4; ++t) gn = make_int4(gn.y, gn.z, gn.w, 0);
+                rows[(long long)(wn >> 2) * l.stride] = gn;
+            }
+            if (wf & 3) {
+                for (int t = wf & 3; t < 4; ++t) gf = make_int4(0, gf.x, gf.y, gf.z);
+                rows[far0 - (long long)(wf >> 2) * l.stride] = gf;
+            }
             // an overflowing list keeps the entries that fit (the first cap
             // of the scan) and its simulation reports the overflow
             if (mode == kVlStore && (wn < nn || wf < nf))
