@@ -245,14 +245,18 @@ __device__ __forceinline__ void force_one(const View &v, int stage, int mode, in
         // beyond the short support gs = 0: the pressure and viscosity terms
         // vanish and gsum = gl bit for bit
         R gsum = gl, gs = (R)0;
+        // the heat record {q/rho^2, rho}: with heat flux in 3D it also
+        // carries the density the viscosity needs
+        T4 qj = make_v4<R>(0, 0, 0, 0);
         if constexpr (NEAR) {
+            if (heat) qj = Q[j];
             gs = kernel_g<K, R, true>(ks, dd);
             R ps = fsi + (D == 2 ? fvj.z : fvj.w);
             // Monaghan viscosity on approaching pairs within the short
             // support (beyond it gs = 0, so ps no longer enters gsum and the
             // warp skips the block when none of its pairs needs it)
             if (visc && dvdx < (R)0 && gs != (R)0) {
-                const R rhoj = D == 2 ? fvj.w : RHO[j];
+                const R rhoj = D == 2 ? fvj.w : (heat ? qj.w : RHO[j]);
                 R mu = fdiv<R>(hs * dvdx, rsq + eps_h2);
                 ps += fdiv<R>((R)2 * (-alpha_c * mu + beta * mu * mu), rhoi + rhoj);
             }
@@ -265,7 +269,6 @@ __device__ __forceinline__ void force_one(const View &v, int stage, int mode, in
         // (scaling by 2 is exact, so the bits are those of the halved terms)
         R du = gsum * dvdx * pj.w;
         if (heat && NEAR) {
-            T4 qj = Q[j];
             R dq = (qi.x + qj.x) * d[0] + (qi.y + qj.y) * d[1];
             if (D == 3) dq += (qi.z + qj.z) * d[2];
             du -= (R)2 * dq * gs * pj.w;

@@ -139,7 +139,7 @@ struct View {
     // evaluation (stage s reads *_in, its force pass writes stage s+1's *_out)
     void *pk_pos_in, *pk_vel_in;     // float4 / double4: {xl, yl, zl, m}, {vx, vy, vz, 0}
     void *pk_pos_out, *pk_vel_out;
-    void *pk_f, *pk_q;               // {p/rho^2, rho, T_hi, T_lo}, {q/rho^2, 0}
+    void *pk_f, *pk_q;               // {p/rho^2, rho, T_hi, T_lo}, {q/rho^2, rho}
     void *pk_fv;                     // force-pass view of j: 2D {vx, vy, p/rho^2, rho},
                                      // 3D {vx, vy, vz, p/rho^2} (rho from `rho`)
     double *xe_in[3], *xe_out[3];    // FP64 raw evaluation positions (exact pair test)

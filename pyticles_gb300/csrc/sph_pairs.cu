@@ -166,7 +166,9 @@ __device__ __forceinline__ void heat_one(const View &v, int i) {
     R qq[3] = {kap * q[0].get(), kap * q[1].get(), kap * q[2].get()};
     R ir2 = (R)1 / (fi.y * fi.y);
     for (int a = 0; a < D; ++a) ((R *)v.q[a])[i] = qq[a];
-    ((T4 *)v.pk_q)[i] = make_v4<R>(qq[0] * ir2, qq[1] * ir2, qq[2] * ir2, (R)0);
+    // {q/rho^2, rho}: the force pass's heat record, which in 3D also gives
+    // it the neighbour's density
+    ((T4 *)v.pk_q)[i] = make_v4<R>(qq[0] * ir2, qq[1] * ir2, qq[2] * ir2, fi.y);
 }
 
 template <typename R, int D, int K, bool ONE, bool PERSIST>
