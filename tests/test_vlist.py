@@ -318,3 +318,36 @@ def test_state_round_trips_keep_the_trajectory(scheme):
         assert bins_ref >= 2
     for a, b in zip(ref, got):
         assert np.array_equal(a, b)
+
+
+def test_lists_grow_with_a_denser_state():
+    """A state set from outside that is far denser than the one the rows were
+    sized for: the engine measures again, grows the rows and evaluates the
+    oracle's pair set; a later, sparser state keeps working."""
+    rng = np.random.default_rng(11)
+    n = 1600
+    prm, r, v, m, T0 = workloads.config_2d(40, 1005, viscosity=True)
+    r, v = r[:n], v[:n]
+    m = np.full(n, 0.2)    # keeps the packed state's densities below the pole b rho = 1
+    u = np.full(n, 0.5)
+    with listed(prm, r, v, m, u) as e:
+        s = e.add(prm, r, v, m, u)
+        e.advance(2)
+        e.sync()
+        # the same particles packed into a quarter of the box: about four
+        # times the neighbours per particle
+        dense = 0.5 * r + rng.uniform(-0.05, 0.05, size=r.shape)
+        e.set_state(s, dense, v, m, u)
+        d = e.derivatives(s)
+        nip = e.pair_count(s)
+        ref = oracle.derivatives(prm, dense, v, m, u)
+        assert nip == ref["nip"]
+        for k in ("rho", "vdot", "udot"):
+            assert rel_l2(d[k], ref[k]) < 1e-5, k
+        e.advance(2)
+        e.sync()
+        e.set_state(s, r, v, m, u)
+        d = e.derivatives(s)
+        ref = oracle.derivatives(prm, r, v, m, u)
+        for k in ("rho", "vdot", "udot"):
+            assert rel_l2(d[k], ref[k]) < MIXED_TOL, k
