@@ -95,3 +95,26 @@ def test_algorithmic_counts():
     assert opcount.flops_per_pair(3, heat=True) == 151
     assert opcount.force_bytes_per_particle(2, 4, False) == 216
     assert opcount.force_bytes_per_step_average(2, 4) == (216 + 184) / 2
+
+
+def test_autotuner_candidates_follow_the_schemes_rules():
+    """Which pair schemes the tuner times (host logic only): pair lists for
+    any mixed-precision group without collisions, cluster pairs for 3D
+    ones, neither in FP64 or with a collision force."""
+    from pyticles_gb300 import autotune
+    g2 = _abi.make_params(dim=2)
+    g3 = _abi.make_params(dim=3, box=(10.0, 10.0, 10.0), kernel="cubic", h_short=1.0,
+                          h_long=2.0)
+    gc = _abi.make_params(dim=2, collision_cutoff=0.5)   # a collision force
+    assert autotune.list_candidate(g2, "mixed", []) and autotune.list_candidate(g3, "mixed", [])
+    assert not autotune.list_candidate(g2, "fp64", [])
+    assert not autotune.list_candidate(gc, "mixed", [])
+    assert autotune.cluster_candidate(g3, "mixed", [])
+    assert not autotune.cluster_candidate(g2, "mixed", [])
+
+
+def test_tuning_carries_the_list_skin():
+    """sph_tuning.list_skin round-trips through the binding's structure."""
+    t = _abi.SphTuning(block_size=128, use_graph=1, steps_per_graph=4, rebin=0,
+                       cell_ratio=0.5, pair_scheme=2, persistent=0, list_skin=0.025)
+    assert (t.pair_scheme, t.list_skin) == (2, 0.025)
