@@ -2,8 +2,8 @@
 pair and collision kernels test every cell and particle index they derive
 and report SPH_EBOUNDS instead of accessing out of range.  Ordinary
 workloads -- batched, 2D and 3D, binning on demand, collisions, small
-single-cell boxes, cluster pairs beside cell windows -- run clean under it
-and give the release build's bits.
+single-cell boxes, cluster pairs beside cell windows, pair lists in 2D
+batches and in 3D -- run clean under it and give the release build's bits.
 The library is loaded in a child process (PYTICLES_CHECKS=1)."""
 import os
 import subprocess
@@ -64,6 +64,23 @@ with Engine(p4, "mixed", max_particles=len(r5) + len(r4), max_sims=2) as e:
         e.derivatives(s)
         out.append(e.get_state(s)[0].sum())
     e.sync()
+# pair lists: a batch of two 2D simulations, and the 3D fluid
+with Engine(sims[0][0], "mixed", max_particles=len(sims[0][1]) + len(sims[2][1]),
+            max_sims=2) as e:
+    ids = [e.add(*sims[0]), e.add(*sims[2])]
+    e.set_tuning(pair_scheme=2, steps_per_graph=4)
+    e.advance(12)
+    e.sync()
+    for s in ids:
+        e.derivatives(s)
+        out.append(e.get_state(s)[0].sum())
+    e.sync()
+with Engine(p3, "mixed", max_particles=len(r3)) as e:
+    s = e.add(p3, r3, v3, m3, workloads.vdw_energy(np.full(len(r3), 0.7), T3))
+    e.set_tuning(pair_scheme=2, steps_per_graph=3)
+    e.advance(6)
+    e.sync()
+    out.append(e.get_state(s)[0].sum())
 print(repr([float(x) for x in out]))
 """
 
