@@ -289,7 +289,7 @@ def timed_workload(sims, steps, warmup, torch, stream, tune=True, rebin=0):
             "pass_ms_per_step": {k: p["ms"] / steps for k, p in passes.items()}}
 
 
-def serve_window(njobs, time_limit, budget_gb, seed=5000, dist=None):
+def serve_window(njobs, time_limit, budget_gb, seed=5000, dist=None, schemes=(0, 1)):
     """A fixed Poisson arrival window of the served workload (20 jobs/s, 70%
     2D, N log-uniform in [1e3, 1e6], steps uniform in [100, 5000]), served in
     real time within an HBM budget small enough that admission queues.  The
@@ -298,15 +298,18 @@ def serve_window(njobs, time_limit, budget_gb, seed=5000, dist=None):
     are reported as unfinished, and the work they did counts toward the
     achieved load.  Offered load counts each job's pairs from the fluid's
     density (56.5 unordered pairs per particle in 2D, about 200 in 3D) x 2
-    evaluations x its steps, over the arrival window."""
+    evaluations x its steps, over the arrival window.  schemes: the 2D and
+    3D groups' pair schemes."""
     from pyticles_gb300 import replicas, serve
     jobs = serve.poisson_jobs(njobs, seed=seed)
     if dist is not None and dist.is_initialized():
         # each rank serves its round-robin share of the one arrival stream
         jobs = replicas.shard(jobs, dist.get_rank(), dist.get_world_size())
     offered = sum(j.n * (56.5 if j.dim == 2 else 200.0) * 2 * j.steps for j in jobs)
-    srv = serve.Server(budget_gb * 1e9, chunk=25, max_sims=256)
+    srv = serve.Server(budget_gb * 1e9, chunk=25, max_sims=256, pair_scheme_2d=schemes[0],
+                       pair_scheme_3d=schemes[1])
     rep = srv.run(jobs, realtime=True, time_limit=time_limit)
+    rep["pair_schemes"] = {"2d": schemes[0], "3d": schemes[1]}
     rep["job_records"] = srv.job_records(jobs)
     srv.close()
     rep["offered_pair_interactions_per_s"] = offered / max(rep["arrival_window_s"], 1e-9)

@@ -37,7 +37,9 @@ from .workloads import lattice_system, rng_for, vdw_energy
 # ids and sort scratch, seven packed vectors (positions and velocities of two
 # stages, force factors, heat factors, the force pass's neighbour record),
 # staging.
-def bytes_per_particle(precision="mixed", integrator="ieuler", cluster=False):
+def bytes_per_particle(precision="mixed", integrator="ieuler", cluster=False, lists=0):
+    """HBM an engine holds per particle of capacity.  lists = the dimension
+    of a group on per-particle pair lists (0: none)."""
     rs = 4 if precision == "mixed" else 8
     v4 = 4 * rs
     b = 3 * 8 * 8 + 9 * rs + 5 * 8 + 9 * 4 + 7 * v4 + 10 * rs + 8 * 8
@@ -49,6 +51,12 @@ def bytes_per_particle(precision="mixed", integrator="ieuler", cluster=False):
         # lists: 1.4 times the longest, about 415 entries of 8 B per cluster
         # of 8 in a fluid at n = 0.7 (denser fluids need proportionally more)
         b += 72 + 16 + 16 + 440
+    if lists and precision == "mixed":
+        # pair lists (csrc/sph_vlist.cu): rows of 1.25 times the longest
+        # list of 4-byte entries -- about 180 in the served 2D fluid (spacing
+        # 1, cutoff 6) and 600 in the 3D one (n = 0.7, cutoff 5.148) -- the
+        # counts and the build positions
+        b += 4 * (180 if lists == 2 else 600) + 4 + 16
     return b
 
 
@@ -214,22 +222,26 @@ class Server:
 
     def __init__(self, hbm_budget_bytes, precision="mixed", chunk=25, max_sims=256,
                  share_2d=0.6, engine_factory=default_engine_factory, clock=time.perf_counter,
-                 streams=None, group_params=None, pair_scheme_3d=1):
-        """pair_scheme_3d: the 3D group's pair scheme (1: cluster pairs, whose
-        tables and lists count against the group's share of the budget)."""
+                 streams=None, group_params=None, pair_scheme_3d=1, pair_scheme_2d=0):
+        """pair_scheme_2d / _3d: each group's pair scheme.  The defaults (cell
+        windows; cluster pairs, whose tables and lists count against the
+        group's share of the budget) give every job the bits it would have
+        alone; pair lists (2) are faster, and a job's results then follow
+        the engine's list builds (equal to the job alone to rounding)."""
         self.precision = precision
         self.chunk = chunk
         self.clock = clock
         self.hbm_budget = float(hbm_budget_bytes)
-        self.bpp = {2: bytes_per_particle(precision),
-                    3: bytes_per_particle(precision, cluster=pair_scheme_3d == 1)}
+        self.bpp = {2: bytes_per_particle(precision, lists=2 if pair_scheme_2d == 2 else 0),
+                    3: bytes_per_particle(precision, cluster=pair_scheme_3d == 1,
+                                          lists=3 if pair_scheme_3d == 2 else 0)}
         caps = {2: hbm_budget_bytes * share_2d / self.bpp[2],
                 3: hbm_budget_bytes * (1 - share_2d) / self.bpp[3]}
         if group_params is None:
             group_params = {2: make_job(0, 0.0, 2, 256, 1, 1).params,
                             3: make_job(0, 0.0, 3, 1000, 1, 2).params}
         streams = streams or {2: None, 3: None}
-        schemes = {2: 0, 3: pair_scheme_3d}
+        schemes = {2: pair_scheme_2d, 3: pair_scheme_3d}
         self.groups = {d: Group(d, group_params[d], caps[d], max_sims, precision, chunk,
                                 engine_factory, streams[d], schemes[d]) for d in (2, 3)}
         self.rejected = []

@@ -264,3 +264,25 @@ def test_nan_job_does_not_disturb_the_mix():
         alone = run_alone(job)
         for a, b in zip(alone, job.result):
             assert np.array_equal(a, b), job.job_id
+
+
+@pytest.mark.gpu
+def test_served_on_pair_lists_match_alone_to_rounding():
+    """Both groups on pair lists: every job completes, and its state equals
+    the same job run alone on lists to rounding (the list builds follow the
+    engine, not the job)."""
+    from pyticles_gb300 import Engine
+    jobs = small_jobs(seed=83)
+    srv = Server(2e9, chunk=10, max_sims=8, pair_scheme_2d=2, pair_scheme_3d=2)
+    rep = srv.run(jobs, realtime=False)
+    srv.close()
+    assert rep["completed"] == len(jobs) and rep["failed"] == 0
+    for job in jobs:
+        with Engine(job.params, "mixed", max_particles=job.n) as e:
+            s = e.add(job.params, job.r, job.v, job.m, job.u)
+            e.set_tuning(pair_scheme=2)
+            e.advance(job.steps)
+            e.sync()
+            alone = e.get_state(s)
+        for a, b in zip(alone, job.result):
+            assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(a), job.job_id
