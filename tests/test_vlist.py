@@ -351,3 +351,28 @@ def test_lists_grow_with_a_denser_state():
         ref = oracle.derivatives(prm, r, v, m, u)
         for k in ("rho", "vdot", "udot"):
             assert rel_l2(d[k], ref[k]) < MIXED_TOL, k
+
+
+def test_lists_follow_simulations_joining_and_leaving():
+    """Simulations added to and removed from an engine on lists between
+    advances (a new layout each time, the rows measured again): each one
+    tracks the oracle's trajectory."""
+    sims = workloads.batched_2d(3, seed_base=4300, n_lo=256, n_hi=2048, ramp_steps=10)
+    st = [(p, r, v, m, oracle.initial_energy(p, r, v, m, T)) for p, r, v, m, T in sims]
+    total = sum(len(x[1]) for x in st)
+    with Engine(st[0][0], "mixed", max_particles=total, max_sims=3) as e:
+        e.set_tuning(pair_scheme=2)
+        a = e.add(*st[0])
+        b = e.add(*st[1])
+        e.advance(3)
+        e.remove(b)
+        c = e.add(*st[2])
+        e.advance(3)
+        e.sync()
+        assert lists_in_use(e)
+        ra = e.get_state(a)
+        rc = e.get_state(c)
+    for got, (p, r, v, m, u), steps in ((ra, st[0], 6), (rc, st[2], 3)):
+        ref = oracle.advance(p, r, v, m, u, steps)[:3]
+        for x, y in zip(got, ref):
+            assert rel_l2(x, y) < MIXED_TOL
