@@ -831,16 +831,22 @@ struct ProfScope {
     cudaStream_t st;
     int kind;
     cudaEvent_t b = nullptr;
+    unsigned flags = cudaEventRecordDefault;
     ProfScope(sph_engine *e_, int kind_, cudaStream_t st_) : e(e_), st(st_), kind(kind_) {
         if (!e->prof_on || e->prof_used + 2 > e->prof_pool.size()) return;
         cudaEvent_t a = e->prof_pool[e->prof_used++];
         b = e->prof_pool[e->prof_used++];
-        // external record nodes when captured, so the events are timeable
-        cudaEventRecordWithFlags(a, st, cudaEventRecordExternal);
+        // external record nodes when captured, so the events are timeable;
+        // plain records for the eager steps of an advance (the external
+        // flag is refused outside a capture)
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &cs);
+        if (cs == cudaStreamCaptureStatusActive) flags = cudaEventRecordExternal;
+        cudaEventRecordWithFlags(a, st, flags);
         e->prof_recs.push_back({kind, a, b});
     }
     ~ProfScope() {
-        if (b) cudaEventRecordWithFlags(b, st, cudaEventRecordExternal);
+        if (b) cudaEventRecordWithFlags(b, st, flags);
     }
 };
 

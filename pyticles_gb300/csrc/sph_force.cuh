@@ -320,8 +320,11 @@ __global__ void __launch_bounds__(256, (ONE && D == 2) ? 5 : 4) k_force(const __
 #ifndef SPH_VL_FORCE3_BLOCKS
 #define SPH_VL_FORCE3_BLOCKS 4
 #endif
+#ifndef SPH_VL_FORCE_MULTI_BLOCKS
+#define SPH_VL_FORCE_MULTI_BLOCKS 4
+#endif
 template <int D, int K, int VH, bool ONE>
-__global__ void __launch_bounds__(256, ONE ? (D == 2 ? SPH_VL_FORCE_BLOCKS : SPH_VL_FORCE3_BLOCKS) : 4)
+__global__ void __launch_bounds__(256, ONE ? (D == 2 ? SPH_VL_FORCE_BLOCKS : SPH_VL_FORCE3_BLOCKS) : SPH_VL_FORCE_MULTI_BLOCKS)
     k_force_vl(const __grid_constant__ View v, int stage, int mode, int integ) {
     force_one<float, D, K, VH, ONE, true>(v, stage, mode, integ,
                                           blockIdx.x * blockDim.x + threadIdx.x);

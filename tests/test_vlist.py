@@ -376,3 +376,23 @@ def test_lists_follow_simulations_joining_and_leaving():
         ref = oracle.advance(p, r, v, m, u, steps)[:3]
         for x, y in zip(got, ref):
             assert rel_l2(x, y) < MIXED_TOL
+
+
+def test_profiled_advance_with_eager_steps():
+    """Per-pass profiling over an advance that ends in eager steps (50 steps
+    in graph chunks of 17: two graphs and 16 steps enqueued one by one) on
+    pair lists: no error, every pass timed."""
+    prm, r, v, m, T0 = workloads.config_2d(32, 1006, viscosity=True)
+    u = oracle.initial_energy(prm, r, v, m, T0)
+    with listed(prm, r, v, m, u) as e:
+        s = e.add(prm, r, v, m, u)
+        e.set_tuning(steps_per_graph=50)
+        e.advance(50)
+        e.sync()
+        e.profile(True)
+        e.advance(50)
+        e.sync()
+        prof = e.profile_read()
+        e.profile(False)
+        assert prof["force"]["launches"] > 0 and prof["force"]["ms"] > 0
+        assert prof["density"]["launches"] == prof["force"]["launches"]
