@@ -376,11 +376,32 @@ def accuracy_track(prm, r, v, m, u, steps, every, stream, knobs=None):
                    # of this workload (one evaluation = its pair count)
                    "oracle_eval": {"value": ref["nip"] / t_ref, "unit": UNIT,
                                    "seconds": t_ref, "cores": oracle.threads(),
-                                   "kind": "port"}}
+                                   "cpu": cpu_model(), "kind": "port"}}
             for k in ("rho", "vdot", "udot"):
                 row[k] = float(np.linalg.norm(g[k] - ref[k]) / np.linalg.norm(ref[k]))
             out.append(row)
     return out
+
+
+def cpu_model():
+    """The host CPU as /proc/cpuinfo names it (model name, else the Arm
+    implementer/part codes), else the machine type."""
+    import platform
+    try:
+        info = open("/proc/cpuinfo").read().splitlines()
+    except OSError:
+        info = []
+    fields = {}
+    for line in info:
+        if ":" in line:
+            k, _, val = line.partition(":")
+            fields.setdefault(k.strip(), val.strip())
+    if fields.get("model name"):
+        return fields["model name"]
+    if fields.get("CPU part"):
+        return (f"{platform.machine()} (CPU implementer {fields.get('CPU implementer', '?')}, "
+                f"part {fields['CPU part']})")
+    return platform.processor() or platform.machine()
 
 
 def oracle_rate(side, seed, budget_s, max_steps):
@@ -429,7 +450,7 @@ def reference_arm(args):
                        "evals_per_step": 2, "precision": "fp64 (the reference's arithmetic)",
                        "sample": {"n": len(r), "pairs_per_eval": nip}},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.threads(),
-                             "kind": "port", "sample": sample},
+                             "cpu": cpu_model(), "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -615,7 +636,7 @@ def main():
     if rank == 0 and not args.no_cpu:
         rate, csteps, ct, cores, cn = oracle_rate(min(args.side, 512), 1000, args.cpu_seconds,
                                                   50)
-        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
                "sample": f"FP64 C oracle, 2D vdW fluid N={cn}, {csteps} improved-Euler steps, "
                          f"{ct:.1f} s"}
     if rank != 0:
