@@ -197,32 +197,39 @@ def batched_workload(nsims, ramp_steps=500):
 
 
 def batched_arm(sims, steps, torch, stream, dist=None):
-    """The batched workload timed with one thread per particle and as
-    persistent launches (tuning.persistent) over the flattened table, after
-    autotuning the other knobs on a sample; the faster is the arm's value.
-    Under torchrun each rank runs its round-robin share of the simulations
-    (replicas.shard); the work adds up over the slowest rank's time."""
+    """The batched workload after autotuning the knobs on a sample.  The cell
+    windows are timed with one thread per particle ("grid") and as
+    persistent launches (tuning.persistent) over the flattened table, and
+    the pair lists ("lists", which launch one thread per particle) when the
+    tuner chose them; the fastest is the arm's value.  Under torchrun each
+    rank runs its round-robin share of the simulations (replicas.shard); the
+    work adds up over the slowest rank's time."""
     from pyticles_gb300 import replicas
     from pyticles_gb300 import autotune
     knobs, _ = autotune.tune(sims[0][0], "mixed", autotune.sample_sims(sims, 1 << 20), steps=3,
                              warmup=2)
-    variants = {}
-    for persistent in (0, 1):
-        k = dict(knobs, rebin=0, persistent=persistent)
+    forms = {"grid": dict(knobs, rebin=0, persistent=0, pair_scheme=0),
+             "persistent": dict(knobs, rebin=0, persistent=1, pair_scheme=0)}
+    if knobs.get("pair_scheme") == 2:
+        forms["lists"] = dict(knobs, rebin=0, persistent=0)
+    variants, used = {}, {}
+    for name, k in forms.items():
         ms, pairs, passes, kps = run_timed(None, None, None, None, None, "mixed", steps, 3,
                                            torch, stream, knobs=k, sims=sims)
         ms, pairs = replicas.combine(ms, pairs, dist, device="cuda")
-        variants["persistent" if persistent else "grid"] = {
+        variants[name] = {
             "ms_per_step": ms / steps, "value": pairs * 2 * steps / (ms * 1e-3),
             "pass_ms_per_step": {kk: p["ms"] / steps for kk, p in passes.items()},
             "pairs_per_eval": pairs}
+        used[name] = {kk: k[kk] for kk in ("block_size", "cell_ratio", "pair_scheme",
+                                            "persistent") if kk in k}
     best = min(variants, key=lambda name: variants[name]["ms_per_step"])
     b = variants[best]
     nall = replicas.combine(0.0, sum(len(x[1]) for x in sims), dist, device="cuda")[1]
     sall = replicas.combine(0.0, len(sims), dist, device="cuda")[1]
     return {"sims": int(sall), "n": int(nall), "steps": steps,
             "ms_per_step": b["ms_per_step"], "pairs_per_eval": b["pairs_per_eval"],
-            "value": b["value"], "unit": UNIT, "tuning": dict(knobs, persistent=int(best == "persistent")),
+            "value": b["value"], "unit": UNIT, "tuning": used[best],
             "launch": best, "variants": variants,
             "pass_ms_per_step": b["pass_ms_per_step"]}
 
@@ -232,8 +239,9 @@ def batched_accuracy(sims, steps, stream, knobs):
     largest simulation of the batch, each advanced `steps` steps from the
     same initial state (the quench included): relative L2 of r, v, u after
     the steps, and of rho, vdot, udot of one evaluation at the GPU's final
-    state.  A simulation gives the same bits alone as in the batch, so the
-    three run in their own engine."""
+    state.  The three run in an engine of their own (on cell windows a
+    simulation gives the same bits there as in the full batch; on pair
+    lists the same to rounding)."""
     from oracle import oracle
     from pyticles_gb300 import Engine
     order = sorted(range(len(sims)), key=lambda k: len(sims[k][1]))
