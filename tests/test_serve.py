@@ -286,3 +286,17 @@ def test_served_on_pair_lists_match_alone_to_rounding():
             alone = e.get_state(s)
         for a, b in zip(alone, job.result):
             assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(a), job.job_id
+
+
+def test_budget_counts_the_pair_lists():
+    """A group on pair lists counts their rows against the HBM budget: the
+    2D fluid's lists (about 180 entries of 4 bytes) and the 3D fluid's
+    (about 600), plus counts and build positions; FP64 engines have none."""
+    base = serve.bytes_per_particle("mixed")
+    assert serve.bytes_per_particle("mixed", lists=2) == base + 4 * 180 + 20
+    assert serve.bytes_per_particle("mixed", lists=3) == base + 4 * 600 + 20
+    assert serve.bytes_per_particle("fp64", lists=2) == serve.bytes_per_particle("fp64")
+    srv = Server(1e9, share_2d=0.5, engine_factory=FakeEngine, clock=FakeClock(),
+                 group_params={2: None, 3: None}, pair_scheme_2d=2, pair_scheme_3d=2)
+    assert srv.groups[2].capacity == int(0.5e9 / (base + 740))
+    assert srv.groups[3].capacity == int(0.5e9 / (base + 2420))
