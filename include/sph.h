@@ -246,8 +246,8 @@ typedef struct sph_tuning {
                                  neighbour_list.py:160-234); the passes walk
                                  the lists and still apply the exact pair test
                                  at every evaluation.  Mixed-precision
-                                 engines (2D, or 3D up to 8.4 M particles)
-                                 without collisions whose boxes span at least
+                                 engines (up to 67 M particles in 2D, 8.4 M
+                                 in 3D) without collisions whose boxes span at least
                                  2W+1 cells per axis (W <= 3); otherwise cell
                                  windows.  Bins on demand like rebin = 1 for
                                  improved Euler and RK4, so the summation
